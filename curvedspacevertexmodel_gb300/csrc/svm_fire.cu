@@ -1,0 +1,308 @@
+// FIRE energy minimisation over velocity Verlet with every decision on the device.
+//
+// Restates energyMinimizerFIRE::minimize / fireStepCPU (src/updaters/energyMinimizerFIRE.cpp:
+// 122-200) and velocityVerlet::integrateEOMCPU (src/updaters/velocityVerlet.cpp:6-38).  One
+// iteration is
+//   k_fire_vv1     per vertex: the previous iteration's FIRE velocity update, then
+//                  disp = dt v + dt^2/2 F, v += dt/2 F / m, move onto the sphere (in place)
+//   [T1]           unless motion is restricted
+//   geometry       k_corners, k_cells, k_fallback
+//   k_fire_force   per vertex: F, v += dt/2 F / m, block partials of F.v, F.F, v.v, max |F|^2;
+//                  the last block reduces them in a fixed order and runs the FIRE control
+//                  (power test, dt / alpha adaptation, stopping test)
+// The host launches captured batches of iterations and reads only the `done` flag between them.
+#include <cstdio>
+#include <vector>
+#include "svm_internal.cuh"
+#include "svm_force.cuh"
+
+using namespace svm;
+
+struct FireState {
+    double dt, alpha, alphaUsed, scaling, power, forceNorm, velNorm, maxF2, rmsOverN, maxForce;
+    double dtMin, dtMax, dtInc, dtDec, alphaStart, alphaDec, alphaMin, cutoff;
+    int nMin, nSince, iterations, maxIterations, criterion, done, pending, zeroV;
+};
+
+struct svm_fire {
+    svm_model* m = nullptr;
+    FireState* d = nullptr;
+    FireState h{};
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    int nBlocks = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graphCriterion = -1;
+    int graphIters = 0;
+    int graphCur = -1;
+    unsigned graphVersion = ~0u;
+};
+
+namespace {
+
+constexpr int kB = 256;
+
+__device__ double bsum(double v, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+    __syncthreads();
+    return r;
+}
+__device__ double bmax(double v, double* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ D3 move_exact_f(D3 p, D3 v, double R) {
+    const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
+    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
+    const double s = vp / pp;
+    D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
+         __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
+    const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
+    const double inv = 1.0 / sqrt(qq);
+    return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
+}
+
+// FIRE velocity update of fireStepCPU (energyMinimizerFIRE.cpp:146-149, 168-172).
+__device__ __forceinline__ D3 fire_velocity(const FireState& S, D3 v, D3 f) {
+    if (S.zeroV) return D3{0.0, 0.0, 0.0};
+    const double a1 = 1.0 - S.alphaUsed, as = S.alphaUsed * S.scaling;
+    return D3{__dadd_rn(__dmul_rn(a1, v.x), __dmul_rn(as, f.x)), __dadd_rn(__dmul_rn(a1, v.y), __dmul_rn(as, f.y)),
+              __dadd_rn(__dmul_rn(a1, v.z), __dmul_rn(as, f.z))};
+}
+
+__global__ void k_fire_vv1(const FireState* __restrict__ Sp, double4_32a* __restrict__ pos,
+                           double4_32a* __restrict__ vel, const double4_32a* __restrict__ force, int nV, double R) {
+    const FireState S = *Sp;
+    if (S.done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    const D3 f = ld3(force, i);
+    D3 v = ld3(vel, i);
+    if (S.pending) v = fire_velocity(S, v, f);
+    const double dt = S.dt, hv = (0.5 / 1.0) * dt, h2 = 0.5 * dt * dt;
+    const D3 d{__dadd_rn(__dmul_rn(dt, v.x), __dmul_rn(h2, f.x)), __dadd_rn(__dmul_rn(dt, v.y), __dmul_rn(h2, f.y)),
+               __dadd_rn(__dmul_rn(dt, v.z), __dmul_rn(h2, f.z))};
+    v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
+    st3(vel, i, v);
+    st3(pos, i, move_exact_f(ld3(pos, i), d, R));
+}
+
+// Clears the pending flag after the first vertex kernel of an iteration has consumed it.
+__global__ void k_fire_consume(FireState* S) {
+    if (!S->done) S->pending = 0;
+}
+
+__global__ void k_fire_force(ForceArgs A, FireState* __restrict__ Sp, int nV, double4_32a* __restrict__ force,
+                             double4_32a* __restrict__ vel, double* __restrict__ partials, unsigned* __restrict__ ticket) {
+    __shared__ double sh[32];
+    __shared__ bool amLast;
+    if (Sp->done) return;
+    const double dt = Sp->dt;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double P = 0.0, FF = 0.0, VV = 0.0;
+    if (i < nV) {
+        const D3 f = vertex_force(A, i);
+        st3(force, i, f);
+        const double hv = (0.5 / 1.0) * dt;
+        D3 v = ld3(vel, i);
+        v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
+        st3(vel, i, v);
+        P = __dadd_rn(__dadd_rn(__dmul_rn(f.x, v.x), __dmul_rn(f.y, v.y)), __dmul_rn(f.z, v.z));
+        FF = __dadd_rn(__dadd_rn(__dmul_rn(f.x, f.x), __dmul_rn(f.y, f.y)), __dmul_rn(f.z, f.z));
+        VV = __dadd_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), __dmul_rn(v.z, v.z));
+    }
+    const double bP = bsum(P, sh), bF = bsum(FF, sh), bV = bsum(VV, sh), bM = bmax(FF, sh);
+    if (threadIdx.x == 0) {
+        double* q = partials + 4 * blockIdx.x;
+        q[0] = bP; q[1] = bF; q[2] = bV; q[3] = bM;
+        __threadfence();
+        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!amLast) return;
+    double sP = 0.0, sF = 0.0, sV = 0.0, sM = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        sP += __ldcg(partials + 4 * b); sF += __ldcg(partials + 4 * b + 1);
+        sV += __ldcg(partials + 4 * b + 2); sM = fmax(sM, __ldcg(partials + 4 * b + 3));
+    }
+    const double tP = bsum(sP, sh), tF = bsum(sF, sh), tV = bsum(sV, sh), tM = bmax(sM, sh);
+    if (threadIdx.x == 0) {
+        FireState S = *Sp;
+        S.power = tP; S.forceNorm = tF; S.velNorm = tV; S.maxF2 = tM;
+        S.rmsOverN = sqrt(tF) / (double)nV;
+        S.maxForce = sqrt(tM);
+        S.scaling = tF > 0. ? sqrt(tV / tF) : 0.0;
+        S.alphaUsed = S.alpha;
+        S.zeroV = tP > 0 ? 0 : 1;
+        if (tP > 0) {
+            if (S.nSince > S.nMin) {
+                S.dt = fmin(S.dt * S.dtInc, S.dtMax);
+                S.alpha = S.alpha * S.alphaDec;
+                S.alpha = fmax(S.alpha, S.alphaMin);
+            }
+            S.nSince += 1;
+        } else {
+            S.nSince = 0;
+            S.dt = S.dt * S.dtDec;
+            S.dt = fmax(S.dt, S.dtMin);
+            S.alpha = S.alphaStart;
+        }
+        S.iterations += 1;
+        S.pending = 1;
+        const double crit = S.criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
+        if (S.iterations >= S.maxIterations || !(crit > S.cutoff)) S.done = 1;
+        *Sp = S;
+        *ticket = 0u;
+    }
+}
+
+// Applies a pending FIRE velocity update (after the loop ends).
+__global__ void k_fire_finish(FireState* __restrict__ Sp, double4_32a* __restrict__ vel,
+                              const double4_32a* __restrict__ force, int nV) {
+    const FireState S = *Sp;
+    if (!S.pending) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    st3(vel, i, fire_velocity(S, ld3(vel, i), ld3(force, i)));
+}
+__global__ void k_fire_clear_pending(FireState* Sp) { Sp->pending = 0; }
+
+ForceArgs fargs(svm_model* m) {
+    ForceArgs A;
+    A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
+    A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
+    return A;
+}
+
+int fire_iteration(svm_fire* F) {
+    svm_model* m = F->m;
+    const int nb = (m->nVertices + kB - 1) / kB;
+    k_fire_vv1<<<nb, kB, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
+    k_fire_consume<<<1, 1, 0, m->stream>>>(F->d);
+    m->cornersValid = false;
+    int rc;
+    if (!m->restricted) {
+        rc = launch_corners(m, true);
+        if (rc) return rc;
+        rc = launch_t1_apply(m);
+        if (rc) return rc;
+    }
+    rc = launch_geometry(m);
+    if (rc) return rc;
+    k_fire_force<<<nb, kB, 0, m->stream>>>(fargs(m), F->d, m->nVertices, m->force, m->vel, F->partials, F->ticket);
+    return check_launch();
+}
+
+}  // namespace
+
+extern "C" {
+
+int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, double dtInc, double dtDec,
+                    double alphaDec, int nMin, double forceCutoff, double alphaMin, int maxIterations, svm_fire** out) {
+    if (!m || !out || !(dt > 0) || maxIterations < 0) return SVM_ERR_ARG;
+    svm_fire* F = new svm_fire();
+    F->m = m;
+    FireState& S = F->h;
+    S = FireState{};
+    S.dt = dt; S.dtMin = dt * .01; S.alphaStart = alphaStart; S.alpha = alphaStart; S.dtMax = dtMax;
+    S.dtInc = dtInc; S.dtDec = dtDec; S.alphaDec = alphaDec; S.nMin = nMin; S.cutoff = forceCutoff;
+    S.alphaMin = alphaMin; S.maxIterations = maxIterations; S.rmsOverN = 100.; S.maxForce = 100.;
+    F->nBlocks = (m->nVertices + kB - 1) / kB;
+    bool ok = cudaMalloc(&F->d, sizeof(FireState)) == cudaSuccess &&
+              cudaMalloc(&F->partials, sizeof(double) * 4 * (F->nBlocks + 1)) == cudaSuccess &&
+              cudaMalloc(&F->ticket, sizeof(unsigned)) == cudaSuccess;
+    if (!ok) { svm_fire_destroy(F); return SVM_ERR_CUDA; }
+    cudaMemsetAsync(F->ticket, 0, sizeof(unsigned), m->stream);
+    cudaMemcpyAsync(F->d, &S, sizeof(FireState), cudaMemcpyHostToDevice, m->stream);
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) { svm_fire_destroy(F); return SVM_ERR_CUDA; }
+    *out = F;
+    return SVM_OK;
+}
+
+int svm_fire_destroy(svm_fire* F) {
+    if (!F) return SVM_ERR_ARG;
+    if (F->m && F->m->stream) cudaStreamSynchronize(F->m->stream);
+    if (F->graph) cudaGraphExecDestroy(F->graph);
+    if (F->d) cudaFree(F->d);
+    if (F->partials) cudaFree(F->partials);
+    if (F->ticket) cudaFree(F->ticket);
+    delete F;
+    return SVM_OK;
+}
+
+int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value) {
+    if (!F) return SVM_ERR_ARG;
+    svm_model* m = F->m;
+    FireState S;
+    if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    const int it0 = S.iterations;
+    S.criterion = criterion;
+    S.done = S.iterations >= S.maxIterations ? 1 : 0;
+    S.rmsOverN = 110.0; S.maxForce = 110.0;  // minimize() restarts the stopping test (cpp:187)
+    cudaMemcpyAsync(F->d, &S, sizeof(FireState), cudaMemcpyHostToDevice, m->stream);
+    int rc = svm_model_compute_forces(m);  // sim->computeForces() before the loop (cpp:186)
+    if (rc) return rc;
+    // iterations in captured batches; kernels of a batch after convergence return at once
+    const int batch = 32;
+    if (!F->graph || F->graphCriterion != criterion || F->graphIters != batch || F->graphCur != m->cur ||
+        F->graphVersion != m->paramsVersion) {
+        if (F->graph) { cudaGraphExecDestroy(F->graph); F->graph = nullptr; }
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SVM_ERR_CUDA;
+        int r = SVM_OK;
+        for (int k = 0; k < batch && !r; ++k) r = fire_iteration(F);
+        cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
+        if (r || ce != cudaSuccess) { cudaGetLastError(); return SVM_ERR_CUDA; }
+        ce = cudaGraphInstantiate(&F->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { F->graph = nullptr; return SVM_ERR_CUDA; }
+        F->graphCriterion = criterion;
+        F->graphIters = batch;
+        F->graphCur = m->cur;
+        F->graphVersion = m->paramsVersion;
+    }
+    int* doneHost = nullptr;
+    cudaMallocHost(&doneHost, sizeof(int));
+    while (true) {
+        if (cudaGraphLaunch(F->graph, m->stream) != cudaSuccess) { cudaFreeHost(doneHost); return SVM_ERR_CUDA; }
+        cudaMemcpyAsync(doneHost, &F->d->done, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+        if (cudaStreamSynchronize(m->stream) != cudaSuccess) { cudaFreeHost(doneHost); return SVM_ERR_CUDA; }
+        if (*doneHost) break;
+    }
+    cudaFreeHost(doneHost);
+    const int nb = (m->nVertices + kB - 1) / kB;
+    k_fire_finish<<<nb, kB, 0, m->stream>>>(F->d, m->vel, m->force, m->nVertices);
+    k_fire_clear_pending<<<1, 1, 0, m->stream>>>(F->d);
+    if (check_launch()) return SVM_ERR_CUDA;
+    if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    F->h = S;
+    if (iterations) *iterations = S.iterations - it0;
+    if (value) *value = criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
+    return SVM_OK;
+}
+
+int svm_fire_state(svm_fire* F, double* s7) {
+    if (!F || !s7) return SVM_ERR_ARG;
+    FireState S;
+    if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, F->m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(F->m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    s7[0] = S.dt; s7[1] = S.alpha; s7[2] = S.power; s7[3] = S.rmsOverN; s7[4] = S.maxForce;
+    s7[5] = S.nSince; s7[6] = S.iterations;
+    return SVM_OK;
+}
+
+}  // extern "C"

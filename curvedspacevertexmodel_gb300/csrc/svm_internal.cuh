@@ -1,0 +1,203 @@
+// Internal state and FP64 device math of libsvm.
+//
+// Device layout (structure of arrays, one GPU):
+//   pos[2]      double4_32a[Nv]   vertex positions (x,y,z,0); two buffers so the fused
+//                             force+integrate+move kernel reads old and writes new positions
+//   vsph        double4_32a[Nv]   per-vertex spherical coordinates (cos t, sin t, cos p, sin p)
+//   vcell/vnbr  int4[Nv]      vertex->cell and vertex->vertex slots (w unused)
+//   vlast/vnext int4[Nv]      ring predecessor / successor of the vertex in each of its cells
+//   vrpos       int4[Nv]      position of the vertex in each of its cells' rings
+//   ring        int[N*Wc]     clockwise ring of each cell, capacity Wc; ringCount int[N]
+//   corner      double2[N*Wc] per ring position k: (arc(ring[k-1], ring[k]), included angle at k)
+//   cellPos     double4_32a[N]    renormalised ring centroid; cellSph double4_32a[N] its (cos t, ...)
+//   ap, pref    double2[N]    (area, perimeter) and (A0, P0)
+//   force, vel  double4_32a[Nv]
+// The reference keeps AoS double[3] vertices and scatters (last, cur, next) vertex copies into
+// per-(vertex, cell) slots every step (src/model/sphericalVertexModel.cu:94-96); here the force
+// kernel gathers them through vlast/vnext instead, which removes 3 x 24 B x 3Nv of writes.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/svm.h"
+
+namespace svm {
+
+constexpr double kPI = 3.141592653589793115997963468544185161590576171875;
+
+struct D3 { double x, y, z; };
+
+__device__ __forceinline__ D3 ld3(const double4_32a* p, int i) {
+    double4_32a t = p[i];
+    return D3{t.x, t.y, t.z};
+}
+__device__ __forceinline__ void st3(double4_32a* p, int i, D3 v) { p[i] = make_double4_32a(v.x, v.y, v.z, 0.0); }
+__device__ __forceinline__ D3 add3(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 sub3(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 scl3(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
+// dot (inc/functions.h:131-138): accumulated in component order
+__device__ __forceinline__ double dot3(D3 a, D3 b) { double s = a.x * b.x; s += a.y * b.y; s += a.z * b.z; return s; }
+__device__ __forceinline__ D3 cross3(D3 p1, D3 p2) {          // inc/functions.h:160-167
+    return D3{p1.y * p2.z - p1.z * p2.y, p1.z * p2.x - p1.x * p2.z, p1.x * p2.y - p1.y * p2.x};
+}
+__device__ __forceinline__ double det3(D3 a, D3 b, D3 c) {    // a . (b x c), sphericalDomain.h:123-125
+    return a.x * (b.y * c.z - b.z * c.y) + a.y * (b.z * c.x - b.x * c.z) + a.z * (b.x * c.y - b.y * c.x);
+}
+
+// putInBoxReal (sphericalDomain.h:183-187): p <- R p / |p|
+__device__ __forceinline__ D3 renorm(D3 p, double R) {
+    double inv = 1.0 / sqrt(dot3(p, p));
+    return scl3(R, scl3(inv, p));
+}
+// move(p, v) (sphericalDomain.h:203-209): project v onto the tangent plane at p, add, renormalise
+__device__ __forceinline__ D3 sphere_move(D3 p, D3 v, double R) {
+    double s = dot3(v, p) / dot3(p, p);
+    D3 d = sub3(v, scl3(s, p));
+    return renorm(add3(p, d), R);
+}
+// geodesicDistance (sphericalDomain.h:94-112)
+__device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
+    double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
+    double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    return R * acos(num / den);
+}
+// includedAngle (sphericalDomain.h:114-133)
+__device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
+    D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
+    double det = det3(p1, p2, p3);
+    double a = acos(-dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1))));
+    if (det > 0) a = -a;
+    if (a < 0) a += 2. * kPI;
+    return a;
+}
+// sphericalTriangleArea (sphericalDomain.h:135-166)
+__device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
+    D3 p1 = scl3(1.0 / sqrt(dot3(q1, q1)), q1), p2 = scl3(1.0 / sqrt(dot3(q2, q2)), q2),
+       p3 = scl3(1.0 / sqrt(dot3(q3, q3)), q3);
+    double d12 = dot3(p1, p2), d13 = dot3(p1, p3), d23 = dot3(p2, p3);
+    double area = -kPI;
+    area += acos((d23 - d12 * d13) / (sqrt(1 - d12 * d12) * sqrt(1 - d13 * d13)));
+    area += acos((d12 - d13 * d23) / (sqrt(1 - d13 * d13) * sqrt(1 - d23 * d23)));
+    area += acos((d13 - d12 * d23) / (sqrt(1 - d12 * d12) * sqrt(1 - d23 * d23)));
+    return area * (R * R);
+}
+
+// Spherical coordinates of a point as the reference's gradients compute them
+// (sphericalDomain.h:218-232, 251-261): cos t = z/|p|, sin t = sqrt(1 - cos^2 t),
+// cos p = x / sqrt(x^2+y^2), sin p = y / sqrt(x^2+y^2).
+__device__ __forceinline__ double4_32a sph_coords(D3 p) {
+    double r = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+    double cosT = p.z / r;
+    double sinT = sqrt(1. - cosT * cosT);
+    double rxy = sqrt(p.x * p.x + p.y * p.y);
+    return make_double4_32a(cosT, sinT, p.x / rxy, p.y / rxy);
+}
+
+// gradientGeodesicDistance (sphericalDomain.h:248-273) in the (theta, phi) basis of v1:
+// returns (d/dtheta, d/dphi) components.
+__device__ __forceinline__ double2 grad_geodesic(double4_32a s1, double4_32a s2) {
+    double sP12 = s1.w * s2.z - s1.z * s2.w;
+    double cP12 = s1.z * s2.z + s1.w * s2.w;
+    double dp = s1.x * s2.x + cP12 * s1.y * s2.y;
+    double dinv = 1. / sqrt(1 - dp * dp);
+    double gT = 1.0 * (s2.x * s1.y - s1.x * cP12 * s2.y) * dinv;
+    double gP = s2.y * sP12 * dinv;
+    return make_double2(gT, gP);
+}
+
+// gradientTriangleArea (sphericalDomain.h:347-411) in the (theta, phi) basis of v1; the sign
+// follows det(v1, v2, v3).  Returns (d/dtheta, d/dphi) components.
+__device__ __forceinline__ double2 grad_triangle(double4_32a a, double4_32a b, double4_32a c, D3 v1, D3 v2, D3 v3, double R) {
+    double sP12 = a.w * b.z - a.z * b.w;
+    double sP13 = a.w * c.z - a.z * c.w;
+    double cP12 = a.z * b.z + a.w * b.w;
+    double cP13 = a.z * c.z + a.w * c.w;
+    double cP23 = b.z * c.z + b.w * c.w;
+    double s12 = a.x * b.x + cP12 * a.y * b.y;
+    double s13 = a.x * c.x + cP13 * a.y * c.y;
+    double s23 = b.x * c.x + cP23 * b.y * c.y;
+    double d12 = a.x * cP12 * b.y - b.x * a.y;
+    double d13 = a.x * cP13 * c.y - c.x * a.y;
+    double g = 1 - s12 * s12 - s13 * s13 - s23 * s23 + 2.0 * s12 * s13 * s23;
+    double q12 = (-1. + s12 * s12), q13 = (-1. + s13 * s13);
+    double den1 = sqrt(q12 * q12 * g);
+    double den2 = sqrt(q13 * q13 * g);
+    double den3 = sqrt((s12 * s12 - 1.) * (s13 * s13 - 1.) * (s12 * s12 - 1.) * (s13 * s13 - 1.) * g);
+    double gT = (d13 * (s12 * s12 - 1.0) + d12 * (s23 - s12 * s13)) / den1
+              + (d12 * (s13 * s13 - 1.0) + d13 * (s23 - s12 * s13)) / den2
+              - (d12 * (s13 * s13 - 1.) * (s13 - s12 * s23) + d13 * (s12 * s12 - 1.0) * (s12 - s13 * s23)) / den3;
+    gT *= R;
+    double gP = ((s12 * s13 - s23) * sP12 * b.y - (-1 + s12 * s12) * sP13 * c.y) / (den1)
+              - ((-1 + s13 * s13) * sP12 * b.y + (-(s12 * s13) + s23) * sP13 * c.y) / (den2)
+              + ((-1 + s13 * s13) * (s13 - s12 * s23) * sP12 * b.y + (-1 + s12 * s12) * (s12 - s13 * s23) * sP13 * c.y) / (den3);
+    gP *= R;
+    if (det3(v1, v2, v3) < 0) { gT = -gT; gP = -gP; }
+    return make_double2(gT, gP);
+}
+
+// (theta, phi) components to Cartesian with the basis of sphericalDomain.h:218-232:
+// thetaHat = (cos t cos p, cos t sin p, -sin t), phiHat = (-sin p, cos p, 0).
+__device__ __forceinline__ D3 from_basis(double4_32a s, double2 g) {
+    return D3{g.x * (s.x * s.z) + g.y * (-s.w), g.x * (s.x * s.w) + g.y * s.z, g.x * (-s.y) + g.y * 0};
+}
+
+// ---- host-side state -----------------------------------------------------------------------
+struct T1Scratch {
+    unsigned* bits = nullptr;      // one bit per (vertex, slot) position, 3*Nv bits
+    unsigned* summary = nullptr;   // one bit per word of `bits`
+    int* count = nullptr;          // number of candidate positions found by the test
+    int* flipLog = nullptr;        // (v1, v2) pairs, capacity flipLogCap
+    int* flipCount = nullptr;
+    int* touched = nullptr;        // cells whose rings changed during the apply kernel
+    int nWords = 0, nSummary = 0, flipLogCap = 0, touchedCap = 0;
+};
+
+}  // namespace svm
+
+struct svm_model {
+    int nCells = 0, nVertices = 0, Wc = 0;
+    double R = 1.0, Kr = 1.0, t1Threshold = 0.1;
+    bool restricted = false;
+    bool ownStream = false;
+    cudaStream_t stream = nullptr;
+    int cur = 0;                       // index of the current position buffer
+    bool cornersValid = false;         // corner/vsph arrays match the current state
+    double4_32a* pos[2] = {nullptr, nullptr};
+    double4_32a* vsph = nullptr;
+    int4 *vcell = nullptr, *vnbr = nullptr, *vlast = nullptr, *vnext = nullptr, *vrpos = nullptr;
+    int* ring = nullptr;
+    int* ringCount = nullptr;
+    double2* corner = nullptr;
+    double4_32a* cellPos = nullptr;
+    double4_32a* cellSph = nullptr;
+    double2* ap = nullptr;
+    double2* pref = nullptr;
+    double4_32a* force = nullptr;
+    double4_32a* vel = nullptr;
+    double* noiseBuf = nullptr;        // [3*Nv] staging for host-supplied noise / displacements
+    double* dispBuf = nullptr;         // [3*Nv]
+    // reductions: per-block partials + ticket (last-block-done pattern)
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    double* scalars = nullptr;         // [0] total area, [1] excess, [2] energy ...
+    int* fallbackFlag = nullptr;
+    int* status = nullptr;             // SVM_DEV_* bits
+    unsigned long long* stepCounter = nullptr;
+    svm::T1Scratch t1;
+    int maxPartialBlocks = 0;
+    // graph cache for svm_brownian_run
+    cudaGraphExec_t bdGraph = nullptr;
+    double bdT = 0, bdDt = 0, bdMu = 0;
+    uint64_t bdSeed = 0;
+    int bdGraphCur = -1;
+    // bumped by every setter whose value a captured graph bakes in (Kr, threshold, restriction)
+    unsigned paramsVersion = 0;
+    unsigned bdGraphVersion = ~0u;
+};
+
+namespace svm {
+// launch helpers shared across translation units (svm_model.cu)
+int launch_geometry(svm_model* m);
+int launch_corners(svm_model* m, bool t1test);
+int launch_t1_apply(svm_model* m);
+int check_launch();
+}  // namespace svm

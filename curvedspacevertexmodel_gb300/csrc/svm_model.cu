@@ -1,0 +1,1081 @@
+// Spherical vertex model on one GB300: geometry, forces, Brownian step, moves and T1 flips,
+// plus the model half of the C ABI declared in include/svm.h.
+//
+// Kernel sequence of one Brownian timestep (invariant: `corner` and `vsph` describe the current
+// positions and topology when a step starts):
+//   k_cells         per cell: centroid, area (spherical excess), perimeter, total-area check
+//   k_fallback      per cell: triangle-fan areas, only when the total area is off by > 1e-6
+//   k_force_bd      per vertex: force, Brownian displacement, move onto the sphere (new buffer)
+//   k_corners       per vertex: spherical coordinates, per-corner arc and angle, T1 edge test
+//   k_t1_apply      one block: the CPU's sequential T1 order over the flagged edges; patches
+//                   corners of every cell whose ring changed
+// None of them synchronises with the host, so a run of steps is captured as one CUDA graph.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include "svm_internal.cuh"
+#include "svm_force.cuh"
+#include "svm_hull.h"
+
+using namespace svm;
+
+namespace svm {
+
+constexpr int kBlock = 256;
+constexpr int kApplyThreads = 256;
+constexpr int kExtractCap = 1024;  // positions extracted per bitmap chunk (32 words)
+constexpr int kHeapCap = 512;
+
+inline int blocksFor(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "libsvm: CUDA error %s\n", cudaGetErrorString(e));
+        return SVM_ERR_CUDA;
+    }
+    return SVM_OK;
+}
+
+// Block-wide sum in a fixed order (warp shuffle tree, then warps in index order).
+__device__ double block_sum(double v) {
+    __shared__ double warpSums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) warpSums[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < nw; ++w) r += warpSums[w];
+    }
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+// ---- geometry ------------------------------------------------------------------------------
+
+// Per vertex: spherical coordinates and, for each of its three cells, the arc from the ring
+// predecessor and the included angle at the vertex (the per-corner terms of
+// computeGeometryCPU, sphericalVertexModel.cpp:257-276).  With `t1test`, also marks every edge
+// (v, u), v < u, shorter than the T1 threshold (sphericalVertexModel.cpp:469-481).
+__global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph,
+                          const int4* __restrict__ vcell, const int4* __restrict__ vlast,
+                          const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
+                          const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV,
+                          double R, int t1test, double t1Threshold, T1Scratch t1) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 p = ld3(pos, v);
+    vsph[v] = sph_coords(p);
+    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
+        const double arc = geodesic(pl, p, R);
+        const double ang = included_angle(pl, p, px);
+        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = make_double2(arc, ang);
+    }
+    if (t1test) {
+        const int4 nb = vnbr[v];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            const int u = comp(nb, s);
+            if (v < u && geodesic(p, ld3(pos, u), R) < t1Threshold) {
+                const int q = 3 * v + s;
+                atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
+                atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
+                atomicAdd(t1.count, 1);
+            }
+        }
+    }
+}
+
+// Per cell: centroid (sum of ring vertices in ring order, renormalised), perimeter and angle sum
+// in the CPU's order (ring positions n-2, n-1, 0, ..., n-3), area = (sum - (n-2) pi) wrapped
+// by floor(area / pi), times R^2 (sphericalVertexModel.cpp:228-303).  The last block to finish
+// totals the areas and raises the fallback flag when |sum A - 4 pi R^2| > 1e-6 (304-310).
+__global__ void k_cells(const double4_32a* __restrict__ pos, const int* __restrict__ ring,
+                        const int* __restrict__ ringCount, const double2* __restrict__ corner, int Wc, int nC,
+                        double R, double4_32a* __restrict__ cellPos, double4_32a* __restrict__ cellSph,
+                        double2* __restrict__ ap, double* __restrict__ partials, unsigned* __restrict__ ticket,
+                        double* __restrict__ scalars, int* __restrict__ fallbackFlag) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double area = 0.0;
+    if (c < nC) {
+        const int n = ringCount[c];
+        const int* rg = ring + (long)c * Wc;
+        D3 cp{0.0, 0.0, 0.0};
+        for (int k = 0; k < n; ++k) cp = add3(cp, ld3(pos, rg[k]));
+        cp = renorm(cp, R);
+        st3(cellPos, c, cp);
+        cellSph[c] = sph_coords(cp);
+        const double2* cr = corner + (long)c * Wc;
+        double per = 0.0, ang = 0.0;
+        int k = n - 2;
+        for (int t = 0; t < n; ++t) {
+            const double2 q = cr[k];
+            per += q.x;
+            ang += q.y;
+            k = (k + 1 == n) ? 0 : k + 1;
+        }
+        area = __dsub_rn(ang, __dmul_rn((double)(n - 2), kPI));
+        const int extra = (int)floor(area / (1.0 * kPI));
+        if (extra > 0) area = __dsub_rn(area, __dmul_rn((double)extra, kPI));
+        area = __dmul_rn(__dmul_rn(area, R), R);
+        ap[c] = make_double2(area, per);
+    }
+    const double bs = block_sum(area);
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amLast) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(partials + b);
+        const double total = block_sum(s);
+        if (threadIdx.x == 0) {
+            const double excess = total - 4.0 * kPI * R * R;
+            scalars[0] = total;
+            scalars[1] = excess;
+            *fallbackFlag = fabs(excess) > 1e-6 ? 1 : 0;
+            *ticket = 0u;
+        }
+    }
+}
+
+// recomputeAreasCPU (sphericalVertexModel.cpp:162-207): area as a sum of spherical triangles
+// (centroid, ring[k-1], ring[k]) starting from (ring[n-2], ring[n-1]).
+__global__ void k_fallback(const double4_32a* __restrict__ pos, const int* __restrict__ ring,
+                           const int* __restrict__ ringCount, const double4_32a* __restrict__ cellPos, int Wc, int nC,
+                           double R, const int* __restrict__ fallbackFlag, double2* __restrict__ ap) {
+    if (*fallbackFlag == 0) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nC) return;
+    const int n = ringCount[c];
+    const int* rg = ring + (long)c * Wc;
+    const D3 cp = ld3(cellPos, c);
+    D3 last = ld3(pos, rg[n - 2]), cur = ld3(pos, rg[n - 1]);
+    double area = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const D3 next = ld3(pos, rg[k]);
+        area += triangle_area(cp, last, cur, R);
+        last = cur;
+        cur = next;
+    }
+    ap[c].x = area;
+}
+
+// ---- forces and integration ------------------------------------------------------------------
+
+__global__ void k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    st3(force, v, vertex_force(A, v));
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11): ten rounds of two 32x32->64 multiplies with a Weyl-sequence key schedule.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
+    const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { key.x += W0; key.y += W1; }
+        const unsigned hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        const unsigned hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+    }
+    return ctr;
+}
+// 53-bit uniform in (0, 1) from two 32-bit words.
+__device__ __forceinline__ double u53(unsigned a, unsigned b) {
+    const unsigned long long x = ((unsigned long long)a << 21) ^ (unsigned long long)(b >> 11);
+    return ((double)(x & ((1ull << 53) - 1)) + 0.5) * 0x1.0p-53;
+}
+// Three standard normals for (vertex, step) by Box-Muller on two Philox draws.
+__device__ __forceinline__ D3 philox_normals3(uint64_t seed, unsigned long long step, int v) {
+    const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    const uint4 r0 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 0u), key);
+    const uint4 r1 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 1u), key);
+    const double a = sqrt(-2.0 * log(u53(r0.x, r0.y)));
+    double s0, c0;
+    sincospi(2.0 * u53(r0.z, r0.w), &s0, &c0);
+    const double b = sqrt(-2.0 * log(u53(r1.x, r1.y)));
+    const double c1 = cospi(2.0 * u53(r1.z, r1.w));
+    return D3{a * c0, a * s0, b * c1};
+}
+
+// disp_d = xi_d sqrt(2 dt mu T) + F_d dt mu (brownianDynamics.cpp:37-44), products rounded
+// before the sum as on the CPU.
+__device__ __forceinline__ double bd_disp(double xi, double np, double f, double fp) {
+    return __dadd_rn(__dmul_rn(xi, np), __dmul_rn(f, fp));
+}
+// sphericalDomain::move with every product and sum rounded separately (no contraction), so the
+// renormalised positions follow the CPU's sequence of roundings.
+__device__ __forceinline__ D3 move_exact(D3 p, D3 v, double R) {
+    const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
+    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
+    const double s = vp / pp;
+    D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
+         __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
+    const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
+    const double inv = 1.0 / sqrt(qq);
+    return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
+}
+
+// Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
+template <int kNoise>
+__global__ void k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force, double4_32a* __restrict__ posNext,
+                           const double* __restrict__ noise, uint64_t seed,
+                           const unsigned long long* __restrict__ stepCounter, double np, double fp) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 f = vertex_force(A, v);
+    st3(force, v, f);
+    D3 xi;
+    if (kNoise == SVM_NOISE_BUFFER) xi = D3{noise[3 * v], noise[3 * v + 1], noise[3 * v + 2]};
+    else xi = philox_normals3(seed, *stepCounter, v);
+    const D3 d{bd_disp(xi.x, np, f.x, fp), bd_disp(xi.y, np, f.y, fp), bd_disp(xi.z, np, f.z, fp)};
+    st3(posNext, v, move_exact(ld3(A.pos, v), d, A.R));
+}
+
+// moveParticles (sphericalVertexModel.cpp:111-148): p <- move(p, scale * disp), in place.
+__global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__ disp, double scale, int nV, double R) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 d{__dmul_rn(scale, disp[3 * v]), __dmul_rn(scale, disp[3 * v + 1]), __dmul_rn(scale, disp[3 * v + 2])};
+    st3(pos, v, move_exact(ld3(pos, v), d, R));
+}
+
+// Standalone T1 edge test (gpu_vm_test_edges_for_T1, sphericalVertexModel.cu:225-273).
+__global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __restrict__ vnbr, int nV, double R,
+                          double t1Threshold, T1Scratch t1) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 p = ld3(pos, v);
+    const int4 nb = vnbr[v];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int u = comp(nb, s);
+        if (v < u && geodesic(p, ld3(pos, u), R) < t1Threshold) {
+            const int q = 3 * v + s;
+            atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
+            atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
+            atomicAdd(t1.count, 1);
+        }
+    }
+}
+
+// ---- T1 apply ------------------------------------------------------------------------------
+struct ApplyArgs {
+    double4_32a* pos;
+    double4_32a* vsph;
+    int4 *vcell, *vnbr, *vlast, *vnext, *vrpos;
+    int* ring;
+    int* ringCount;
+    double2* corner;
+    int Wc, nV, nC;
+    double R, t1Threshold;
+    int* status;
+    unsigned long long* stepCounter;
+    int bumpStep;
+};
+
+__device__ __forceinline__ int& compRef(int4* a, int v, int s) { return reinterpret_cast<int*>(a + v)[s]; }
+
+// Locate `target` in ring `cell` the way getCellVertexSetForT1 does
+// (sphericalVertexModel.cpp:642-652): returns its predecessor and successor.
+__device__ void ring_neighbours(const ApplyArgs& A, int cell, int target, int& vlast, int& vnext) {
+    const int n = A.ringCount[cell];
+    const int* rg = A.ring + (long)cell * A.Wc;
+    vlast = rg[n - 2];
+    int vcur = rg[n - 1];
+    vnext = vcur;
+    for (int k = 0; k < n; ++k) {
+        vnext = rg[k];
+        if (vcur == target) break;
+        vlast = vcur;
+        vcur = vnext;
+    }
+}
+
+__device__ void ring_remove(const ApplyArgs& A, int cell, int target) {
+    int* rg = A.ring + (long)cell * A.Wc;
+    const int n = A.ringCount[cell];
+    int idx = 0;
+    for (int k = 0; k < n - 1; ++k) {
+        if (rg[k] == target) idx += 1;
+        rg[k] = rg[idx];
+        idx += 1;
+    }
+    A.ringCount[cell] = n - 1;
+}
+
+__device__ void ring_insert_after(const ApplyArgs& A, int cell, int after, int added) {
+    int* rg = A.ring + (long)cell * A.Wc;
+    const int n = A.ringCount[cell];
+    int k = 0;
+    while (k < n && rg[k] != after) ++k;
+    for (int j = n; j > k + 1; --j) rg[j] = rg[j - 1];
+    rg[k + 1] = added;
+    A.ringCount[cell] = n + 1;
+}
+
+// rodriguesRotation (inc/functions.h:175-181)
+__device__ __forceinline__ D3 rodrigues(D3 v, D3 k, double theta) {
+    const D3 cp{__dsub_rn(__dmul_rn(k.y, v.z), __dmul_rn(k.z, v.y)), __dsub_rn(__dmul_rn(k.z, v.x), __dmul_rn(k.x, v.z)),
+                __dsub_rn(__dmul_rn(k.x, v.y), __dmul_rn(k.y, v.x))};
+    const double c = cos(theta), s = sin(theta);
+    const double w = __dmul_rn(1.0 - c, __dadd_rn(__dadd_rn(__dmul_rn(k.x, v.x), __dmul_rn(k.y, v.y)), __dmul_rn(k.z, v.z)));
+    return D3{__dadd_rn(__dadd_rn(__dmul_rn(c, v.x), __dmul_rn(s, cp.x)), __dmul_rn(w, k.x)),
+              __dadd_rn(__dadd_rn(__dmul_rn(c, v.y), __dmul_rn(s, cp.y)), __dmul_rn(w, k.y)),
+              __dadd_rn(__dadd_rn(__dmul_rn(c, v.z), __dmul_rn(s, cp.z)), __dmul_rn(w, k.z))};
+}
+__device__ __forceinline__ D3 renorm_exact(D3 p, double R) {
+    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
+    const double inv = 1.0 / sqrt(pp);
+    return D3{__dmul_rn(R, __dmul_rn(inv, p.x)), __dmul_rn(R, __dmul_rn(inv, p.y)), __dmul_rn(R, __dmul_rn(inv, p.z))};
+}
+
+// One flip as testAndPerformT1TransitionsCPU does it (sphericalVertexModel.cpp:483-599).
+// Returns false when the flip is forbidden or does not fit the ring capacity.
+__device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs) {
+    const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
+    cs.w = -1;
+    for (int ff = 0; ff < 3; ++ff) {
+        const int t = compRef(A.vcell, v2, ff);
+        if (t != c[0] && t != c[1] && t != c[2]) cs.w = t;
+    }
+    cs.x = cs.y = cs.z = -1;
+    for (int q = 0; q < 3; ++q) {
+        int vl, vx;
+        ring_neighbours(A, c[q], v1, vl, vx);
+        if (vl == v2) cs.x = c[q];
+        else if (vx == v2) cs.z = c[q];
+        else cs.y = c[q];
+    }
+    if (cs.x < 0 || cs.y < 0 || cs.z < 0 || cs.w < 0) { atomicOr(A.status, SVM_DEV_BAD_TOPOLOGY); return false; }
+    int vl, vx;
+    ring_neighbours(A, cs.y, v1, vl, vx);
+    vs.x = vl; vs.y = vx;
+    ring_neighbours(A, cs.w, v2, vl, vx);
+    vs.w = vl; vs.z = vx;
+    // forbid a T1 that would shrink a triangular cell (sphericalVertexModel.cpp:485-487)
+    if (A.ringCount[cs.x] == 3 || A.ringCount[cs.z] == 3) return false;
+    if (A.ringCount[cs.y] + 1 > A.Wc || A.ringCount[cs.w] + 1 > A.Wc) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    D3 p1 = ld3(A.pos, v1), p2 = ld3(A.pos, v2);
+    D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
+    mid = renorm_exact(mid, 1.0);
+    const D3 vC = ld3(A.pos, vs.z);
+    double det = vC.x * (p1.y * p2.z - p1.z * p2.y) + vC.y * (p1.z * p2.x - p1.x * p2.z) + vC.z * (p1.x * p2.y - p1.y * p2.x);
+    det = det > 0 ? 1. : -1.;
+    const double theta = -0.5 * det * kPI;
+    p1 = rodrigues(p1, mid, theta);
+    p2 = rodrigues(p2, mid, theta);
+    const D3 diff{__dmul_rn(0.5, __dsub_rn(p1.x, p2.x)), __dmul_rn(0.5, __dsub_rn(p1.y, p2.y)), __dmul_rn(0.5, __dsub_rn(p1.z, p2.z))};
+    p1 = D3{__dadd_rn(p1.x, diff.x), __dadd_rn(p1.y, diff.y), __dadd_rn(p1.z, diff.z)};
+    p2 = D3{__dsub_rn(p2.x, diff.x), __dsub_rn(p2.y, diff.y), __dsub_rn(p2.z, diff.z)};
+    st3(A.pos, v1, renorm_exact(p1, A.R));
+    st3(A.pos, v2, renorm_exact(p2, A.R));
+    for (int k = 0; k < 3; ++k) {
+        if (compRef(A.vcell, v1, k) == cs.z) compRef(A.vcell, v1, k) = cs.w;
+        if (compRef(A.vcell, v2, k) == cs.x) compRef(A.vcell, v2, k) = cs.y;
+        if (compRef(A.vnbr, vs.y, k) == v1) compRef(A.vnbr, vs.y, k) = v2;
+        if (compRef(A.vnbr, vs.z, k) == v2) compRef(A.vnbr, vs.z, k) = v1;
+        if (compRef(A.vnbr, v1, k) == vs.y) compRef(A.vnbr, v1, k) = vs.z;
+        if (compRef(A.vnbr, v2, k) == vs.z) compRef(A.vnbr, v2, k) = vs.y;
+    }
+    ring_remove(A, cs.x, v2);
+    ring_insert_after(A, cs.y, v1, v2);
+    ring_remove(A, cs.z, v1);
+    ring_insert_after(A, cs.w, v2, v1);
+    return true;
+}
+
+__device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
+    const int v = q / 3, s = q - 3 * (q / 3);
+    const int u = compRef(A.vnbr, v, s);
+    return v < u && geodesic(ld3(A.pos, v), ld3(A.pos, u), A.R) < A.t1Threshold;
+}
+
+// Applies the flagged T1 flips in the order of the CPU loop (ascending vertex1, then slot),
+// re-testing each edge against the current state when it is reached and re-testing, after every
+// flip, the edges of the six vertices whose slots or positions the flip changed.  Flags ahead of
+// the extracted window live in the bitmap; flags inside it in a small heap.  Afterwards every
+// cell whose ring changed gets its ring bookkeeping (vrpos/vlast/vnext) and corners rebuilt.
+__global__ void __launch_bounds__(kApplyThreads) k_t1_apply(ApplyArgs A, T1Scratch t1) {
+    __shared__ int buf[kExtractCap];
+    __shared__ int heap[kHeapCap];
+    __shared__ int nbuf, head, nheap, extractWord, nTouched;
+    __shared__ int nSummaryHit;
+    const int tid = threadIdx.x;
+    const int total = *t1.count;
+    if (total == 0) {
+        if (tid == 0 && A.bumpStep) *A.stepCounter += 1ull;
+        return;
+    }
+    if (tid == 0) { nbuf = 0; head = 0; nheap = 0; extractWord = 0; nTouched = 0; }
+    __syncthreads();
+    int lastProcessed = -1;
+    while (true) {
+        // Refill the window from the bitmap when both the window and the heap are empty.
+        if (head == nbuf && nheap == 0) {
+            __syncthreads();
+            if (tid == 0) { nSummaryHit = 0x7fffffff; }
+            __syncthreads();
+            const int sw0 = extractWord >> 5;
+            for (int sw = sw0 + tid; sw < t1.nSummary; sw += blockDim.x) {
+                if (t1.summary[sw] != 0u) { atomicMin(&nSummaryHit, sw); break; }
+            }
+            __syncthreads();
+            const int sw = nSummaryHit;
+            if (sw == 0x7fffffff) break;  // uniform: nothing left
+            // positions of the 32 bitmap words under summary word sw, in ascending order
+            unsigned word = 0u;
+            const int w = sw * 32 + tid;
+            if (tid < 32 && w < t1.nWords) word = t1.bits[w];
+            int cnt = __popc(word);
+            int incl = cnt;
+            if (tid < 32) {
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if ((tid & 31) >= o) incl += y;
+                }
+            }
+            if (tid < 32) {
+                int at = incl - cnt;
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1u;
+                    buf[at++] = w * 32 + b;
+                }
+                if (w < t1.nWords) t1.bits[w] = 0u;
+                if (tid == 31) { nbuf = incl; head = 0; extractWord = (sw + 1) * 32; t1.summary[sw] = 0u; }
+            }
+            __syncthreads();
+            continue;
+        }
+        // Sequential part: one candidate by thread 0.
+        if (tid == 0) {
+            int q;
+            const bool fromHeap = nheap > 0 && (head == nbuf || heap[0] < buf[head]);
+            if (fromHeap) {
+                q = heap[0];
+                const int x = heap[--nheap];
+                int i = 0;
+                while (true) {
+                    int l = 2 * i + 1, r = l + 1, mI = i;
+                    int mv = x;
+                    if (l < nheap && heap[l] < mv) { mI = l; mv = heap[l]; }
+                    if (r < nheap && heap[r] < mv) { mI = r; mv = heap[r]; }
+                    if (mI == i) break;
+                    heap[i] = heap[mI];
+                    i = mI;
+                }
+                if (nheap > 0) heap[i] = x;
+            } else {
+                q = buf[head++];
+            }
+            if (q != lastProcessed) {
+                lastProcessed = q;
+                if (t1_candidate(A, q)) {
+                    const int v1 = q / 3, v2 = compRef(A.vnbr, v1, q - 3 * v1);
+                    int4 cs, vs;
+                    if (t1_flip(A, v1, v2, cs, vs)) {
+                        const int fc = atomicAdd(t1.flipCount, 1);
+                        if (fc < t1.flipLogCap) { t1.flipLog[2 * fc] = v1; t1.flipLog[2 * fc + 1] = v2; }
+                        if (nTouched + 4 <= t1.touchedCap) {
+                            t1.touched[nTouched++] = cs.x; t1.touched[nTouched++] = cs.y;
+                            t1.touched[nTouched++] = cs.z; t1.touched[nTouched++] = cs.w;
+                        } else {
+                            atomicOr(A.status, SVM_DEV_T1_OVERFLOW);
+                        }
+                        const int aff[6] = {v1, v2, vs.x, vs.y, vs.z, vs.w};
+                        const int windowEnd = extractWord * 32;
+                        for (int a = 0; a < 6; ++a)
+                            for (int s = 0; s < 3; ++s) {
+                                const int r = 3 * aff[a] + s;
+                                if (r <= q || !t1_candidate(A, r)) continue;
+                                if (r >= windowEnd) {
+                                    t1.bits[r >> 5] |= 1u << (r & 31);
+                                    t1.summary[r >> 10] |= 1u << ((r >> 5) & 31);
+                                } else if (nheap < kHeapCap) {
+                                    int i = nheap++;
+                                    while (i > 0 && heap[(i - 1) / 2] > r) { heap[i] = heap[(i - 1) / 2]; i = (i - 1) / 2; }
+                                    heap[i] = r;
+                                } else {
+                                    atomicOr(A.status, SVM_DEV_T1_OVERFLOW);
+                                }
+                            }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // Rebuild ring bookkeeping and corners of every touched cell.
+    __syncthreads();
+    const int nt = nTouched;
+    for (int e = tid; e < nt * A.Wc; e += blockDim.x) {
+        const int cell = t1.touched[e / A.Wc], k = e % A.Wc;
+        const int n = A.ringCount[cell];
+        if (k >= n) continue;
+        const int* rg = A.ring + (long)cell * A.Wc;
+        const int u = rg[k];
+        const int last = rg[k == 0 ? n - 1 : k - 1], next = rg[k + 1 == n ? 0 : k + 1];
+        for (int s = 0; s < 3; ++s)
+            if (compRef(A.vcell, u, s) == cell) {
+                compRef(A.vrpos, u, s) = k;
+                compRef(A.vlast, u, s) = last;
+                compRef(A.vnext, u, s) = next;
+            }
+    }
+    // moved vertices: spherical coordinates
+    const int nflip = nt / 4;
+    (void)nflip;
+    __syncthreads();
+    for (int e = tid; e < nt * A.Wc; e += blockDim.x) {
+        const int cell = t1.touched[e / A.Wc], k = e % A.Wc;
+        const int n = A.ringCount[cell];
+        if (k >= n) continue;
+        const int* rg = A.ring + (long)cell * A.Wc;
+        const D3 pl = ld3(A.pos, rg[k == 0 ? n - 1 : k - 1]), p = ld3(A.pos, rg[k]), px = ld3(A.pos, rg[k + 1 == n ? 0 : k + 1]);
+        A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
+        // every vertex of a touched cell gets fresh spherical coordinates (identical values when
+        // it did not move, so concurrent writers agree)
+        A.vsph[rg[k]] = sph_coords(p);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        *t1.count = 0;
+        if (A.bumpStep) *A.stepCounter += 1ull;
+    }
+}
+
+// Ring bookkeeping for all vertices after a topology upload: for each cell and ring position,
+// record it in the vertex's slot for that cell.
+__global__ void k_ring_index(const int* __restrict__ ring, const int* __restrict__ ringCount, int Wc, int nC,
+                             int4* vcell, int4* vlast, int4* vnext, int4* vrpos, int* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nC) return;
+    const int n = ringCount[c];
+    const int* rg = ring + (long)c * Wc;
+    for (int k = 0; k < n; ++k) {
+        const int u = rg[k];
+        bool found = false;
+        for (int s = 0; s < 3; ++s)
+            if (compRef(vcell, u, s) == c) {
+                compRef(vrpos, u, s) = k;
+                compRef(vlast, u, s) = rg[k == 0 ? n - 1 : k - 1];
+                compRef(vnext, u, s) = rg[k + 1 == n ? 0 : k + 1];
+                found = true;
+            }
+        if (!found) atomicOr(status, SVM_DEV_BAD_TOPOLOGY);
+    }
+}
+
+__global__ void k_energy(const double2* __restrict__ ap, const double2* __restrict__ pref, double Kr, int nC,
+                         double* partials, unsigned* ticket, double* out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (c < nC) {
+        const double da = ap[c].x - pref[c].x, dp = ap[c].y - pref[c].y;
+        e = __dadd_rn(__dmul_rn(__dmul_rn(Kr, da), da), __dmul_rn(dp, dp));
+    }
+    const double bs = block_sum(e);
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amLast) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(partials + b);
+        const double total = block_sum(s);
+        if (threadIdx.x == 0) { *out = total; *ticket = 0u; }
+    }
+}
+
+// ---- launch helpers --------------------------------------------------------------------------
+static ForceArgs force_args(svm_model* m, int buf) {
+    ForceArgs A;
+    A.pos = m->pos[buf]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
+    A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
+    return A;
+}
+static ApplyArgs apply_args(svm_model* m, int bump) {
+    ApplyArgs A;
+    A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vnbr = m->vnbr; A.vlast = m->vlast;
+    A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
+    A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
+    A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
+    return A;
+}
+
+int launch_corners(svm_model* m, bool t1test) {
+    k_corners<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
+        m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+        m->R, t1test ? 1 : 0, m->t1Threshold, m->t1);
+    m->cornersValid = true;
+    return check_launch();
+}
+
+static int launch_cells(svm_model* m) {
+    const int nb = blocksFor(m->nCells);
+    k_cells<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R,
+                                           m->cellPos, m->cellSph, m->ap, m->partials, m->ticket, m->scalars,
+                                           m->fallbackFlag);
+    k_fallback<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc, m->nCells,
+                                              m->R, m->fallbackFlag, m->ap);
+    return check_launch();
+}
+
+int launch_geometry(svm_model* m) {
+    int rc = SVM_OK;
+    if (!m->cornersValid) rc = launch_corners(m, false);
+    if (rc) return rc;
+    return launch_cells(m);
+}
+
+int launch_t1_apply(svm_model* m) {
+    k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, 1), m->t1);
+    return check_launch();
+}
+
+// One fused Brownian timestep (see the file header).
+static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise, uint64_t seed) {
+    int rc = launch_geometry(m);
+    if (rc) return rc;
+    const double fp = dt * mu;
+    const double np = sqrt(2.0 * fp * T);
+    const int nxt = 1 - m->cur;
+    if (noiseMode == SVM_NOISE_BUFFER)
+        k_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+    else
+        k_force_bd<SVM_NOISE_PHILOX><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+    if ((rc = check_launch())) return rc;
+    m->cur = nxt;
+    // corners of the moved state, with the T1 edge test fused in
+    rc = launch_corners(m, !m->restricted);
+    if (rc) return rc;
+    k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, 1), m->t1);
+    return check_launch();
+}
+
+}  // namespace svm
+
+// ================================ C ABI ===================================================
+extern "C" {
+
+const char* svm_status_string(int s) {
+    switch (s) {
+        case SVM_OK: return "ok";
+        case SVM_ERR_ARG: return "invalid argument";
+        case SVM_ERR_CUDA: return "CUDA error";
+        case SVM_ERR_HULL: return "convex hull failed";
+        case SVM_ERR_DEVICE: return "device status set";
+        case SVM_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown";
+    }
+}
+
+int svm_device_count(int* count) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); n = 0; }
+    if (count) *count = n;
+    return n > 0 ? SVM_OK : SVM_ERR_NO_DEVICE;
+}
+
+struct svm_topology { svm::Topology t; };
+
+int svm_topology_from_points(const double* pts, int n, svm_topology** out) {
+    if (!pts || n < 4 || !out) return SVM_ERR_ARG;
+    std::vector<int> tris;
+    svm_topology* t = new svm_topology();
+    if (!svm::convexHullTriangles(pts, n, tris) || !svm::topologyFromTriangles(pts, n, tris, t->t)) {
+        delete t;
+        return SVM_ERR_HULL;
+    }
+    *out = t;
+    return SVM_OK;
+}
+
+int svm_topology_from_triangles(const double* pts, int n, const int* tri, int ntri, svm_topology** out) {
+    if (!pts || !tri || n < 4 || ntri != 2 * n - 4 || !out) return SVM_ERR_ARG;
+    std::vector<int> tris(tri, tri + 3 * (size_t)ntri);
+    svm_topology* t = new svm_topology();
+    if (!svm::topologyFromTriangles(pts, n, tris, t->t)) { delete t; return SVM_ERR_HULL; }
+    *out = t;
+    return SVM_OK;
+}
+
+int svm_topology_sizes(const svm_topology* t, int* nC, int* nV, int* maxRing) {
+    if (!t) return SVM_ERR_ARG;
+    if (nC) *nC = t->t.nCells;
+    if (nV) *nV = t->t.nVertices;
+    if (maxRing) *maxRing = t->t.maxRing;
+    return SVM_OK;
+}
+
+int svm_topology_get(const svm_topology* t, double* vp, int* rings, int stride, unsigned* counts, int* vc, int* vn) {
+    if (!t) return SVM_ERR_ARG;
+    const svm::Topology& T = t->t;
+    if (rings && stride < T.maxRing) return SVM_ERR_ARG;
+    if (vp) std::memcpy(vp, T.vertexPos.data(), sizeof(double) * T.vertexPos.size());
+    if (vc) std::memcpy(vc, T.vertexCells.data(), sizeof(int) * T.vertexCells.size());
+    if (vn) std::memcpy(vn, T.vertexNeighbors.data(), sizeof(int) * T.vertexNeighbors.size());
+    for (int c = 0; c < T.nCells; ++c) {
+        const int b = T.ringOffsets[c], e = T.ringOffsets[c + 1];
+        if (counts) counts[c] = (unsigned)(e - b);
+        if (rings)
+            for (int k = 0; k < stride; ++k) rings[(size_t)c * stride + k] = k < e - b ? T.ringVertices[b + k] : -1;
+    }
+    return SVM_OK;
+}
+
+void svm_topology_free(svm_topology* t) { delete t; }
+
+#define SVM_CUDA(x)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (x);                                                                \
+        if (e_ != cudaSuccess) {                                                             \
+            std::fprintf(stderr, "libsvm: %s failed: %s\n", #x, cudaGetErrorString(e_));     \
+            return SVM_ERR_CUDA;                                                             \
+        }                                                                                    \
+    } while (0)
+
+int svm_model_create(int nCells, int nVertices, int Wc, double radius, void* stream, svm_model** out) {
+    if (nCells < 4 || nVertices != 2 * nCells - 4 || Wc < 3 || Wc > 64 || !(radius > 0) || !out) return SVM_ERR_ARG;
+    int ndev = 0;
+    if (svm_device_count(&ndev) != SVM_OK) return SVM_ERR_NO_DEVICE;
+    svm_model* m = new svm_model();
+    m->nCells = nCells; m->nVertices = nVertices; m->Wc = Wc; m->R = radius;
+    if (stream) { m->stream = (cudaStream_t)stream; }
+    else {
+        if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) { delete m; return SVM_ERR_CUDA; }
+        m->ownStream = true;
+    }
+    const size_t nV = nVertices, nC = nCells;
+    bool ok = true;
+    auto alloc = [&](void** p, size_t bytes) { if (ok && cudaMalloc(p, bytes) != cudaSuccess) ok = false; if (ok) cudaMemset(*p, 0, bytes); };
+    alloc((void**)&m->pos[0], nV * sizeof(double4_32a));
+    alloc((void**)&m->pos[1], nV * sizeof(double4_32a));
+    alloc((void**)&m->vsph, nV * sizeof(double4_32a));
+    alloc((void**)&m->vcell, nV * sizeof(int4));
+    alloc((void**)&m->vnbr, nV * sizeof(int4));
+    alloc((void**)&m->vlast, nV * sizeof(int4));
+    alloc((void**)&m->vnext, nV * sizeof(int4));
+    alloc((void**)&m->vrpos, nV * sizeof(int4));
+    alloc((void**)&m->ring, nC * Wc * sizeof(int));
+    alloc((void**)&m->ringCount, nC * sizeof(int));
+    alloc((void**)&m->corner, nC * Wc * sizeof(double2));
+    alloc((void**)&m->cellPos, nC * sizeof(double4_32a));
+    alloc((void**)&m->cellSph, nC * sizeof(double4_32a));
+    alloc((void**)&m->ap, nC * sizeof(double2));
+    alloc((void**)&m->pref, nC * sizeof(double2));
+    alloc((void**)&m->force, nV * sizeof(double4_32a));
+    alloc((void**)&m->vel, nV * sizeof(double4_32a));
+    alloc((void**)&m->noiseBuf, 3 * nV * sizeof(double));
+    alloc((void**)&m->dispBuf, 3 * nV * sizeof(double));
+    m->maxPartialBlocks = svm::blocksFor((long)std::max(nV, nC)) + 8;
+    alloc((void**)&m->partials, (size_t)m->maxPartialBlocks * 8 * sizeof(double));
+    alloc((void**)&m->ticket, 8 * sizeof(unsigned));
+    alloc((void**)&m->scalars, 16 * sizeof(double));
+    alloc((void**)&m->fallbackFlag, sizeof(int));
+    alloc((void**)&m->status, sizeof(int));
+    alloc((void**)&m->stepCounter, sizeof(unsigned long long));
+    m->t1.nWords = (int)((3 * nV + 31) / 32);
+    m->t1.nSummary = (m->t1.nWords + 31) / 32;
+    m->t1.flipLogCap = 1 << 16;
+    m->t1.touchedCap = 4 * 8192;
+    alloc((void**)&m->t1.bits, (size_t)m->t1.nSummary * 32 * sizeof(unsigned));
+    alloc((void**)&m->t1.summary, (size_t)m->t1.nSummary * sizeof(unsigned));
+    alloc((void**)&m->t1.count, sizeof(int));
+    alloc((void**)&m->t1.flipLog, 2 * (size_t)m->t1.flipLogCap * sizeof(int));
+    alloc((void**)&m->t1.flipCount, sizeof(int));
+    alloc((void**)&m->t1.touched, (size_t)m->t1.touchedCap * sizeof(int));
+    if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
+    std::vector<double2> pref(nC, make_double2(1.0, 3.8));
+    cudaMemcpy(m->pref, pref.data(), nC * sizeof(double2), cudaMemcpyHostToDevice);
+    if (cudaDeviceSynchronize() != cudaSuccess) { svm_model_destroy(m); return SVM_ERR_CUDA; }
+    *out = m;
+    return SVM_OK;
+}
+
+int svm_model_destroy(svm_model* m) {
+    if (!m) return SVM_ERR_ARG;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+                    m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
+                    m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
+                    m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
+    if (m->ownStream && m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return SVM_OK;
+}
+
+static int upload_positions(svm_model* m, const double* in) {
+    std::vector<double4_32a> p(m->nVertices);
+    for (int i = 0; i < m->nVertices; ++i) p[i] = make_double4_32a(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
+    SVM_CUDA(cudaMemcpyAsync(m->pos[m->cur], p.data(), sizeof(double4_32a) * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    m->cornersValid = false;
+    return SVM_OK;
+}
+
+int svm_model_set_topology(svm_model* m, const double* vp, const int* rings, int stride, const unsigned* counts,
+                           const int* vc, const int* vn) {
+    if (!m || !vp || !rings || !counts || !vc || !vn || stride < 3) return SVM_ERR_ARG;
+    const int nC = m->nCells, nV = m->nVertices, Wc = m->Wc;
+    std::vector<int> rg((size_t)nC * Wc, -1), cnt(nC);
+    for (int c = 0; c < nC; ++c) {
+        if ((int)counts[c] > Wc || (int)counts[c] > stride || counts[c] < 3) return SVM_ERR_ARG;
+        cnt[c] = (int)counts[c];
+        for (int k = 0; k < cnt[c]; ++k) {
+            const int u = rings[(size_t)c * stride + k];
+            if (u < 0 || u >= nV) return SVM_ERR_ARG;
+            rg[(size_t)c * Wc + k] = u;
+        }
+    }
+    std::vector<int4> vcell(nV), vnbr(nV);
+    for (int v = 0; v < nV; ++v) {
+        for (int s = 0; s < 3; ++s)
+            if (vc[3 * v + s] < 0 || vc[3 * v + s] >= nC || vn[3 * v + s] < 0 || vn[3 * v + s] >= nV) return SVM_ERR_ARG;
+        vcell[v] = make_int4(vc[3 * v], vc[3 * v + 1], vc[3 * v + 2], -1);
+        vnbr[v] = make_int4(vn[3 * v], vn[3 * v + 1], vn[3 * v + 2], -1);
+    }
+    SVM_CUDA(cudaMemcpyAsync(m->ring, rg.data(), sizeof(int) * rg.size(), cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaMemcpyAsync(m->ringCount, cnt.data(), sizeof(int) * nC, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaMemcpyAsync(m->vcell, vcell.data(), sizeof(int4) * nV, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaMemcpyAsync(m->vnbr, vnbr.data(), sizeof(int4) * nV, cudaMemcpyHostToDevice, m->stream));
+    k_ring_index<<<svm::blocksFor(nC), svm::kBlock, 0, m->stream>>>(m->ring, m->ringCount, Wc, nC, m->vcell, m->vlast,
+                                                                    m->vnext, m->vrpos, m->status);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    int rc = upload_positions(m, vp);
+    if (rc) return rc;
+    int st = 0;
+    SVM_CUDA(cudaMemcpy(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost));
+    return st ? SVM_ERR_DEVICE : SVM_OK;
+}
+
+int svm_model_set_preferred_parameters(svm_model* m, double a0, double p0) {
+    if (!m) return SVM_ERR_ARG;
+    std::vector<double2> pref(m->nCells, make_double2(a0, p0));
+    SVM_CUDA(cudaMemcpyAsync(m->pref, pref.data(), sizeof(double2) * m->nCells, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_set_preferred_array(svm_model* m, const double* a0p0) {
+    if (!m || !a0p0) return SVM_ERR_ARG;
+    SVM_CUDA(cudaMemcpyAsync(m->pref, a0p0, sizeof(double2) * m->nCells, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_set_scalar_model_parameter(svm_model* m, double kr) {
+    if (!m) return SVM_ERR_ARG;
+    m->Kr = kr; m->paramsVersion++;
+    return SVM_OK;
+}
+int svm_model_set_t1_threshold(svm_model* m, double t) {
+    if (!m) return SVM_ERR_ARG;
+    m->t1Threshold = t; m->paramsVersion++;
+    return SVM_OK;
+}
+int svm_model_set_restricted_motion(svm_model* m, int r) {
+    if (!m) return SVM_ERR_ARG;
+    m->restricted = r != 0; m->paramsVersion++;
+    return SVM_OK;
+}
+
+int svm_model_compute_geometry(svm_model* m) {
+    if (!m) return SVM_ERR_ARG;
+    m->cornersValid = false;  // corners follow the current state; recompute them
+    return svm::launch_geometry(m);
+}
+
+int svm_model_compute_forces(svm_model* m) {
+    if (!m) return SVM_ERR_ARG;
+    int rc = svm_model_compute_geometry(m);
+    if (rc) return rc;
+    k_force<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(svm::force_args(m, m->cur), m->nVertices, m->force);
+    return svm::check_launch();
+}
+
+int svm_model_compute_energy(svm_model* m, double* e) {
+    if (!m || !e) return SVM_ERR_ARG;
+    k_energy<<<svm::blocksFor(m->nCells), svm::kBlock, 0, m->stream>>>(m->ap, m->pref, m->Kr, m->nCells,
+                                                                         m->partials + m->maxPartialBlocks,
+                                                                         m->ticket + 1, m->scalars + 2);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    SVM_CUDA(cudaMemcpyAsync(e, m->scalars + 2, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_enforce_topology(svm_model* m) {
+    if (!m) return SVM_ERR_ARG;
+    k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnbr, m->nVertices, m->R,
+                                                                             m->t1Threshold, m->t1);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    // corners must exist for the patching in k_t1_apply to be meaningful; recompute afterwards
+    k_t1_apply<<<1, svm::kApplyThreads, 0, m->stream>>>(svm::apply_args(m, 0), m->t1);
+    m->cornersValid = false;
+    return svm::check_launch();
+}
+
+int svm_model_move_particles(svm_model* m, const double* disp, double scale) {
+    if (!m || !disp) return SVM_ERR_ARG;
+    k_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], disp, scale, m->nVertices, m->R);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    m->cornersValid = false;
+    if (!m->restricted) return svm_model_enforce_topology(m);
+    return SVM_OK;
+}
+
+int svm_model_move_particles_host(svm_model* m, const double* disp, double scale) {
+    if (!m || !disp) return SVM_ERR_ARG;
+    SVM_CUDA(cudaMemcpyAsync(m->dispBuf, disp, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+    return svm_model_move_particles(m, m->dispBuf, scale);
+}
+
+static int get_vec4(svm_model* m, const double4_32a* src, int n, double* out) {
+    std::vector<double4_32a> h(n);
+    SVM_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    for (int i = 0; i < n; ++i) { out[3 * i] = h[i].x; out[3 * i + 1] = h[i].y; out[3 * i + 2] = h[i].z; }
+    return SVM_OK;
+}
+
+int svm_model_get_positions(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->pos[m->cur], m->nVertices, out); }
+int svm_model_set_positions(svm_model* m, const double* in) { if (!m || !in) return SVM_ERR_ARG; return upload_positions(m, in); }
+int svm_model_get_forces(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->force, m->nVertices, out); }
+int svm_model_get_velocities(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->vel, m->nVertices, out); }
+int svm_model_get_cell_positions(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->cellPos, m->nCells, out); }
+
+int svm_model_set_velocities(svm_model* m, const double* in) {
+    if (!m || !in) return SVM_ERR_ARG;
+    std::vector<double4_32a> p(m->nVertices);
+    for (int i = 0; i < m->nVertices; ++i) p[i] = make_double4_32a(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
+    SVM_CUDA(cudaMemcpyAsync(m->vel, p.data(), sizeof(double4_32a) * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_get_area_perimeter(svm_model* m, double* out) {
+    if (!m || !out) return SVM_ERR_ARG;
+    SVM_CUDA(cudaMemcpyAsync(out, m->ap, sizeof(double2) * m->nCells, cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_get_rings(svm_model* m, int* rings, int stride, unsigned* counts) {
+    if (!m || !rings || !counts) return SVM_ERR_ARG;
+    std::vector<int> rg((size_t)m->nCells * m->Wc), cnt(m->nCells);
+    SVM_CUDA(cudaMemcpyAsync(rg.data(), m->ring, sizeof(int) * rg.size(), cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaMemcpyAsync(cnt.data(), m->ringCount, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    for (int c = 0; c < m->nCells; ++c) {
+        if (cnt[c] > stride) return SVM_ERR_ARG;
+        counts[c] = (unsigned)cnt[c];
+        for (int k = 0; k < stride; ++k) rings[(size_t)c * stride + k] = k < cnt[c] ? rg[(size_t)c * m->Wc + k] : -1;
+    }
+    return SVM_OK;
+}
+
+static int get_int4x3(svm_model* m, const int4* src, int* out) {
+    std::vector<int4> h(m->nVertices);
+    SVM_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(int4) * m->nVertices, cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    for (int i = 0; i < m->nVertices; ++i) { out[3 * i] = h[i].x; out[3 * i + 1] = h[i].y; out[3 * i + 2] = h[i].z; }
+    return SVM_OK;
+}
+int svm_model_get_vertex_cells(svm_model* m, int* out) { if (!m || !out) return SVM_ERR_ARG; return get_int4x3(m, m->vcell, out); }
+int svm_model_get_vertex_neighbors(svm_model* m, int* out) { if (!m || !out) return SVM_ERR_ARG; return get_int4x3(m, m->vnbr, out); }
+
+int svm_model_status(svm_model* m, int* st) {
+    if (!m || !st) return SVM_ERR_ARG;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    SVM_CUDA(cudaMemcpy(st, m->status, sizeof(int), cudaMemcpyDeviceToHost));
+    SVM_CUDA(cudaMemset(m->status, 0, sizeof(int)));
+    return SVM_OK;
+}
+
+int svm_model_take_flips(svm_model* m, int* pairs, int cap, int* count) {
+    if (!m || !count) return SVM_ERR_ARG;
+    int n = 0;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    SVM_CUDA(cudaMemcpy(&n, m->t1.flipCount, sizeof(int), cudaMemcpyDeviceToHost));
+    *count = n;
+    const int k = std::min(std::min(n, cap), m->t1.flipLogCap);
+    if (pairs && k > 0) SVM_CUDA(cudaMemcpy(pairs, m->t1.flipLog, sizeof(int) * 2 * k, cudaMemcpyDeviceToHost));
+    SVM_CUDA(cudaMemset(m->t1.flipCount, 0, sizeof(int)));
+    return SVM_OK;
+}
+
+int svm_model_synchronize(svm_model* m) {
+    if (!m) return SVM_ERR_ARG;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_device_positions(svm_model* m, void** p) {
+    if (!m || !p) return SVM_ERR_ARG;
+    *p = m->pos[m->cur];
+    return SVM_OK;
+}
+
+int svm_brownian_step(svm_model* m, double T, double dt, double mu, int mode, const double* noise, uint64_t seed) {
+    if (!m || (mode == SVM_NOISE_BUFFER && !noise) || (mode != SVM_NOISE_BUFFER && mode != SVM_NOISE_PHILOX)) return SVM_ERR_ARG;
+    return svm::bd_step(m, T, dt, mu, mode, noise, seed);
+}
+
+int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, const double* noise) {
+    if (!m || !noise) return SVM_ERR_ARG;
+    SVM_CUDA(cudaMemcpyAsync(m->noiseBuf, noise, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+    return svm::bd_step(m, T, dt, mu, SVM_NOISE_BUFFER, m->noiseBuf, 0);
+}
+
+int svm_brownian_run(svm_model* m, double T, double dt, double mu, uint64_t seed, int nSteps) {
+    if (!m || nSteps < 0) return SVM_ERR_ARG;
+    int rc = svm::launch_geometry(m);  // make corners valid outside the capture
+    if (rc) return rc;
+    const bool reuse = m->bdGraph && m->bdT == T && m->bdDt == dt && m->bdMu == mu && m->bdSeed == seed &&
+                       m->bdGraphCur == m->cur && m->bdGraphVersion == m->paramsVersion;
+    if (!reuse) {
+        if (m->bdGraph) { cudaGraphExecDestroy(m->bdGraph); m->bdGraph = nullptr; }
+        // a pair of steps returns the position buffers to their starting roles
+        cudaGraph_t g;
+        const int cur0 = m->cur;
+        SVM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+        int r1 = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+        int r2 = r1 ? r1 : svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+        cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
+        m->cur = cur0;
+        if (r2 || ce != cudaSuccess) { cudaGetLastError(); return SVM_ERR_CUDA; }
+        ce = cudaGraphInstantiate(&m->bdGraph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { m->bdGraph = nullptr; return SVM_ERR_CUDA; }
+        m->bdT = T; m->bdDt = dt; m->bdMu = mu; m->bdSeed = seed;
+        m->bdGraphCur = m->cur; m->bdGraphVersion = m->paramsVersion;
+    }
+    for (int i = 0; i + 1 < nSteps; i += 2) SVM_CUDA(cudaGraphLaunch(m->bdGraph, m->stream));
+    if (nSteps % 2) {
+        rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+        if (rc) return rc;
+    }
+    return SVM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,403 @@
+"""Host-side mirror of the reference's model / updater / simulation classes over libsvm.
+
+Class and method names follow the reference (src/model/sphericalVertexModel.h,
+src/updaters/brownianDynamics.h, src/updaters/energyMinimizerFIRE.h, src/simulation/simulation.h)
+so that a driver written against the reference reads the same.  Everything runs on the GPU through
+the C ABI; there is no CPU branch: setCPUOperation(True) raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+
+PI = 3.141592653589793115997963468544185161590576171875
+
+
+class Topology:
+    """Initial spherical Voronoi topology of a set of cell centres (the convexHullCGAL contract)."""
+
+    @classmethod
+    def from_arrays(cls, vertexPositions, rings, ringCounts, vertexCells, vertexNeighbors) -> "Topology":
+        """A topology given directly in the reference layouts (e.g. a saved state)."""
+        t = cls.__new__(cls)
+        t.vertexPositions = np.ascontiguousarray(vertexPositions, dtype=np.float64).reshape(-1, 3)
+        t.rings = np.ascontiguousarray(rings, dtype=np.int32)
+        t.ringCounts = np.ascontiguousarray(ringCounts, dtype=np.uint32)
+        t.vertexCells = np.ascontiguousarray(vertexCells, dtype=np.int32).reshape(-1, 3)
+        t.vertexNeighbors = np.ascontiguousarray(vertexNeighbors, dtype=np.int32).reshape(-1, 3)
+        t.nCells = t.rings.shape[0]
+        t.nVertices = t.vertexPositions.shape[0]
+        t.maxRing = int(t.ringCounts.max())
+        t.radius = float(np.linalg.norm(t.vertexPositions[0]))
+        return t
+
+    def __init__(self, centres: np.ndarray, triangles: np.ndarray | None = None):
+        pts = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1)
+        n = pts.size // 3
+        h = C.c_void_p()
+        if triangles is None:
+            call("svm_topology_from_points", pts, n, C.byref(h))
+        else:
+            tri = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1)
+            call("svm_topology_from_triangles", pts, n, tri, tri.size // 3, C.byref(h))
+        try:
+            nc, nv, mr = C.c_int(), C.c_int(), C.c_int()
+            call("svm_topology_sizes", h, C.byref(nc), C.byref(nv), C.byref(mr))
+            self.nCells, self.nVertices, self.maxRing = nc.value, nv.value, mr.value
+            W = self.maxRing
+            self.vertexPositions = np.empty(3 * self.nVertices)
+            self.rings = np.empty(self.nCells * W, dtype=np.int32)
+            self.ringCounts = np.empty(self.nCells, dtype=np.uint32)
+            self.vertexCells = np.empty(3 * self.nVertices, dtype=np.int32)
+            self.vertexNeighbors = np.empty(3 * self.nVertices, dtype=np.int32)
+            call("svm_topology_get", h, self.vertexPositions, self.rings, W, self.ringCounts, self.vertexCells,
+                 self.vertexNeighbors)
+        finally:
+            _lib.lib().svm_topology_free(h)
+        self.vertexPositions = self.vertexPositions.reshape(-1, 3)
+        self.rings = self.rings.reshape(self.nCells, W)
+        self.vertexCells = self.vertexCells.reshape(-1, 3)
+        self.vertexNeighbors = self.vertexNeighbors.reshape(-1, 3)
+        self.radius = float(np.sqrt(np.dot(pts[:3], pts[:3])))
+
+
+def random_cell_centres(seed: int, n: int) -> np.ndarray:
+    out = np.empty(3 * n)
+    call("svm_random_cell_centres", int(seed), int(n), out)
+    return out.reshape(n, 3)
+
+
+class noiseSource:
+    """Seed holder mirroring src/utilities/noiseSource.h (reproducible mt19937 seed for the
+    initial cell centres; the same seed keys the in-kernel Philox stream of the dynamics)."""
+
+    def __init__(self, reproducible: bool = True):
+        self.Reproducible = reproducible
+        self.RNGSeed = -1
+
+    def setReproducibleSeed(self, seed: int):
+        self.RNGSeed = int(seed)
+        self.Reproducible = True
+
+    def setReproducible(self, rep: bool):
+        self.Reproducible = rep
+
+
+class sphericalVertexModel:
+    """GPU spherical vertex model; N counts CELLS as in the reference constructor
+    (sphericalVertexModel.cpp:5-82)."""
+
+    def __init__(self, n: int, noise: noiseSource | None = None, a0: float = 1.0, p0: float = 3.8,
+                 useGPU: bool = True, neverGPU: bool = False, ringCapacity: int = 16, stream=None,
+                 topology: Topology | None = None, radius: float | None = None):
+        if not useGPU or neverGPU:
+            raise ValueError("this model runs on the GPU only")
+        self.nCells = int(n)
+        self.noise = noise or noiseSource(True)
+        if topology is None:
+            centres = random_cell_centres(self.noise.RNGSeed, self.nCells)
+            topology = Topology(centres)
+        self.topology = topology
+        self.nVertices = topology.nVertices
+        self.radius = math.sqrt(self.nCells / (4.0 * PI)) if radius is None else float(radius)
+        cap = max(int(ringCapacity), topology.maxRing + 1)
+        self.ringCapacity = cap
+        h = C.c_void_p()
+        call("svm_model_create", self.nCells, self.nVertices, cap, self.radius,
+             C.c_void_p(stream) if stream else None, C.byref(h))
+        self._h = h
+        call("svm_model_set_topology", h, np.ascontiguousarray(topology.vertexPositions).reshape(-1),
+             np.ascontiguousarray(topology.rings).reshape(-1), topology.rings.shape[1], topology.ringCounts,
+             np.ascontiguousarray(topology.vertexCells).reshape(-1),
+             np.ascontiguousarray(topology.vertexNeighbors).reshape(-1))
+        self._restricted = False
+        self.t1Threshold = 0.1
+        call("svm_model_set_t1_threshold", h, 0.1)
+        self.setPreferredParameters(a0, p0)
+        self.setScalarModelParameter(1.0)
+        self.computeGeometry()
+
+    # ---- lifetime ----
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().svm_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- parameters (sphericalVertexModel.h:80-90, simpleModel.h:145) ----
+    def setPreferredParameters(self, a0: float, p0: float):
+        call("svm_model_set_preferred_parameters", self._h, float(a0), float(p0))
+
+    def setPreferredParameterArray(self, a0p0: np.ndarray):
+        call("svm_model_set_preferred_array", self._h, np.ascontiguousarray(a0p0, dtype=np.float64).reshape(-1))
+
+    def setScalarModelParameter(self, kr: float):
+        self.Kr = float(kr)
+        call("svm_model_set_scalar_model_parameter", self._h, self.Kr)
+
+    def setT1Threshold(self, t: float):
+        self.t1Threshold = float(t)
+        call("svm_model_set_t1_threshold", self._h, self.t1Threshold)
+
+    @property
+    def restrictedMotion(self) -> bool:
+        return self._restricted
+
+    @restrictedMotion.setter
+    def restrictedMotion(self, r: bool):
+        self._restricted = bool(r)
+        call("svm_model_set_restricted_motion", self._h, int(self._restricted))
+
+    def getNumberOfParticles(self) -> int:
+        return self.nVertices
+
+    # ---- the path ----
+    def computeGeometry(self):
+        call("svm_model_compute_geometry", self._h)
+
+    def computeForces(self, zeroOutForces: bool = True):
+        call("svm_model_compute_forces", self._h)
+
+    def computeEnergy(self) -> float:
+        e = C.c_double()
+        call("svm_model_compute_energy", self._h, C.byref(e))
+        return e.value
+
+    def moveParticles(self, displacements: np.ndarray, scale: float = 1.0):
+        call("svm_model_move_particles_host", self._h, np.ascontiguousarray(displacements, dtype=np.float64).reshape(-1),
+             float(scale))
+
+    def enforceTopology(self):
+        call("svm_model_enforce_topology", self._h)
+
+    # ---- state access ----
+    def _vec(self, fn, n):
+        out = np.empty(3 * n)
+        call(fn, self._h, out)
+        return out.reshape(n, 3)
+
+    def returnPositions(self) -> np.ndarray:
+        return self._vec("svm_model_get_positions", self.nVertices)
+
+    def setPositions(self, p: np.ndarray):
+        call("svm_model_set_positions", self._h, np.ascontiguousarray(p, dtype=np.float64).reshape(-1))
+
+    def returnForces(self) -> np.ndarray:
+        return self._vec("svm_model_get_forces", self.nVertices)
+
+    def returnVelocities(self) -> np.ndarray:
+        return self._vec("svm_model_get_velocities", self.nVertices)
+
+    def setVelocities(self, v: np.ndarray):
+        call("svm_model_set_velocities", self._h, np.ascontiguousarray(v, dtype=np.float64).reshape(-1))
+
+    def cellPositions(self) -> np.ndarray:
+        return self._vec("svm_model_get_cell_positions", self.nCells)
+
+    def areaPerimeter(self) -> np.ndarray:
+        out = np.empty(2 * self.nCells)
+        call("svm_model_get_area_perimeter", self._h, out)
+        return out.reshape(self.nCells, 2)
+
+    def rings(self, stride: int | None = None):
+        W = stride or self.ringCapacity
+        out = np.empty(self.nCells * W, dtype=np.int32)
+        cnt = np.empty(self.nCells, dtype=np.uint32)
+        call("svm_model_get_rings", self._h, out, W, cnt)
+        return out.reshape(self.nCells, W), cnt
+
+    def vertexCellNeighbors(self) -> np.ndarray:
+        out = np.empty(3 * self.nVertices, dtype=np.int32)
+        call("svm_model_get_vertex_cells", self._h, out)
+        return out.reshape(-1, 3)
+
+    def vertexNeighbors(self) -> np.ndarray:
+        out = np.empty(3 * self.nVertices, dtype=np.int32)
+        call("svm_model_get_vertex_neighbors", self._h, out)
+        return out.reshape(-1, 3)
+
+    def deviceStatus(self) -> int:
+        st = C.c_int()
+        call("svm_model_status", self._h, C.byref(st))
+        return st.value
+
+    def takeFlips(self, capacity: int = 1 << 16) -> np.ndarray:
+        out = np.empty(2 * capacity, dtype=np.int32)
+        n = C.c_int()
+        call("svm_model_take_flips", self._h, out, capacity, C.byref(n))
+        return out[: 2 * min(n.value, capacity)].reshape(-1, 2)
+
+    def synchronize(self):
+        call("svm_model_synchronize", self._h)
+
+
+class brownianDynamics:
+    """Overdamped Brownian updater (brownianDynamics.h:11-29)."""
+
+    def __init__(self, reproducible: bool = True):
+        self.temperature = 0.0
+        self.deltaT = 0.01
+        self.mu = 1.0
+        self.reproducible = reproducible
+        self.noise = noiseSource(reproducible)
+        self.model: sphericalVertexModel | None = None
+        self._injected = None
+
+    def setModel(self, model: sphericalVertexModel):
+        self.model = model
+
+    def setT(self, T: float):
+        self.temperature = float(T)
+
+    def setDeltaT(self, dt: float):
+        self.deltaT = float(dt)
+
+    def injectNoise(self, xi: np.ndarray | None):
+        """Standard normals for the next step ([Nv,3], vertex-major), e.g. the reference's stream."""
+        self._injected = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64).reshape(-1)
+
+    def _seed(self) -> int:
+        return self.noise.RNGSeed if self.noise.RNGSeed >= 0 else 1337
+
+    def integrateEquationOfMotion(self):
+        m = self.model
+        if self._injected is not None:
+            call("svm_brownian_step_host_noise", m.handle, self.temperature, self.deltaT, self.mu, self._injected)
+            self._injected = None
+        else:
+            call("svm_brownian_step", m.handle, self.temperature, self.deltaT, self.mu, _lib.SVM_NOISE_PHILOX, None,
+                 self._seed())
+
+    performUpdate = integrateEquationOfMotion
+
+    def run(self, nSteps: int):
+        """nSteps timesteps as one graph-captured launch sequence (Philox noise)."""
+        call("svm_brownian_run", self.model.handle, self.temperature, self.deltaT, self.mu, self._seed(), int(nSteps))
+
+
+class energyMinimizerFIRE:
+    """FIRE minimiser (energyMinimizerFIRE.h:27-68) with device-side control."""
+
+    def __init__(self, model: sphericalVertexModel):
+        self.model = model
+        self._h = None
+        self.params = dict(dt=0.01, alphaStart=0.99, dtMax=0.1, dtInc=1.05, dtDec=0.95, alphaDec=0.9, nMin=5,
+                           forceCutoff=1e-7, alphaMin=0.0)
+        self.maxIterations = 1000
+        self.criterion = _lib.SVM_FIRE_RMS_OVER_N
+        self._last = (0, 100.0)
+
+    def setFIREParameters(self, deltaT, alphaStart, deltaTMax, deltaTInc, deltaTDec, alphaDec, nMin, forceCutoff,
+                          alphaMin=0.75):
+        self.params = dict(dt=deltaT, alphaStart=alphaStart, dtMax=deltaTMax, dtInc=deltaTInc, dtDec=deltaTDec,
+                           alphaDec=alphaDec, nMin=nMin, forceCutoff=forceCutoff, alphaMin=alphaMin)
+        self._reset()
+
+    def setMaximumIterations(self, n: int):
+        self.maxIterations = int(n)
+        self._reset()
+
+    def setForceCutoff(self, fc: float):
+        self.params["forceCutoff"] = float(fc)
+        self._reset()
+
+    def setCriterion(self, criterion: int):
+        self.criterion = int(criterion)
+
+    def _reset(self):
+        if self._h:
+            _lib.lib().svm_fire_destroy(self._h)
+            self._h = None
+
+    def _ensure(self):
+        if self._h is None:
+            p = self.params
+            h = C.c_void_p()
+            call("svm_fire_create", self.model.handle, p["dt"], p["alphaStart"], p["dtMax"], p["dtInc"], p["dtDec"],
+                 p["alphaDec"], int(p["nMin"]), p["forceCutoff"], p["alphaMin"], self.maxIterations, C.byref(h))
+            self._h = h
+
+    def minimize(self) -> int:
+        self._ensure()
+        it, val = C.c_int(), C.c_double()
+        call("svm_fire_minimize", self._h, self.criterion, C.byref(it), C.byref(val))
+        self._last = (it.value, val.value)
+        return it.value
+
+    performUpdate = minimize
+
+    def state(self) -> dict:
+        self._ensure()
+        out = np.empty(7)
+        call("svm_fire_state", self._h, out)
+        return dict(dt=out[0], alpha=out[1], power=out[2], force_rms_over_n=out[3], max_force=out[4],
+                    n_since=int(out[5]), iterations=int(out[6]))
+
+    def getMaxForce(self) -> float:
+        return self.state()["force_rms_over_n"]
+
+    def getCurrentIterations(self) -> int:
+        return self.state()["iterations"]
+
+    def __del__(self):
+        self._reset()
+
+
+class Simulation:
+    """Ordered updaters over one configuration (src/simulation/simulation.{h,cpp})."""
+
+    def __init__(self):
+        self.configuration: sphericalVertexModel | None = None
+        self.updaters = []
+        self.integerTimestep = 0
+        self.Time = 0.0
+        self.integrationTimestep = 0.01
+
+    def setConfiguration(self, config: sphericalVertexModel):
+        self.configuration = config
+
+    def addUpdater(self, upd, config=None):
+        if config is not None and hasattr(upd, "setModel"):
+            upd.setModel(config)
+        self.updaters.append(upd)
+
+    def setIntegrationTimestep(self, dt: float):
+        self.integrationTimestep = float(dt)
+        for u in self.updaters:
+            if hasattr(u, "setDeltaT"):
+                u.setDeltaT(dt)
+
+    def setCPUOperation(self, setcpu: bool):
+        if setcpu:
+            raise ValueError("CPU operation is not available: this path runs on the GPU only")
+
+    def setReproducible(self, reproducible: bool):
+        for u in self.updaters:
+            if hasattr(u, "reproducible"):
+                u.reproducible = reproducible
+
+    def computeForces(self):
+        self.configuration.computeForces(True)
+
+    def moveParticles(self, displacements, scale: float = 1.0):
+        self.configuration.moveParticles(displacements, scale)
+
+    def computeEnergy(self) -> float:
+        return self.configuration.computeEnergy()
+
+    def performTimestep(self):
+        self.integerTimestep += 1
+        self.Time += self.integrationTimestep
+        for u in self.updaters:
+            u.performUpdate()

@@ -1,0 +1,185 @@
+/*
+ * svm.h — C ABI of the GB300 spherical vertex-model step (libsvm.so).
+ *
+ * This is the drop-in boundary for the hot path of DanielMSussman/curvedSpaceVertexModel:
+ * per-cell spherical-polygon geometry, the quadratic area/perimeter vertex forces, T1 edge
+ * flips, the Brownian and FIRE updaters with renormalisation onto the sphere, and the
+ * sphere's cell list.  In the reference these are reached through the model/updater classes
+ * and the free `gpu_*` launcher functions declared in its .cuh headers; each entry point below
+ * cites the reference interface it replaces (paths relative to the reference repository).
+ *
+ * Conventions
+ *   - Every function returns an int status (SVM_OK == 0) and never throws.
+ *   - A model owns its device arrays and a CUDA stream; all device work is ordered on that
+ *     stream.  Functions that take or return host arrays synchronise that stream.
+ *   - Host arrays use the reference's layouts: positions and vectors are AoS double[3*n];
+ *     rings are row-major int[nCells*ringStride] in clockwise order seen from outside with
+ *     ringCounts[nCells]; vertex->cell and vertex->vertex lists are int[3*nVertices];
+ *     area/perimeter pairs are double[2*nCells] (area first).
+ *   - Device-side failures (a ring outgrowing its capacity, a full T1 work list, a cell-list
+ *     bin overflow, a bounded wait that ran out) set bits in a device status word instead of
+ *     trapping; svm_model_status() reads and clears it.
+ */
+#ifndef SVM_H
+#define SVM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------------------- */
+#define SVM_OK 0
+#define SVM_ERR_ARG 1          /* invalid argument or handle */
+#define SVM_ERR_CUDA 2         /* CUDA runtime error (launch, copy, allocation) */
+#define SVM_ERR_HULL 3         /* degenerate or invalid convex hull */
+#define SVM_ERR_DEVICE 4       /* device status word non-zero; see SVM_DEV_* bits */
+#define SVM_ERR_NO_DEVICE 5    /* no CUDA device */
+
+/* device status word bits (svm_model_status) */
+#define SVM_DEV_RING_OVERFLOW 0x1   /* a T1 would grow a ring beyond its capacity */
+#define SVM_DEV_T1_OVERFLOW 0x2     /* T1 bookkeeping capacity exceeded */
+#define SVM_DEV_CELLLIST_OVERFLOW 0x4 /* more points in a bin than the slot table holds */
+#define SVM_DEV_BAD_TOPOLOGY 0x8    /* an edge's cells could not be classified */
+
+/* Noise sources of the Brownian step. */
+#define SVM_NOISE_PHILOX 0     /* in-kernel counter-based Philox4x32-10 + Box-Muller */
+#define SVM_NOISE_BUFFER 1     /* standard normals supplied by the caller, vertex-major [3*Nv] */
+
+/* FIRE stopping criteria. */
+#define SVM_FIRE_RMS_OVER_N 0  /* the reference's sqrt(sum_i |F_i|^2) / N (energyMinimizerFIRE.cpp:140) */
+#define SVM_FIRE_MAX_FORCE 1   /* max_i |F_i| */
+
+const char* svm_status_string(int status);
+int svm_device_count(int* count);
+
+/* Cell centres of the reference's initialisation: n points uniform on the unit sphere drawn from
+ * std::mt19937(seed) through std::uniform_real_distribution<double> (theta = acos(2v-1),
+ * phi = 2 pi u; sphericalModel::setParticlePositionsRandomly, src/model/sphericalModel.cpp:37-51),
+ * then scaled to R = sqrt(n / 4 pi) (sphericalVertexModel.cpp:12).  seed < 0 keeps the default
+ * engine seed 13377 (src/utilities/noiseSource.h:24).  out: double[3n]. */
+int svm_random_cell_centres(int seed, int n, double* out);
+
+/* ---- initial topology (host) ------------------------------------------------------------
+ * Replaces convexHullCGALInterface::sphericalConvexHullForVertexModel
+ * (src/model/convexHullCGAL.cpp:82-186): hull of the cell centres, one vertex per facet at the
+ * normalised facet centroid, CCW vertex->cell / vertex->vertex slots, clockwise cell rings. */
+typedef struct svm_topology svm_topology;
+int svm_topology_from_points(const double* cellCentres, int nCells, svm_topology** out);
+/* Same contract from caller-supplied hull triangles (CCW seen from outside, int[3*nTri]). */
+int svm_topology_from_triangles(const double* cellCentres, int nCells, const int* triangles, int nTriangles,
+                                svm_topology** out);
+int svm_topology_sizes(const svm_topology* t, int* nCells, int* nVertices, int* maxRing);
+int svm_topology_get(const svm_topology* t, double* vertexPos, int* rings, int ringStride,
+                     unsigned* ringCounts, int* vertexCells, int* vertexNeighbors);
+void svm_topology_free(svm_topology* t);
+
+/* ---- model ---------------------------------------------------------------------------------
+ * Device-resident state of sphericalVertexModel (src/model/sphericalVertexModel.h:10-123).
+ * ringCapacity is the fixed per-cell ring capacity (the reference grows its ring width on
+ * demand, sphericalVertexModel.cpp:733-758; here a ring that would outgrow the capacity sets
+ * SVM_DEV_RING_OVERFLOW).  stream may be NULL (the model then creates its own stream). */
+typedef struct svm_model svm_model;
+int svm_model_create(int nCells, int nVertices, int ringCapacity, double radius, void* stream, svm_model** out);
+int svm_model_destroy(svm_model* m);
+/* Upload topology and positions (host arrays, reference layouts). */
+int svm_model_set_topology(svm_model* m, const double* vertexPos, const int* rings, int ringStride,
+                           const unsigned* ringCounts, const int* vertexCells, const int* vertexNeighbors);
+/* setPreferredParameters (sphericalVertexModel.cpp:103-109) and a per-cell variant. */
+int svm_model_set_preferred_parameters(svm_model* m, double a0, double p0);
+int svm_model_set_preferred_array(svm_model* m, const double* a0p0);
+/* setScalarModelParameter (Kr = K_A/K_P, sphericalVertexModel.h:85) */
+int svm_model_set_scalar_model_parameter(svm_model* m, double kr);
+/* setT1Threshold (sphericalVertexModel.h:87) */
+int svm_model_set_t1_threshold(svm_model* m, double threshold);
+/* simpleModel::restrictedMotion (src/model/simpleModel.h:145): no T1 when non-zero */
+int svm_model_set_restricted_motion(svm_model* m, int restricted);
+
+/* computeGeometry -> gpu_spherical_vertex_model_geometry (sphericalVertexModel.cuh:21-35),
+ * with the CPU path's total-area check and triangle fallback (sphericalVertexModel.cpp:304-310). */
+int svm_model_compute_geometry(svm_model* m);
+/* computeForces -> gpu_quadratic_spherical_cellular_force (sphericalVertexModel.cuh:37-51). */
+int svm_model_compute_forces(svm_model* m);
+/* computeEnergy (sphericalVertexModel.cpp:150-160): sum_c Kr (A-A0)^2 + (P-P0)^2; synchronises. */
+int svm_model_compute_energy(svm_model* m, double* energy);
+/* moveParticles -> gpu_move_particles_on_sphere (sphericalVertexModel.cuh:14-19) followed by
+ * enforceTopology unless motion is restricted.  disp is a DEVICE pointer to double[3*Nv]. */
+int svm_model_move_particles(svm_model* m, const double* dispDevice, double scale);
+/* Same with a host displacement array (copied on the model's stream). */
+int svm_model_move_particles_host(svm_model* m, const double* disp, double scale);
+/* enforceTopology -> gpu_vm_test_edges_for_T1 + gpu_vm_parse_multiple_flips + gpu_vm_flip_edges
+ * (sphericalVertexModel.cuh:53-93), with the CPU path's sequential flip order. */
+int svm_model_enforce_topology(svm_model* m);
+
+/* Host getters/setters (synchronise). */
+int svm_model_get_positions(svm_model* m, double* out);
+int svm_model_set_positions(svm_model* m, const double* in);
+int svm_model_get_forces(svm_model* m, double* out);
+int svm_model_get_velocities(svm_model* m, double* out);
+int svm_model_set_velocities(svm_model* m, const double* in);
+int svm_model_get_area_perimeter(svm_model* m, double* out);
+int svm_model_get_cell_positions(svm_model* m, double* out);
+int svm_model_get_rings(svm_model* m, int* rings, int ringStride, unsigned* ringCounts);
+int svm_model_get_vertex_cells(svm_model* m, int* out);
+int svm_model_get_vertex_neighbors(svm_model* m, int* out);
+/* Device status word (SVM_DEV_* bits); read and cleared. */
+int svm_model_status(svm_model* m, int* deviceStatus);
+/* T1 flips performed since the last call, as (vertex1, vertex2) pairs in the order they were
+ * applied; *count receives the total (pairs beyond `capacity` are dropped). */
+int svm_model_take_flips(svm_model* m, int* pairs, int capacity, int* count);
+int svm_model_synchronize(svm_model* m);
+/* Device pointers of the model's arrays (double4 positions / forces, etc.) for callers that
+ * keep data on the GPU.  Valid until svm_model_destroy. */
+int svm_model_device_positions(svm_model* m, void** ptr);
+
+/* ---- Brownian dynamics ---------------------------------------------------------------------
+ * brownianDynamics::integrateEOMGPU (src/updaters/brownianDynamics.cpp:14-27) ->
+ * gpu_brownian_eom_integration (brownianDynamics.cuh:15-22): forces, then
+ * disp = sqrt(2 dt mu T) xi + dt mu F, then moveParticles.  One call = one timestep.
+ * noiseMode SVM_NOISE_BUFFER reads standard normals from noise (DEVICE pointer, [3*Nv]);
+ * SVM_NOISE_PHILOX draws them in-kernel from (seed, the model's step counter, vertex). */
+int svm_brownian_step(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noiseDevice,
+                      uint64_t seed);
+/* Same with host-supplied standard normals (copied on the model's stream). */
+int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, const double* noise);
+/* nSteps timesteps with Philox noise, launched as a captured CUDA graph. */
+int svm_brownian_run(svm_model* m, double T, double dt, double mu, uint64_t seed, int nSteps);
+
+/* ---- FIRE ----------------------------------------------------------------------------------
+ * energyMinimizerFIRE (src/updaters/energyMinimizerFIRE.{h,cpp}) over velocityVerlet
+ * (src/updaters/velocityVerlet.cpp:40-59): setFIREParameters (energyMinimizerFIRE.cpp:203-214),
+ * minimize (180-200).  Reductions and the dt/alpha control run on the device. */
+typedef struct svm_fire svm_fire;
+int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, double dtInc, double dtDec,
+                    double alphaDec, int nMin, double forceCutoff, double alphaMin, int maxIterations,
+                    svm_fire** out);
+int svm_fire_destroy(svm_fire* f);
+/* Runs until the criterion drops to forceCutoff or maxIterations; returns the iterations done
+ * by this call and the final value of the criterion. */
+int svm_fire_minimize(svm_fire* f, int criterion, int* iterations, double* criterionValue);
+/* state: dt, alpha, power, rms_over_n, max_force, n_since, iterations (7 doubles). */
+int svm_fire_state(svm_fire* f, double* state7);
+
+/* ---- cell list -----------------------------------------------------------------------------
+ * hyperrectangularCellList (src/utilities/hyperrectangularCellList.{h,cpp}): cubic grid over
+ * [-radius, radius]^3 with side count floor(2 radius / a) made even, bin_d = floor((x_d +
+ * radius) / h).  Points of a bin are listed in ascending index, as computeCPU does (165-214). */
+typedef struct svm_cell_list svm_cell_list;
+int svm_cell_list_create(double a, double radius, int nPoints, int slotCapacity, void* stream, svm_cell_list** out);
+int svm_cell_list_destroy(svm_cell_list* cl);
+/* Bins the model's current vertex positions (computeCellList -> gpu_compute_cell_list,
+ * hyperrectangularCellList.cuh:18-30). */
+int svm_cell_list_compute_model(svm_cell_list* cl, svm_model* m);
+/* Bins caller points (DEVICE double[3*n] AoS). */
+int svm_cell_list_compute(svm_cell_list* cl, const double* pointsDevice, int n);
+/* nside, Nmax (the reference's grow-only width), per-bin counts [nside^3] and the slot table
+ * [nside^3 * Nmax] (ascending point index, -1 past the count); synchronises. */
+int svm_cell_list_get(svm_cell_list* cl, int* nside, int* nmax, unsigned* counts, int* slots, long slotsCapacity);
+int svm_cell_list_bins(svm_cell_list* cl, int* binOfPoint);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SVM_H */

@@ -296,6 +296,7 @@ def ref_lib():
              C.c_double, C.c_int, C.c_double, C.c_double, C.c_int)
         _sig(lib, "ref_fire_iterations", C.c_int, vp)
         _sig(lib, "ref_fire_force", C.c_double, vp)
+        _sig(lib, "ref_fire_set_max_iterations", None, vp, C.c_int)
         _sig(lib, "ref_steps", None, vp, C.c_int)
         _sig(lib, "ref_set_restricted", None, vp, C.c_int)
         _sig(lib, "ref_set_preferred", None, vp, C.c_double, C.c_double)

@@ -62,6 +62,7 @@ void ref_fire_setup(ref_handle* h, double dt, double alphaStart, double dtMax, d
     h->sim->setCPUOperation(true);
 }
 int ref_fire_iterations(ref_handle* h) { return h->fire->getCurrentIterations(); }
+void ref_fire_set_max_iterations(ref_handle* h, int n) { h->fire->setMaximumIterations(n); }
 double ref_fire_force(ref_handle* h) { return h->fire->getMaxForce(); }
 
 void ref_steps(ref_handle* h, int n) { for (int i = 0; i < n; ++i) h->sim->performTimestep(); }

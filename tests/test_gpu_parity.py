@@ -1,0 +1,261 @@
+"""Parity of the GPU path (libsvm through its C ABI) with the CPU oracle and the reference's golden
+fixtures.  FP64 tolerances are stated per test; connectivity and the T1 flip set are compared
+exactly."""
+import numpy as np
+import pytest
+
+from gpu_helpers import gpu_model, load_gold, oracle_model, params, rel_err, same_rings
+
+pytestmark = pytest.mark.gpu
+
+# The benchmark spec's bar for the FP64 form after 1000 steps: 1e-12 relative.
+RTOL_TRAJ = 1e-12
+# One evaluation of the geometry/forces differs from the CPU only by rounding (acos, FMA).
+RTOL_EVAL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def svm(svm_lib):
+    if svm_lib.device_count() < 1:
+        pytest.fail("no CUDA device: the GPU tests need a GB300")
+    return svm_lib
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return load_gold()
+
+
+def test_geometry_forces_energy_match_golden(svm, gold):
+    m = gpu_model(svm, gold)
+    m.computeForces()
+    assert rel_err(m.areaPerimeter(), gold["init_ap"]) < RTOL_EVAL
+    assert rel_err(m.cellPositions(), gold["init_cellpos"]) < RTOL_EVAL
+    assert rel_err(m.returnForces(), gold["init_forces"]) < RTOL_EVAL
+    assert abs(m.computeEnergy() - float(gold["init_energy"])) / float(gold["init_energy"]) < RTOL_EVAL
+    assert m.deviceStatus() == 0
+
+
+def test_brownian_1000_steps_match_oracle_and_golden(svm, gold, oracle_mod):
+    """Config 1: N=200, T=0.01, dt=0.01, T1 threshold 0.04, the reference's mt19937 noise stream
+    injected into both sides; positions/areas/perimeters/energy within 1e-12 relative after 1000
+    steps, connectivity and the ordered T1 flip list exact."""
+    p = params(gold)
+    gm = gpu_model(svm, gold)
+    om = oracle_model(oracle_mod, gold)
+    bd = svm.brownianDynamics()
+    bd.setModel(gm)
+    bd.setT(p["T"])
+    bd.setDeltaT(p["dt"])
+    bd.mu = p["mu"]
+    noise = oracle_mod.OracleNoise(p["bd_seed"])
+    nv = gm.nVertices
+    total_flips = 0
+    for step in range(1, 1001):
+        xi = noise.normals(3 * nv)
+        bd.injectNoise(xi)
+        bd.integrateEquationOfMotion()
+        om.brownian_step_noise(xi, p["T"], p["dt"], p["mu"])
+        f_gpu = gm.takeFlips()
+        f_orc = om.flips()
+        assert np.array_equal(f_gpu, f_orc), f"T1 flips differ at step {step}: {f_gpu} vs {f_orc}"
+        total_flips += len(f_orc)
+        if step in (1, 10, 100, 1000):
+            assert same_rings(gm, om), step
+            assert np.array_equal(gm.vertexCellNeighbors(), om.vertex_cells()), step
+            assert np.array_equal(gm.vertexNeighbors(), om.vertex_neighbors()), step
+            R = float(gold["init_radius"])
+            assert rel_err(gm.returnPositions(), om.positions(), R) < RTOL_TRAJ, step
+            gm.computeGeometry()
+            om.compute_geometry()
+            assert rel_err(gm.areaPerimeter(), om.area_perimeter()) < RTOL_TRAJ, step
+            e_g, e_o = gm.computeEnergy(), om.energy()
+            assert abs(e_g - e_o) / e_o < RTOL_TRAJ, step
+            # and the fixtures made from the reference itself
+            g = f"s{step}_"
+            assert rel_err(gm.returnPositions(), gold[g + "pos"], R) < RTOL_TRAJ, step
+            assert abs(e_g - float(gold[g + "energy"])) / float(gold[g + "energy"]) < RTOL_TRAJ, step
+    assert total_flips == len(gold["flips"]) and total_flips > 100
+    assert gm.deviceStatus() == 0
+
+
+def test_forced_t1_matches_oracle(svm, gold, oracle_mod):
+    """A hand-shortened edge: enforceTopology flips it exactly as the CPU does."""
+    g = gold
+    gm = gpu_model(svm, g)
+    om = oracle_model(oracle_mod, g)
+    pos = g["init_pos"].copy()
+    nbrs = g["init_vnbrs"]
+    edits = []
+    for v in (3, 40, 101, 250):
+        u = int(nbrs[v][0])
+        pos[u] = pos[v] + 0.02 * (pos[u] - pos[v])
+        pos[u] *= float(g["init_radius"]) / np.linalg.norm(pos[u])
+        edits.append((min(u, v), max(u, v)))
+    gm.setPositions(pos)
+    om.set_positions(pos)
+    gm.enforceTopology()
+    om.lib.orc_enforce_topology(om.h)
+    fg, fo = gm.takeFlips(), om.flips()
+    assert len(fo) >= 3 and np.array_equal(fg, fo)
+    assert same_rings(gm, om)
+    assert np.array_equal(gm.vertexCellNeighbors(), om.vertex_cells())
+    assert np.array_equal(gm.vertexNeighbors(), om.vertex_neighbors())
+    assert rel_err(gm.returnPositions(), om.positions(), float(g["init_radius"])) < 1e-14
+    gm.computeForces()
+    om.compute_forces()
+    assert rel_err(gm.returnForces(), om.forces()) < RTOL_EVAL
+
+
+def test_cell_list_matches_golden(svm, gold):
+    import ctypes as C
+    from curvedspacevertexmodel_gb300 import _lib
+    gm = gpu_model(svm, gold, "s1000_")
+    R = float(gold["init_radius"])
+    h = C.c_void_p()
+    _lib.call("svm_cell_list_create", 1.0, R + 2.5, gm.nVertices, 16, None, C.byref(h))
+    try:
+        _lib.call("svm_cell_list_compute_model", h, gm.handle)
+        nside, nmax = C.c_int(), C.c_int()
+        _lib.call("svm_cell_list_get", h, C.byref(nside), C.byref(nmax), None, None, 0)
+        total = nside.value ** 3
+        counts = np.empty(total, dtype=np.uint32)
+        slots = np.empty(total * nmax.value, dtype=np.int32)
+        _lib.call("svm_cell_list_get", h, C.byref(nside), C.byref(nmax), counts, slots, slots.size)
+    finally:
+        _lib.lib().svm_cell_list_destroy(h)
+    assert nside.value == int(gold["cl_nside"]) and nmax.value == int(gold["cl_nmax"])
+    nz = np.nonzero(counts)[0]
+    assert np.array_equal(nz, gold["cl_bins"])
+    assert np.array_equal(counts[nz], gold["cl_counts"])
+    assert np.array_equal(slots.reshape(total, -1)[nz], gold["cl_slots"])
+
+
+def test_cell_list_large_matches_oracle(svm, oracle_mod):
+    import ctypes as C
+    from curvedspacevertexmodel_gb300 import _lib
+    n = 20000
+    m = svm.sphericalVertexModel(n, svm.noiseSource())
+    R = m.radius
+    pts = m.returnPositions()
+    ref = oracle_mod.oracle_cell_list(pts, 1.0, R + 2.5)
+    h = C.c_void_p()
+    _lib.call("svm_cell_list_create", 1.0, R + 2.5, m.nVertices, 16, None, C.byref(h))
+    try:
+        for _ in range(2):  # the second call exercises the incremental clear
+            _lib.call("svm_cell_list_compute_model", h, m.handle)
+        nside, nmax = C.c_int(), C.c_int()
+        _lib.call("svm_cell_list_get", h, C.byref(nside), C.byref(nmax), None, None, 0)
+        total = nside.value ** 3
+        counts = np.empty(total, dtype=np.uint32)
+        slots = np.empty(total * nmax.value, dtype=np.int32)
+        _lib.call("svm_cell_list_get", h, C.byref(nside), C.byref(nmax), counts, slots, slots.size)
+        bins = np.empty(m.nVertices, dtype=np.int32)
+        _lib.call("svm_cell_list_bins", h, bins)
+    finally:
+        _lib.lib().svm_cell_list_destroy(h)
+    assert nmax.value == ref["nmax"]
+    assert np.array_equal(bins, ref["bins"])
+    assert np.array_equal(counts, ref["counts"])
+    assert np.array_equal(slots.reshape(total, -1), ref["idx"])
+
+
+def test_fire_matches_oracle_and_golden(svm, gold, oracle_mod):
+    """FIRE from the Brownian snapshot (T1 off): 100 iterations close to the oracle, and the full
+    quench reaching the reference's final energy."""
+    g = gold
+    fp = g["fire_params"]
+    gm = gpu_model(svm, g, "s1000_")
+    gm.restrictedMotion = True
+    fire = svm.energyMinimizerFIRE(gm)
+    fire.setFIREParameters(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], int(fp[6]), fp[7], fp[8])
+    fire.setMaximumIterations(100)
+    fire.minimize()
+    R = float(g["init_radius"])
+    om = oracle_model(oracle_mod, g, "s1000_")
+    om.set_restricted(True)
+    of = oracle_mod.OracleFire(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], int(fp[6]), fp[7], fp[8], 100)
+    of.minimize(om, 0)
+    assert fire.getCurrentIterations() == 100
+    assert rel_err(gm.returnPositions(), om.positions(), R) < 1e-10
+    assert rel_err(gm.returnPositions(), g["fire100_pos"], R) < 1e-10
+    st, ost = fire.state(), of.state()
+    assert abs(st["dt"] - ost["dt"]) < 1e-12 and abs(st["alpha"] - ost["alpha"]) < 1e-12
+    # the full quench
+    fire.setMaximumIterations(int(fp[9]))
+    gm2 = gpu_model(svm, g, "s1000_")
+    gm2.restrictedMotion = True
+    fire2 = svm.energyMinimizerFIRE(gm2)
+    fire2.setFIREParameters(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], int(fp[6]), fp[7], fp[8])
+    fire2.setMaximumIterations(int(fp[9]))
+    fire2.minimize()
+    gm2.computeGeometry()
+    e = gm2.computeEnergy()
+    assert abs(e - float(g["fire_energy"])) / float(g["fire_energy"]) < 1e-8
+
+
+def test_graph_run_equals_step_loop(svm, gold):
+    """svm_brownian_run (captured graph) reproduces svm_brownian_step bit for bit."""
+    a = gpu_model(svm, gold)
+    b = gpu_model(svm, gold)
+    for m in (a, b):
+        m.setPreferredParameters(1.0, 3.8)
+    bda, bdb = svm.brownianDynamics(), svm.brownianDynamics()
+    for bd, m in ((bda, a), (bdb, b)):
+        bd.setModel(m)
+        bd.setT(0.01)
+        bd.noise.setReproducibleSeed(77)
+    for _ in range(37):
+        bda.integrateEquationOfMotion()
+    bdb.run(37)
+    assert np.array_equal(a.returnPositions(), b.returnPositions())
+    assert np.array_equal(a.vertexNeighbors(), b.vertexNeighbors())
+    r1, c1 = a.rings()
+    r2, c2 = b.rings()
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+
+
+def test_philox_noise_statistics(svm):
+    """Brownian displacements with negligible forces: tangential variance 2 dt mu T per direction."""
+    n = 20000
+    m = svm.sphericalVertexModel(n, svm.noiseSource())
+    m.setScalarModelParameter(0.0)
+    m.setPreferredParameters(1.0, 0.0)  # forces ~ 2 P dP are O(10); T large makes them negligible
+    m.restrictedMotion = True
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    T, dt = 1e6, 1e-8
+    bd.setT(T)
+    bd.setDeltaT(dt)
+    p0 = m.returnPositions()
+    bd.integrateEquationOfMotion()
+    d = m.returnPositions() - p0
+    var = np.mean(np.sum(d * d, axis=1)) / 2.0  # two tangential directions
+    assert abs(var / (2 * dt * T) - 1.0) < 0.03
+
+
+def test_large_sphere_invariants(svm):
+    """Size-independent properties at N = 20k over 200 noisy steps with T1: total area 4 pi R^2,
+    tangential forces, trivalent connectivity, rings consistent with the vertex lists."""
+    n = 20000
+    m = svm.sphericalVertexModel(n, svm.noiseSource())
+    m.setT1Threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.setT(0.01)
+    bd.noise.setReproducibleSeed(5)
+    bd.run(200)
+    m.computeForces()
+    ap = m.areaPerimeter()
+    R = m.radius
+    assert abs(ap[:, 0].sum() - 4 * np.pi * R * R) / (4 * np.pi * R * R) < 1e-9
+    p, f = m.returnPositions(), m.returnForces()
+    radial = np.abs(np.sum(p * f, axis=1)) / R
+    assert np.max(radial) < 1e-9 * max(1.0, np.max(np.abs(f)))
+    rings, counts = m.rings()
+    vc = m.vertexCellNeighbors()
+    assert counts.sum() == 3 * m.nVertices
+    for c in range(0, n, 97):
+        for v in rings[c, : counts[c]]:
+            assert c in vc[v]
+    assert m.deviceStatus() == 0

@@ -1,0 +1,121 @@
+"""CPU tests of the host side: the spherical hull / initial topology (against scipy's qhull and
+the Euler counts), the product's random cell centres (against the oracle restatement of the
+reference recipe), and the C ABI (the library loads and exports every symbol include/svm.h
+declares; no device work)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def svm(svm_lib):
+    return svm_lib
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "svm.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(svm_\w+)\s*\(", text, re.M)))
+
+
+def test_abi_exports_every_declared_symbol(svm):
+    lib = ctypes.CDLL(svm.LIBPATH)
+    names = declared_symbols()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_abi(svm):
+    from curvedspacevertexmodel_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_cell_centres_match_reference_recipe(svm, oracle_mod):
+    for seed, n in ((1137, 200), (5, 1000)):
+        a = svm.random_cell_centres(seed, n)
+        b = oracle_mod.OracleNoise(seed).cell_centres(n)
+        assert np.array_equal(a, b)
+        R = np.sqrt(n / (4 * svm.PI))
+        assert np.allclose(np.linalg.norm(a, axis=1), R, rtol=1e-14)
+
+
+@pytest.mark.parametrize("n,seed", [(12, 1), (200, 1137), (2000, 9), (20000, 3)])
+def test_topology_against_qhull(svm, n, seed):
+    spatial = pytest.importorskip("scipy.spatial")
+    pts = svm.random_cell_centres(seed, n)
+    topo = svm.Topology(pts)
+    assert topo.nVertices == 2 * n - 4
+    # the same triangle set as qhull
+    hull = spatial.ConvexHull(pts)
+    ours = set()
+    cells = topo.vertexCells
+    for f in range(topo.nVertices):
+        ours.add(tuple(sorted(cells[f])))
+    theirs = {tuple(sorted(s)) for s in hull.simplices}
+    assert ours == theirs
+    # Euler / incidence invariants
+    counts = topo.ringCounts.astype(int)
+    assert counts.sum() == 3 * topo.nVertices
+    for c in range(0, n, max(1, n // 50)):
+        ring = topo.rings[c, : counts[c]]
+        for v in ring:
+            assert c in cells[v]
+    # vertices are the renormalised facet centroids
+    R = np.linalg.norm(pts[0])
+    cen = pts[cells].mean(axis=1)
+    assert np.allclose(topo.vertexPositions, R * cen / np.linalg.norm(cen, axis=1, keepdims=True), rtol=1e-12)
+    # vertex -> vertex slot k is the facet across the edge ending at corner k
+    nbrs = topo.vertexNeighbors
+    for f in range(0, topo.nVertices, max(1, topo.nVertices // 200)):
+        for k in range(3):
+            g = nbrs[f, k]
+            shared = set(cells[f]) & set(cells[g])
+            assert shared == {cells[f][(k + 2) % 3], cells[f][k]}
+
+
+def test_rings_are_clockwise_from_outside(svm):
+    pts = svm.random_cell_centres(1137, 200)
+    topo = svm.Topology(pts)
+    p = topo.vertexPositions
+    for c in range(200):
+        ring = topo.rings[c, : topo.ringCounts[c]]
+        # signed area of the ring polygon about the outward normal at the cell centre
+        nrm = pts[c] / np.linalg.norm(pts[c])
+        s = 0.0
+        for k in range(len(ring)):
+            s += np.dot(np.cross(p[ring[k]], p[ring[(k + 1) % len(ring)]]), nrm)
+        assert s < 0  # clockwise seen from outside
+
+
+def test_topology_from_triangles_matches_hull(svm):
+    spatial = pytest.importorskip("scipy.spatial")
+    pts = svm.random_cell_centres(42, 500)
+    hull = spatial.ConvexHull(pts)
+    tri = hull.simplices.copy()
+    # orient CCW seen from outside
+    for t in tri:
+        a, b, c = pts[t]
+        if np.dot(np.cross(b - a, c - a), a) < 0:
+            t[1], t[2] = t[2], t[1]
+    t1 = svm.Topology(pts)
+    t2 = svm.Topology(pts, triangles=tri)
+    for name in ("vertexPositions", "rings", "ringCounts", "vertexCells", "vertexNeighbors"):
+        assert np.array_equal(getattr(t1, name), getattr(t2, name)), name
+
+
+def test_topology_matches_reference_hull_shim(svm, oracle_mod):
+    if not oracle_mod.ref_available():
+        pytest.skip("oracle/_ref not built")
+    ref = oracle_mod.RefModel(200, 1137, 1.0, 3.8, 1.0, 0.04)
+    t = ref.topology()
+    topo = svm.Topology(svm.random_cell_centres(1137, 200))
+    W = t["rings"].shape[1]
+    assert np.array_equal(t["pos"], topo.vertexPositions)
+    assert np.array_equal(t["rings"], topo.rings[:, :W])
+    assert np.array_equal(t["vcells"], topo.vertexCells)
+    assert np.array_equal(t["vnbrs"], topo.vertexNeighbors)

@@ -1,0 +1,154 @@
+"""The CPU oracle pinned against the reference: golden fixtures made from the reference compiled
+from its sources (tests/golden/make_golden.py), and, where oracle/_ref is built, the reference
+itself on further configurations."""
+import platform
+
+import numpy as np
+import pytest
+
+GOLD = "tests/golden/brownian_n200.npz"
+EXACT = platform.machine() in ("x86_64", "AMD64")  # fixtures were generated on x86-64
+
+
+def close(a, b, rtol=1e-12, atol=1e-12):
+    if EXACT:
+        return np.array_equal(a, b)
+    return np.allclose(a, b, rtol=rtol, atol=atol)
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(GOLD))
+
+
+def oracle_from(oracle_mod, g, prefix="init_"):
+    m = oracle_mod.OracleModel(g[prefix + "pos"], g[prefix + "rings"], g[prefix + "counts"], g[prefix + "vcells"],
+                               g[prefix + "vnbrs"], float(g["init_radius"]))
+    N, SEED, BD_SEED, A0, P0, KR, T, MU, DT, T1 = g["params"]
+    m.set_preferred(A0, P0)
+    m.set_kr(KR)
+    m.set_t1_threshold(T1)
+    return m
+
+
+def test_initial_geometry_and_forces(oracle_mod, gold):
+    m = oracle_from(oracle_mod, gold)
+    m.compute_forces()
+    assert close(m.area_perimeter(), gold["init_ap"])
+    assert close(m.cell_positions(), gold["init_cellpos"])
+    assert close(m.forces(), gold["init_forces"])
+    assert close(np.array(m.energy()), gold["init_energy"])
+
+
+def test_brownian_trajectory_matches_reference(oracle_mod, gold):
+    g = gold
+    m = oracle_from(oracle_mod, g)
+    N, SEED, BD_SEED, A0, P0, KR, T, MU, DT, T1 = g["params"]
+    noise = oracle_mod.OracleNoise(int(BD_SEED))
+    flips = []
+    for step in range(1, 1001):
+        m.brownian_step(noise, T, DT, MU)
+        flips.extend((step, a, b) for a, b in m.flips())
+        if step in (1, 10, 100, 1000):
+            p = f"s{step}_"
+            rings, counts = m.rings(16)
+            assert np.array_equal(rings, g[p + "rings"]) and np.array_equal(counts, g[p + "counts"]), step
+            assert np.array_equal(m.vertex_cells(), g[p + "vcells"]), step
+            assert np.array_equal(m.vertex_neighbors(), g[p + "vnbrs"]), step
+            assert close(m.positions(), g[p + "pos"]), step
+            assert close(m.area_perimeter(), g[p + "ap"]), step
+            assert close(np.array(m.energy()), g[p + "energy"]), step
+    assert np.array_equal(np.array(flips, dtype=np.int32).reshape(-1, 3), g["flips"])
+
+
+def test_cell_list_matches_reference(oracle_mod, gold):
+    g = gold
+    R = float(g["init_radius"])
+    cl = oracle_mod.oracle_cell_list(g["s1000_pos"], 1.0, R + 2.5)
+    assert cl["nside"] == int(g["cl_nside"]) and cl["nmax"] == int(g["cl_nmax"])
+    nz = np.nonzero(cl["counts"])[0]
+    assert np.array_equal(nz, g["cl_bins"])
+    assert np.array_equal(cl["counts"][nz], g["cl_counts"])
+    assert np.array_equal(cl["idx"][nz], g["cl_slots"])
+    assert cl["counts"].sum() == g["s1000_pos"].shape[0]
+
+
+def test_fire_matches_reference(oracle_mod, gold):
+    g = gold
+    m = oracle_from(oracle_mod, g, "s1000_")
+    m.set_restricted(True)
+    fp = g["fire_params"]
+    f = oracle_mod.OracleFire(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], int(fp[6]), fp[7], fp[8], 100)
+    f.minimize(m, 0)
+    assert close(m.positions(), g["fire100_pos"])
+    assert close(np.array(f.state()["force_rms_over_n"]), g["fire100_force"])
+    f2 = oracle_mod.OracleFire(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], int(fp[6]), fp[7], fp[8], int(fp[9]))
+    m2 = oracle_from(oracle_mod, g, "s1000_")
+    m2.set_restricted(True)
+    f2.minimize(m2, 0)
+    assert f2.state()["iterations"] == int(g["fire_iterations"])
+    assert close(m2.positions(), g["fire_pos"])
+    m2.compute_geometry()
+    assert close(np.array(m2.energy()), g["fire_energy"])
+
+
+def test_planted_mistake_is_caught(oracle_mod, gold):
+    """A perturbed oracle state must fail the same comparison (the checker is not vacuous)."""
+    g = gold
+    m = oracle_from(oracle_mod, g)
+    p = m.positions()
+    t = np.cross(p[17], [0.0, 0.0, 1.0])
+    p[17] += 1e-8 * t / np.linalg.norm(t)  # tangential: moves the vertex along the sphere
+    m.set_positions(p)
+    m.compute_forces()
+    assert not np.allclose(m.forces(), g["init_forces"], rtol=1e-12, atol=1e-12)
+
+
+# ---- against the reference itself (needs oracle/_ref, built here from the reference sources) ----
+ref_only = pytest.mark.skipif("not __import__('oracle').ref_available()", reason="oracle/_ref not built")
+
+
+@ref_only
+@pytest.mark.parametrize("n,seed,p0,T,t1,steps", [(120, 7, 3.95, 0.05, 0.08, 300), (64, 3, 3.7, 0.02, 0.1, 300)])
+def test_oracle_bit_exact_against_reference(oracle_mod, n, seed, p0, T, t1, steps):
+    ref = oracle_mod.RefModel(n, seed, 1.0, p0, 1.0, t1)
+    topo = ref.topology()
+    m = oracle_mod.OracleModel(topo["pos"], topo["rings"], topo["counts"], topo["vcells"], topo["vnbrs"], topo["radius"])
+    m.set_preferred(1.0, p0)
+    m.set_t1_threshold(t1)
+    ref.bd_setup(seed + 100, T, 0.01, 1.0)
+    noise = oracle_mod.OracleNoise(seed + 100)
+    nflips = 0
+    for step in range(steps):
+        ref.steps(1)
+        m.brownian_step(noise, T, 0.01, 1.0)
+        nflips += len(m.flips())
+        assert np.array_equal(ref.positions(), m.positions()), step
+    r1, c1 = ref.rings(32)
+    r2, c2 = m.rings(32)
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    assert np.array_equal(ref.area_perimeter(), m.area_perimeter())
+    assert ref.energy() == m.energy()
+    assert nflips > 0
+
+
+@ref_only
+def test_area_fallback_against_reference(oracle_mod):
+    """A vertex pushed across its cell makes the angle-sum area wrong; both sides must take the
+    triangle-fan fallback (sphericalVertexModel.cpp:304-310) and agree."""
+    ref = oracle_mod.RefModel(80, 11, 1.0, 3.8, 1.0, 0.04)
+    topo = ref.topology()
+    p = topo["pos"].copy()
+    v = 1
+    nb = topo["vnbrs"][v]
+    p[v] = p[v] + 2.5 * (p[nb[0]] - p[v])  # overshoot a neighbour: the rings fold over
+    p[v] *= ref.radius / np.linalg.norm(p[v])
+    ref.set_positions(p)
+    ref.compute_geometry()
+    m = oracle_mod.OracleModel(p, topo["rings"], topo["counts"], topo["vcells"], topo["vnbrs"], topo["radius"])
+    m.compute_geometry()
+    assert m.fallback_count() == 1 and abs(m.excess_area()) > 1e-6
+    assert np.array_equal(ref.area_perimeter(), m.area_perimeter())
+    ref.compute_forces()
+    m.compute_forces()
+    assert np.array_equal(ref.forces(), m.forces())
