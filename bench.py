@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Benchmark of the spherical vertex-model Brownian step (vertex-steps/s at N = 100k cells).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the configuration the headline metric is quoted on): FP64 plain overdamped Brownian
+dynamics of the spherical vertex model with N = 100,000 cells (199,996 vertices), cell centres
+uniform on the sphere of radius sqrt(N / 4 pi) from a seed, initial vertices from their spherical
+Voronoi tessellation, A0 = 1, P0 = 3.8, K_A = K_P = 1, T = 0.01, mu = 1, dt = 0.01, T1 threshold
+0.04.  A step is one timestep: geometry, forces, Brownian displacement, move onto the sphere and
+T1 flips.  The state is prepared with the reference driver's own recipe (sphericalVertex.cpp:104-125):
+STAB steps at T = 0 with P0 = 1, then the run parameters; from a raw random-Voronoi start at
+N >= 20k the reference model itself develops inverted cells and diverges, while the stabilised
+start relaxes normally.  Timing starts after the stabilisation and an untimed equilibration.
+
+ours: `value` is device-resident throughput over K steps, each timed with CUDA events on the
+model's stream after an L2 flush (the model state, ~40 MB, would otherwise stay in the 129 MB L2);
+`e2e` is the same step through the C ABI with host buffers: H2D of the positions from pinned host
+memory, the step, D2H of the positions and the energy.  Per-phase CUDA events taken during the
+timed steps give the dominant kernel's launch duration for `roofline`.  `cpu_baseline` times the
+CPU oracle (restatement of the reference CPU path, one core as the reference's vertex-model loops
+are serial) on a bounded sample of the same workload from the same equilibrated state.
+
+reference: the CPU restatement of the reference path on all host cores (one independent replica
+per core, since the reference's vertex-model loops are serial), each bench step one timestep of
+every replica.  Under torchrun only rank 0 runs it.
+
+N > 1 GPUs: independent replicas, one per GPU (scaling "weak"); a barrier and the max over ranks
+of the timed region, value = all vertex-steps / that time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS = 100_000
+PARAMS = dict(a0=1.0, p0=3.8, kr=1.0, T=0.01, mu=1.0, dt=0.01, t1=0.04)
+SEED = 1137
+BD_SEED = 4242
+WORKLOAD = ("spherical vertex model, overdamped Brownian step, FP64 plain form, N=100000 cells "
+            "(199996 vertices), A0=1 P0=3.8 KA=KP=1 T=0.01 mu=1 dt=0.01 T1 threshold 0.04, "
+            "seeded Voronoi start")
+METRIC = "vertex-steps/s at N=100k (FP64 Brownian step)"
+UNIT = "vertex-steps/s"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# --------------------------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------------------------
+def algorithmic_bytes_force(nv: int, nc: int) -> int:
+    """Compulsory bytes of one launch of the fused force + Brownian + move kernel, each array it
+    reads or writes counted once: positions in (24 B) and out (24 B), forces out (24 B), the
+    vertex's spherical coordinates (32 B), vertex->cell, ring-predecessor and ring-successor slots
+    (3 x 12 B), and per cell centroid (24 B), its spherical coordinates (32 B), (A, P) (16 B) and
+    (A0, P0) (16 B)."""
+    return nv * (24 + 24 + 24 + 32 + 36) + nc * (24 + 32 + 16 + 16)
+
+
+def algorithmic_bytes_step(nv: int) -> int:
+    """Compulsory bytes of one Brownian step (positions r/w 48, vertex->cell 12, vertex->vertex
+    12, rings 12, ring sizes 2, (A0, P0) 8) = 94 B per vertex-step."""
+    return 94 * nv
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline_sample(state, steps: int):
+    """The CPU oracle on one core, `steps` Brownian steps of the same workload from `state`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build_oracle()
+    m = oracle.OracleModel(state["pos"], state["rings"], state["counts"], state["vcells"], state["vnbrs"],
+                           state["radius"])
+    m.set_preferred(PARAMS["a0"], PARAMS["p0"])
+    m.set_kr(PARAMS["kr"])
+    m.set_t1_threshold(PARAMS["t1"])
+    noise = oracle.OracleNoise(BD_SEED)
+    m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])  # warm caches
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])
+    dt = time.perf_counter() - t0
+    nv = state["pos"].shape[0]
+    return nv * steps / dt, dt
+
+
+# --------------------------------------------------------------------------------------------
+def run_ours(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    import numpy as np
+    import torch
+    import curvedspacevertexmodel_gb300 as svm
+    from curvedspacevertexmodel_gb300 import _lib
+    import ctypes as C
+
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    torch.cuda.set_device(0)
+    n = args.cells
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(SEED + rank)
+    model = svm.sphericalVertexModel(n, noise, PARAMS["a0"], PARAMS["p0"])
+    # every timing event goes on the stream the model's kernels are launched on
+    stream = torch.cuda.ExternalStream(model.streamHandle())
+    model.setScalarModelParameter(PARAMS["kr"])
+    model.setT1Threshold(PARAMS["t1"])
+    nv, nc = model.nVertices, model.nCells
+    bd = svm.brownianDynamics()
+    bd.setModel(model)
+    bd.setT(PARAMS["T"])
+    bd.setDeltaT(PARAMS["dt"])
+    bd.mu = PARAMS["mu"]
+    bd.noise.setReproducibleSeed(BD_SEED + rank)
+    # untimed preparation: stabilisation at T = 0, P0 = 1, then equilibration at the run parameters
+    bd.setT(0.0)
+    model.setPreferredParameters(PARAMS["a0"], 1.0)
+    bd.run(args.stab)
+    bd.setT(PARAMS["T"])
+    model.setPreferredParameters(PARAMS["a0"], PARAMS["p0"])
+    bd.run(args.equil)
+    for _ in range(max(3, args.warmup)):
+        bd.integrateEquationOfMotion()
+    torch.cuda.synchronize()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")  # > L2 (129 MB)
+
+    # ---- timed region: K steps, each after an L2 flush, events on the model's stream ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _lib.call("svm_model_profile", model.handle, 1)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            starts[i].record(stream)
+            bd.integrateEquationOfMotion()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if pg:
+        pg.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = np.zeros(_lib_phase_count(), dtype=np.float64)
+    launches = np.zeros(_lib_phase_count(), dtype=np.int32)
+    _lib.call("svm_model_profile_read", model.handle, ms, launches)
+    _lib.call("svm_model_profile", model.handle, 0)
+    total_ms = float(sum(step_ms))
+    if pg:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * nv * args.steps / (total_ms / 1e3)
+
+    # warm-L2 reference point: K back-to-back steps in one captured run
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    bd.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    warm_ms = e0.elapsed_time(e1) / args.steps
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    host_pos = torch.empty(3 * nv, dtype=torch.float64).pin_memory().numpy()
+    host_out = torch.empty(3 * nv, dtype=torch.float64).pin_memory().numpy()
+    host_pos[:] = model.returnPositions().reshape(-1)
+    energy = C.c_double()
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _lib.call("svm_model_set_positions", model.handle, host_pos)
+        _lib.call("svm_brownian_step", model.handle, PARAMS["T"], PARAMS["dt"], PARAMS["mu"], _lib.SVM_NOISE_PHILOX,
+                  None, BD_SEED + rank)
+        _lib.call("svm_model_get_positions", model.handle, host_out)
+        _lib.call("svm_model_compute_energy", model.handle, C.byref(energy))
+        host_pos, host_out = host_out, host_pos
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * nv * args.steps / e2e_s
+
+    status = model.deviceStatus()
+    model.computeGeometry()
+    energy_per_cell = model.computeEnergy() / nc
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel ----
+    names = _lib.PHASES
+    dom = int(np.argmax(ms))
+    avg_launch_ms = ms[dom] / max(1, launches[dom])
+    peak, peak_kind = peaks()
+    if names[dom] == "force":
+        alg = algorithmic_bytes_force(nv, nc)
+    else:
+        alg = algorithmic_bytes_step(nv)
+    achieved = alg / (avg_launch_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "force_bd_n100k_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("bytes_per_launch")
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        state = dict(pos=model.returnPositions(), radius=model.radius)
+        state["rings"], state["counts"] = model.rings()
+        state["vcells"], state["vnbrs"] = model.vertexCellNeighbors(), model.vertexNeighbors()
+        v, secs = cpu_baseline_sample(state, args.cpu_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_steps} Brownian steps of the same N=100k workload from the same equilibrated "
+                         f"state on one host core ({secs:.1f} s), the reference's serial CPU path restated"}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cell centres, reference init recipe)",
+        "config": {"workload": WORKLOAD, "n_cells": nc, "n_vertices": nv, "stabilisation_steps": args.stab,
+                   "equilibration_steps": args.equil,
+                   "l2": "flushed before every timed step (512 MB write); state is ~40 MB < 129 MB L2",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single sphere, one GPU",
+                   "noise": "in-kernel Philox4x32-10"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * nv, "d2h_bytes_per_step": 24 * nv + 8},
+        "gpu_launches": int(launches.sum()),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": f"k_{names[dom]}", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
+        "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
+        "warm_l2_ms_per_step": warm_ms,
+        "wall_s": wall,
+        "device_status": status,
+        "energy_per_cell": energy_per_cell,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _lib_phase_count():
+    from curvedspacevertexmodel_gb300 import _lib
+    return len(_lib.PHASES)
+
+
+# --------------------------------------------------------------------------------------------
+def _ref_worker(idx, n, steps, warmup, stab, barrier, q):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle
+    import topology as otopo
+    pts = oracle.OracleNoise(SEED + idx).cell_centres(n)
+    t = otopo.topology(pts)
+    m = oracle.OracleModel(t["pos"], t["rings"], t["counts"], t["vcells"], t["vnbrs"], math.sqrt(n / (4 * math.pi)))
+    m.set_preferred(PARAMS["a0"], PARAMS["p0"])
+    m.set_kr(PARAMS["kr"])
+    m.set_t1_threshold(PARAMS["t1"])
+    noise = oracle.OracleNoise(BD_SEED + idx)
+    m.set_preferred(PARAMS["a0"], 1.0)  # the reference driver's stabilisation (sphericalVertex.cpp:106-115)
+    for _ in range(stab):
+        m.brownian_step(noise, 0.0, PARAMS["dt"], PARAMS["mu"])
+    m.set_preferred(PARAMS["a0"], PARAMS["p0"])
+    for _ in range(warmup):
+        m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])
+    barrier.wait()
+    for _ in range(steps):
+        m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])
+        barrier.wait()
+    q.put(int(np.asarray(m.positions()).shape[0]))
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build_oracle()
+    cores = args.ref_cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(cores + 1)
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_ref_worker, args=(i, args.cells, args.steps, args.warmup, args.ref_stab, barrier, q))
+             for i in range(cores)]
+    for p in procs:
+        p.start()
+    barrier.wait()  # all replicas built and warmed up
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        barrier.wait()
+    dt = time.perf_counter() - t0
+    nvs = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    value = sum(nvs) * args.steps / dt
+    sample = (f"{cores} independent replicas (one per host core) of the N=100k workload, each bench step one "
+              f"Brownian timestep of every replica; CPU restatement of the reference path (-O3)")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cell centres, reference init recipe)",
+        "config": {"workload": WORKLOAD, "n_cells": args.cells, "n_vertices": nvs[0] if nvs else None,
+                   "parallelism": f"{cores} host processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--cells", type=int, default=N_CELLS)
+    ap.add_argument("--stab", type=int, default=100, help="untimed stabilisation steps (T=0, P0=1)")
+    ap.add_argument("--equil", type=int, default=200, help="untimed equilibration steps before warm-up")
+    ap.add_argument("--cpu-steps", type=int, default=25, help="steps of the one-core CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-cores", type=int, default=0)
+    ap.add_argument("--ref-stab", type=int, default=30, help="stabilisation steps of each reference replica")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIBPATH = os.path.join(PKG, "libsvm.so")
+# SVM_LIBRARY selects another build of the same library (e.g. one compiled with other flags).
+LIBPATH = os.environ.get("SVM_LIBRARY") or os.path.join(PKG, "libsvm.so")
 
 SVM_OK = 0
 SVM_ERR_ARG = 1
@@ -25,12 +26,22 @@ SVM_DEV_CELLLIST_OVERFLOW = 0x4
 SVM_DEV_BAD_TOPOLOGY = 0x8
 SVM_NOISE_PHILOX = 0
 SVM_NOISE_BUFFER = 1
+PHASES = ("corners", "cells", "fallback", "force", "t1_apply", "move")
 SVM_FIRE_RMS_OVER_N = 0
 SVM_FIRE_MAX_FORCE = 1
 
-dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
-ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
-up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+def _nullable(ptr):
+    """An ndpointer type that also accepts None (NULL) for optional outputs."""
+    class Nullable(ptr):
+        @classmethod
+        def from_param(cls, obj):
+            return None if obj is None else ptr.from_param(obj)
+    return Nullable
+
+
+dp = _nullable(np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS"))
+ip = _nullable(np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"))
+up = _nullable(np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS"))
 vp = C.c_void_p
 i32 = C.c_int
 f64 = C.c_double
@@ -72,9 +83,13 @@ SIGNATURES = {
     "svm_model_get_vertex_cells": (i32, [vp, ip]),
     "svm_model_get_vertex_neighbors": (i32, [vp, ip]),
     "svm_model_status": (i32, [vp, C.POINTER(i32)]),
+    "svm_model_area_check": (i32, [vp, C.POINTER(f64), C.POINTER(f64), C.POINTER(i32)]),
     "svm_model_take_flips": (i32, [vp, ip, i32, C.POINTER(i32)]),
     "svm_model_synchronize": (i32, [vp]),
+    "svm_model_profile": (i32, [vp, i32]),
+    "svm_model_profile_read": (i32, [vp, dp, ip]),
     "svm_model_device_positions": (i32, [vp, pvp]),
+    "svm_model_stream": (i32, [vp, pvp]),
     "svm_brownian_step": (i32, [vp, f64, f64, f64, i32, vp, u64]),
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
     "svm_brownian_run": (i32, [vp, f64, f64, f64, u64, i32]),

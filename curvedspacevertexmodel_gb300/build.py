@@ -21,7 +21,11 @@ LIB = os.path.join(PKG, "libsvm.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# -fmad=false: no contraction of a*b+c into FMA.  The FP64 path then rounds every product and
+# sum as the reference's CPU code does (x86-64 without FMA), which keeps the cancellation-prone
+# angle-sum areas and the total-area check (|sum A - 4 pi R^2| > 1e-6) on the reference's side of
+# the threshold; measured faster overall on GB300 than the contracted build.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -81,6 +85,13 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
                 print(msg)
     if jobs or not os.path.exists(LIB):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    # the C++ host layer's example driver (links libsvm.so)
+    host = os.path.join(PKG, "host")
+    exe = os.path.join(PKG, "sphericalVertex_gpu")
+    src = os.path.join(host, "sphericalVertex_gpu.cpp")
+    if _needs(exe, [src, os.path.join(host, "svm.hpp"), LIB]):
+        run([shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + host, src, "-o", exe,
+             "-L" + PKG, "-lsvm", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

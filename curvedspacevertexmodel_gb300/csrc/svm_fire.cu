@@ -189,8 +189,11 @@ ForceArgs fargs(svm_model* m) {
 int fire_iteration(svm_fire* F) {
     svm_model* m = F->m;
     const int nb = (m->nVertices + kB - 1) / kB;
-    k_fire_vv1<<<nb, kB, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
-    k_fire_consume<<<1, 1, 0, m->stream>>>(F->d);
+    {
+        PhaseTimer pt(m, SVM_PHASE_MOVE);
+        k_fire_vv1<<<nb, kB, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
+        k_fire_consume<<<1, 1, 0, m->stream>>>(F->d);
+    }
     m->cornersValid = false;
     int rc;
     if (!m->restricted) {
@@ -201,6 +204,7 @@ int fire_iteration(svm_fire* F) {
     }
     rc = launch_geometry(m);
     if (rc) return rc;
+    PhaseTimer pt(m, SVM_PHASE_FORCE);
     k_fire_force<<<nb, kB, 0, m->stream>>>(fargs(m), F->d, m->nVertices, m->force, m->vel, F->partials, F->ticket);
     return check_launch();
 }

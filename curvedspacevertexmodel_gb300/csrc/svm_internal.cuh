@@ -18,6 +18,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 #include "../../include/svm.h"
 
 namespace svm {
@@ -189,12 +190,27 @@ struct svm_model {
     double bdT = 0, bdDt = 0, bdMu = 0;
     uint64_t bdSeed = 0;
     int bdGraphCur = -1;
+    // per-phase event timing (svm_model_profile)
+    bool prof = false;
+    std::vector<cudaEvent_t> profEvents[SVM_PHASE_COUNT];   // start/stop pairs, in launch order
+    int profUsed[SVM_PHASE_COUNT] = {0};
+    double profMs[SVM_PHASE_COUNT] = {0};
+    int profLaunches[SVM_PHASE_COUNT] = {0};
     // bumped by every setter whose value a captured graph bakes in (Kr, threshold, restriction)
     unsigned paramsVersion = 0;
     unsigned bdGraphVersion = ~0u;
 };
 
 namespace svm {
+// Brackets one phase launch with profiling events when profiling is on and the stream is not
+// being captured.
+struct PhaseTimer {
+    svm_model* m;
+    int phase;
+    bool on;
+    PhaseTimer(svm_model* m_, int phase_);
+    ~PhaseTimer();
+};
 // launch helpers shared across translation units (svm_model.cu)
 int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);

@@ -29,6 +29,43 @@ constexpr int kHeapCap = 512;
 
 inline int blocksFor(long n, int b = kBlock) { return (int)((n + b - 1) / b); }
 
+static bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &st);
+    return st != cudaStreamCaptureStatusNone;
+}
+
+static void profile_drain(svm_model* m) {
+    cudaStreamSynchronize(m->stream);
+    for (int ph = 0; ph < SVM_PHASE_COUNT; ++ph) {
+        for (int k = 0; k + 1 < m->profUsed[ph]; k += 2) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, m->profEvents[ph][k], m->profEvents[ph][k + 1]) == cudaSuccess) {
+                m->profMs[ph] += ms;
+                m->profLaunches[ph] += 1;
+            }
+        }
+        m->profUsed[ph] = 0;
+    }
+}
+
+PhaseTimer::PhaseTimer(svm_model* m_, int phase_) : m(m_), phase(phase_), on(m_->prof && !capturing(m_->stream)) {
+    if (!on) return;
+    auto& ev = m->profEvents[phase];
+    if (m->profUsed[phase] + 2 > 512) profile_drain(m);
+    while ((int)ev.size() < m->profUsed[phase] + 2) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ev.push_back(e);
+    }
+    cudaEventRecord(ev[m->profUsed[phase]], m->stream);
+}
+PhaseTimer::~PhaseTimer() {
+    if (!on) return;
+    cudaEventRecord(m->profEvents[phase][m->profUsed[phase] + 1], m->stream);
+    m->profUsed[phase] += 2;
+}
+
 int check_launch() {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -619,6 +656,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
 }
 
 int launch_corners(svm_model* m, bool t1test) {
+    PhaseTimer pt(m, SVM_PHASE_CORNERS);
     k_corners<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
         m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
         m->R, t1test ? 1 : 0, m->t1Threshold, m->t1);
@@ -628,9 +666,13 @@ int launch_corners(svm_model* m, bool t1test) {
 
 static int launch_cells(svm_model* m) {
     const int nb = blocksFor(m->nCells);
-    k_cells<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R,
-                                           m->cellPos, m->cellSph, m->ap, m->partials, m->ticket, m->scalars,
-                                           m->fallbackFlag);
+    {
+        PhaseTimer pt(m, SVM_PHASE_CELLS);
+        k_cells<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R,
+                                               m->cellPos, m->cellSph, m->ap, m->partials, m->ticket, m->scalars,
+                                               m->fallbackFlag);
+    }
+    PhaseTimer pt(m, SVM_PHASE_FALLBACK);
     k_fallback<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc, m->nCells,
                                               m->R, m->fallbackFlag, m->ap);
     return check_launch();
@@ -644,6 +686,7 @@ int launch_geometry(svm_model* m) {
 }
 
 int launch_t1_apply(svm_model* m) {
+    PhaseTimer pt(m, SVM_PHASE_T1APPLY);
     k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, 1), m->t1);
     return check_launch();
 }
@@ -655,19 +698,21 @@ static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, 
     const double fp = dt * mu;
     const double np = sqrt(2.0 * fp * T);
     const int nxt = 1 - m->cur;
+    {
+    PhaseTimer pt(m, SVM_PHASE_FORCE);
     if (noiseMode == SVM_NOISE_BUFFER)
         k_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
             force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     else
         k_force_bd<SVM_NOISE_PHILOX><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
             force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+    }
     if ((rc = check_launch())) return rc;
     m->cur = nxt;
     // corners of the moved state, with the T1 edge test fused in
     rc = launch_corners(m, !m->restricted);
     if (rc) return rc;
-    k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, 1), m->t1);
-    return check_launch();
+    return launch_t1_apply(m);
 }
 
 }  // namespace svm
@@ -819,18 +864,35 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
+    for (auto& v : m->profEvents) for (cudaEvent_t e : v) cudaEventDestroy(e);
     if (m->ownStream && m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return SVM_OK;
 }
 
-static int upload_positions(svm_model* m, const double* in) {
-    std::vector<double4_32a> p(m->nVertices);
-    for (int i = 0; i < m->nVertices; ++i) p[i] = make_double4_32a(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
-    SVM_CUDA(cudaMemcpyAsync(m->pos[m->cur], p.data(), sizeof(double4_32a) * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+__global__ void k_aos_to_d4(const double* __restrict__ in, double4_32a* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_double4_32a(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
+}
+__global__ void k_d4_to_aos(const double4_32a* __restrict__ in, double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { const double4_32a q = in[i]; out[3 * i] = q.x; out[3 * i + 1] = q.y; out[3 * i + 2] = q.z; }
+}
+
+// Host AoS double[3n] -> device double4 through the staging buffer (a pinned caller buffer is
+// copied by DMA without a host-side repack).
+static int upload_vec(svm_model* m, const double* in, double4_32a* dst, int n) {
+    SVM_CUDA(cudaMemcpyAsync(m->dispBuf, in, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, m->stream));
+    k_aos_to_d4<<<svm::blocksFor(n), svm::kBlock, 0, m->stream>>>(m->dispBuf, dst, n);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
     SVM_CUDA(cudaStreamSynchronize(m->stream));
-    m->cornersValid = false;
     return SVM_OK;
+}
+
+static int upload_positions(svm_model* m, const double* in) {
+    int rc = upload_vec(m, in, m->pos[m->cur], m->nVertices);
+    m->cornersValid = false;
+    return rc;
 }
 
 int svm_model_set_topology(svm_model* m, const double* vp, const int* rings, int stride, const unsigned* counts,
@@ -909,6 +971,7 @@ int svm_model_compute_forces(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     int rc = svm_model_compute_geometry(m);
     if (rc) return rc;
+    svm::PhaseTimer pt(m, SVM_PHASE_FORCE);
     k_force<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(svm::force_args(m, m->cur), m->nVertices, m->force);
     return svm::check_launch();
 }
@@ -937,7 +1000,10 @@ int svm_model_enforce_topology(svm_model* m) {
 
 int svm_model_move_particles(svm_model* m, const double* disp, double scale) {
     if (!m || !disp) return SVM_ERR_ARG;
+    {
+    svm::PhaseTimer pt(m, SVM_PHASE_MOVE);
     k_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], disp, scale, m->nVertices, m->R);
+    }
     if (svm::check_launch()) return SVM_ERR_CUDA;
     m->cornersValid = false;
     if (!m->restricted) return svm_model_enforce_topology(m);
@@ -951,10 +1017,12 @@ int svm_model_move_particles_host(svm_model* m, const double* disp, double scale
 }
 
 static int get_vec4(svm_model* m, const double4_32a* src, int n, double* out) {
-    std::vector<double4_32a> h(n);
-    SVM_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, m->stream));
+    double* stage = n <= m->nVertices ? m->dispBuf : nullptr;
+    if (!stage) return SVM_ERR_ARG;
+    k_d4_to_aos<<<svm::blocksFor(n), svm::kBlock, 0, m->stream>>>(src, stage, n);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    SVM_CUDA(cudaMemcpyAsync(out, stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, m->stream));
     SVM_CUDA(cudaStreamSynchronize(m->stream));
-    for (int i = 0; i < n; ++i) { out[3 * i] = h[i].x; out[3 * i + 1] = h[i].y; out[3 * i + 2] = h[i].z; }
     return SVM_OK;
 }
 
@@ -966,11 +1034,7 @@ int svm_model_get_cell_positions(svm_model* m, double* out) { if (!m || !out) re
 
 int svm_model_set_velocities(svm_model* m, const double* in) {
     if (!m || !in) return SVM_ERR_ARG;
-    std::vector<double4_32a> p(m->nVertices);
-    for (int i = 0; i < m->nVertices; ++i) p[i] = make_double4_32a(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
-    SVM_CUDA(cudaMemcpyAsync(m->vel, p.data(), sizeof(double4_32a) * m->nVertices, cudaMemcpyHostToDevice, m->stream));
-    SVM_CUDA(cudaStreamSynchronize(m->stream));
-    return SVM_OK;
+    return upload_vec(m, in, m->vel, m->nVertices);
 }
 
 int svm_model_get_area_perimeter(svm_model* m, double* out) {
@@ -1012,6 +1076,19 @@ int svm_model_status(svm_model* m, int* st) {
     return SVM_OK;
 }
 
+int svm_model_area_check(svm_model* m, double* total, double* excess, int* taken) {
+    if (!m) return SVM_ERR_ARG;
+    double sc[2];
+    int f = 0;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    SVM_CUDA(cudaMemcpy(sc, m->scalars, sizeof(sc), cudaMemcpyDeviceToHost));
+    SVM_CUDA(cudaMemcpy(&f, m->fallbackFlag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (total) *total = sc[0];
+    if (excess) *excess = sc[1];
+    if (taken) *taken = f;
+    return SVM_OK;
+}
+
 int svm_model_take_flips(svm_model* m, int* pairs, int cap, int* count) {
     if (!m || !count) return SVM_ERR_ARG;
     int n = 0;
@@ -1024,9 +1101,35 @@ int svm_model_take_flips(svm_model* m, int* pairs, int cap, int* count) {
     return SVM_OK;
 }
 
+int svm_model_profile(svm_model* m, int enable) {
+    if (!m) return SVM_ERR_ARG;
+    if (m->prof) svm::profile_drain(m);
+    m->prof = enable != 0;
+    for (int ph = 0; ph < SVM_PHASE_COUNT; ++ph) { m->profMs[ph] = 0; m->profLaunches[ph] = 0; }
+    return SVM_OK;
+}
+
+int svm_model_profile_read(svm_model* m, double* ms, int* launches) {
+    if (!m) return SVM_ERR_ARG;
+    svm::profile_drain(m);
+    for (int ph = 0; ph < SVM_PHASE_COUNT; ++ph) {
+        if (ms) ms[ph] = m->profMs[ph];
+        if (launches) launches[ph] = m->profLaunches[ph];
+        m->profMs[ph] = 0;
+        m->profLaunches[ph] = 0;
+    }
+    return SVM_OK;
+}
+
 int svm_model_synchronize(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_stream(svm_model* m, void** s) {
+    if (!m || !s) return SVM_ERR_ARG;
+    *s = (void*)m->stream;
     return SVM_OK;
 }
 

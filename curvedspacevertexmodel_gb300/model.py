@@ -227,6 +227,12 @@ class sphericalVertexModel:
         call("svm_model_get_vertex_neighbors", self._h, out)
         return out.reshape(-1, 3)
 
+    def areaCheck(self):
+        """(total area, excess over 4 pi R^2, fallback taken) of the last geometry pass."""
+        t, e, f = C.c_double(), C.c_double(), C.c_int()
+        call("svm_model_area_check", self._h, C.byref(t), C.byref(e), C.byref(f))
+        return t.value, e.value, bool(f.value)
+
     def deviceStatus(self) -> int:
         st = C.c_int()
         call("svm_model_status", self._h, C.byref(st))
@@ -237,6 +243,12 @@ class sphericalVertexModel:
         n = C.c_int()
         call("svm_model_take_flips", self._h, out, capacity, C.byref(n))
         return out[: 2 * min(n.value, capacity)].reshape(-1, 2)
+
+    def streamHandle(self) -> int:
+        """The cudaStream_t the model's work runs on (e.g. for torch.cuda.ExternalStream)."""
+        s = C.c_void_p()
+        call("svm_model_stream", self._h, C.byref(s))
+        return s.value or 0
 
     def synchronize(self):
         call("svm_model_synchronize", self._h)

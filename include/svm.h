@@ -124,6 +124,9 @@ int svm_model_get_cell_positions(svm_model* m, double* out);
 int svm_model_get_rings(svm_model* m, int* rings, int ringStride, unsigned* ringCounts);
 int svm_model_get_vertex_cells(svm_model* m, int* out);
 int svm_model_get_vertex_neighbors(svm_model* m, int* out);
+/* The last geometry pass's total-area check (sphericalVertexModel.cpp:304-310): sum of cell
+ * areas, its excess over 4 pi R^2, and whether the triangle-fan fallback replaced the areas. */
+int svm_model_area_check(svm_model* m, double* totalArea, double* excess, int* fallbackTaken);
 /* Device status word (SVM_DEV_* bits); read and cleared. */
 int svm_model_status(svm_model* m, int* deviceStatus);
 /* T1 flips performed since the last call, as (vertex1, vertex2) pairs in the order they were
@@ -133,6 +136,23 @@ int svm_model_synchronize(svm_model* m);
 /* Device pointers of the model's arrays (double4 positions / forces, etc.) for callers that
  * keep data on the GPU.  Valid until svm_model_destroy. */
 int svm_model_device_positions(svm_model* m, void** ptr);
+/* The CUDA stream (cudaStream_t) all of the model's work is ordered on. */
+int svm_model_stream(svm_model* m, void** stream);
+
+/* Per-phase CUDA-event timing on the model's stream (the GPU counterpart of the reference's
+ * geoProf / forceProf / moveProf profilers, sphericalVertexModel.h:87-89 and
+ * src/utilities/profiler.h:8-45).  While enabled, every launch of a phase outside graph capture
+ * is bracketed by events; svm_model_profile_read synchronises and returns, per phase, the total
+ * milliseconds and the number of launches since the last read.  Phases: */
+#define SVM_PHASE_CORNERS 0    /* per-vertex corner arcs/angles (+ fused T1 edge test) */
+#define SVM_PHASE_CELLS 1      /* per-cell centroid, area, perimeter, total-area check */
+#define SVM_PHASE_FALLBACK 2   /* triangle-fan area fallback */
+#define SVM_PHASE_FORCE 3      /* forces (+ fused Brownian integrate and move, or FIRE half-kick) */
+#define SVM_PHASE_T1APPLY 4    /* ordered T1 flips */
+#define SVM_PHASE_MOVE 5       /* standalone moves and velocity-Verlet drift */
+#define SVM_PHASE_COUNT 6
+int svm_model_profile(svm_model* m, int enable);
+int svm_model_profile_read(svm_model* m, double* msPerPhase, int* launchesPerPhase);
 
 /* ---- Brownian dynamics ---------------------------------------------------------------------
  * brownianDynamics::integrateEOMGPU (src/updaters/brownianDynamics.cpp:14-27) ->

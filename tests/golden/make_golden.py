@@ -33,6 +33,9 @@ FIRE = dict(dt=0.01, alpha_start=0.1, dt_max=0.1, dt_inc=1.1, dt_dec=0.5, alpha_
 
 
 def snapshot(m, prefix, out):
+    # the reference keeps areaPerimeter from the start of the last step; recompute it for the
+    # current positions (no effect on the trajectory: every step recomputes geometry first)
+    m.compute_geometry()
     rings, counts = m.rings(W)
     out[prefix + "pos"] = m.positions()
     out[prefix + "rings"] = rings

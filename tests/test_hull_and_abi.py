@@ -119,3 +119,17 @@ def test_topology_matches_reference_hull_shim(svm, oracle_mod):
     assert np.array_equal(t["rings"], topo.rings[:, :W])
     assert np.array_equal(t["vcells"], topo.vertexCells)
     assert np.array_equal(t["vnbrs"], topo.vertexNeighbors)
+
+
+def test_oracle_topology_matches_product(svm, oracle_mod):
+    """The reference leg builds its initial state without product code; it must agree."""
+    pytest.importorskip("scipy.spatial")
+    import topology as otopo
+    pts = svm.random_cell_centres(1137, 300)
+    t = otopo.topology(pts)
+    topo = svm.Topology(pts)
+    assert np.array_equal(t["pos"], topo.vertexPositions)
+    assert np.array_equal(t["rings"], topo.rings)
+    assert np.array_equal(t["counts"], topo.ringCounts)
+    assert np.array_equal(t["vcells"], topo.vertexCells)
+    assert np.array_equal(t["vnbrs"], topo.vertexNeighbors)

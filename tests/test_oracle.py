@@ -56,6 +56,7 @@ def test_brownian_trajectory_matches_reference(oracle_mod, gold):
             assert np.array_equal(m.vertex_cells(), g[p + "vcells"]), step
             assert np.array_equal(m.vertex_neighbors(), g[p + "vnbrs"]), step
             assert close(m.positions(), g[p + "pos"]), step
+            m.compute_geometry()
             assert close(m.area_perimeter(), g[p + "ap"]), step
             assert close(np.array(m.energy()), g[p + "energy"]), step
     assert np.array_equal(np.array(flips, dtype=np.int32).reshape(-1, 3), g["flips"])
