@@ -27,6 +27,7 @@ SVM_DEV_BAD_TOPOLOGY = 0x8
 SVM_NOISE_PHILOX = 0
 SVM_NOISE_BUFFER = 1
 PHASES = ("corners", "cells", "fallback", "force", "t1_apply", "move")
+SVM_NOALLOC_MAX_CELLS = 2097152
 SVM_FIRE_RMS_OVER_N = 0
 SVM_FIRE_MAX_FORCE = 1
 
@@ -90,6 +91,7 @@ SIGNATURES = {
     "svm_model_profile_read": (i32, [vp, dp, ip]),
     "svm_model_device_positions": (i32, [vp, pvp]),
     "svm_model_stream": (i32, [vp, pvp]),
+    "svm_energy_noalloc": (i32, [vp, vp, f64, i32, vp, vp]),
     "svm_brownian_step": (i32, [vp, f64, f64, f64, i32, vp, u64]),
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
     "svm_brownian_run": (i32, [vp, f64, f64, f64, u64, i32]),

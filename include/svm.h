@@ -154,6 +154,23 @@ int svm_model_stream(svm_model* m, void** stream);
 int svm_model_profile(svm_model* m, int enable);
 int svm_model_profile_read(svm_model* m, double* msPerPhase, int* launchesPerPhase);
 
+/* ---- allocation-free energy -----------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory — hosts whose
+ * device memory belongs entirely to their own pool allocator, and per-step code that must not pay
+ * cudaMalloc's implicit device-wide synchronisation — this computes
+ * energy = sum_c Kr (A_c - A0_c)^2 + (P_c - P0_c)^2 (the quantity of svm_model_compute_energy)
+ * from caller-owned DEVICE arrays areaPerimeter[2*nCells] and preference[2*nCells] into the DEVICE
+ * double *energy, on `stream` (NULL: the legacy default stream), without allocating.  Its scratch is
+ * one static device array in libsvm of SVM_NOALLOC_MAX_CELLS / 256 + 32 doubles (64 KB) per device;
+ * nCells above SVM_NOALLOC_MAX_CELLS returns SVM_ERR_ARG.  Every call on a device shares that
+ * array (it keeps the last call's contents; the part that must start at zero is cleared on
+ * `stream` before each launch), so calls that overlap on the GPU race.  The first call on each
+ * device looks up the array's address (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture. */
+#define SVM_NOALLOC_MAX_CELLS 2097152
+int svm_energy_noalloc(const double* areaPerimeter, const double* preference, double kr, int nCells,
+                       double* energy, void* stream);
+
 /* ---- Brownian dynamics ---------------------------------------------------------------------
  * brownianDynamics::integrateEOMGPU (src/updaters/brownianDynamics.cpp:14-27) ->
  * gpu_brownian_eom_integration (brownianDynamics.cuh:15-22): forces, then
