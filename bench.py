@@ -196,6 +196,7 @@ def run_ours(args):
     for _ in range(max(3, args.warmup)):
         bd.integrateEquationOfMotion()
     torch.cuda.synchronize()
+    model.t1Stats()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")  # > L2 (129 MB)
 
     # ---- timed region: K steps, each after an L2 flush, events on the model's stream ----
@@ -221,6 +222,7 @@ def run_ours(args):
     ms = np.zeros(_lib_phase_count(), dtype=np.float64)
     launches = np.zeros(_lib_phase_count(), dtype=np.int32)
     _lib.call("svm_model_profile_read", model.handle, ms, launches)
+    t1stats = model.t1Stats()
     _lib.call("svm_model_profile", model.handle, 0)
     total_ms = float(sum(step_ms))
     if pg:
@@ -268,7 +270,7 @@ def run_ours(args):
     # ---- roofline of the dominant kernel ----
     names = _lib.PHASES
     dom = int(np.argmax(ms))
-    avg_launch_ms = ms[dom] / max(1, launches[dom])
+    avg_launch_ms = ms[dom] / max(1, launches[dom])  # the force phase is one kernel per bracket
     peak, peak_kind = peaks()
     if names[dom] == "force":
         alg = algorithmic_bytes_force(nv, nc)
@@ -304,6 +306,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
         "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
         "warm_l2_ms_per_step": warm_ms,
+        "t1_per_step": {k: v / args.steps for k, v in t1stats.items()},
         "wall_s": wall,
         "device_status": status,
         "energy_per_cell": energy_per_cell,

@@ -199,7 +199,7 @@ int fire_iteration(svm_fire* F) {
     if (!m->restricted) {
         rc = launch_corners(m, true);
         if (rc) return rc;
-        rc = launch_t1_apply(m);
+        rc = launch_t1_apply(m, 0);
         if (rc) return rc;
     }
     rc = launch_geometry(m);

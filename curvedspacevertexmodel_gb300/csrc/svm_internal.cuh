@@ -61,6 +61,23 @@ __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
     return R * acos(num / den);
 }
+// The T1 length test geodesic(p1, p2) < t, i.e. R acos(c) < t with c = p1.p2 / (|p1||p2|).  acos
+// is decreasing, so away from c = cos(t / R) the answer is c > cos(t / R); the formula itself is
+// evaluated only when c lies within [cosLo, cosHi], a bracket around cos(t / R) of half-width
+// 1e-9, which is many orders wider than the error of acos and of the rounding of c, or when c > 1.
+__host__ __device__ inline void t1_bracket(double t, double R, double* lo, double* hi) {
+    const double c = cos(t / R);
+    *lo = c - 1e-9;
+    *hi = c + 1e-9;
+}
+__device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, double cosLo, double cosHi) {
+    const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
+    const double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    const double c = num / den;
+    if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
+    if (c < cosLo) return false;
+    return R * acos(c) < t;
+}
 // includedAngle (sphericalDomain.h:114-133)
 __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
@@ -142,15 +159,43 @@ __device__ __forceinline__ D3 from_basis(double4_32a s, double2 g) {
 }
 
 // ---- host-side state -----------------------------------------------------------------------
+// Old values of everything one T1 flip overwrites, so a parallel pass can be rolled back.
+struct UndoEntry {
+    int v1, v2, b, c;              // vertices whose vertex->vertex slots change
+    int cells[4];                  // cells i, j, k, l whose rings change
+    double4_32a p1, p2;            // old positions of v1, v2
+    int4 vc1, vc2;                 // old vertex->cell slots of v1, v2
+    int4 vn[4];                    // old vertex->vertex slots of v1, v2, b, c
+    int counts[4];                 // old ring sizes
+};
+
 struct T1Scratch {
     unsigned* bits = nullptr;      // one bit per (vertex, slot) position, 3*Nv bits
     unsigned* summary = nullptr;   // one bit per word of `bits`
     int* count = nullptr;          // number of candidate positions found by the test
-    int* flipLog = nullptr;        // (v1, v2) pairs, capacity flipLogCap
+    int* flipLog = nullptr;        // (pass, position, v1, v2) per flip, capacity flipLogCap
     int* flipCount = nullptr;
+    int* pass = nullptr;           // T1 passes so far (orders the flip log across passes)
     int* touched = nullptr;        // cells whose rings changed during the apply kernel
     int nWords = 0, nSummary = 0, flipLogCap = 0, touchedCap = 0;
+    // parallel pass (deterministic reservations), capacity `cap` pending positions
+    int* listA = nullptr;          // pending positions of this round
+    int* listB = nullptr;          // pending positions of the next round
+    int* listOrig = nullptr;       // the candidates as flagged by the test (for a rollback)
+    int* fp = nullptr;             // footprint of each pending position, kFootprint ints
+    int* resV = nullptr;           // per vertex: lowest position reserving it this round
+    int* resC = nullptr;           // per cell: same
+    int* comV = nullptr;           // per vertex: highest position that has executed on it
+    int* comC = nullptr;           // per cell: same
+    int* comList = nullptr;        // footprints of executed positions (to clear comV/comC)
+    UndoEntry* undo = nullptr;     // one entry per committed flip
+    int* undoRings = nullptr;      // old rings of the four cells, 4*Wc ints per entry
+    int* ctr = nullptr;            // [0] pending, [1] next, [2] undo entries, [3] rollback, [4] executed
+    int* stats = nullptr;          // svm_model_t1_stats counters
+    int cap = 0, undoCap = 0;
 };
+constexpr int kFootprint = 14;     // 8 vertex slots + 6 cell slots (duplicates allowed)
+constexpr int kResFree = 0x7f7f7f7f;
 
 }  // namespace svm
 
@@ -195,7 +240,8 @@ struct svm_model {
     std::vector<cudaEvent_t> profEvents[SVM_PHASE_COUNT];   // start/stop pairs, in launch order
     int profUsed[SVM_PHASE_COUNT] = {0};
     double profMs[SVM_PHASE_COUNT] = {0};
-    int profLaunches[SVM_PHASE_COUNT] = {0};
+    int profLaunches[SVM_PHASE_COUNT] = {0};   // kernel launches (a bracket may hold several)
+    std::vector<int> profKernels[SVM_PHASE_COUNT];
     // bumped by every setter whose value a captured graph bakes in (Kr, threshold, restriction)
     unsigned paramsVersion = 0;
     unsigned bdGraphVersion = ~0u;
@@ -208,12 +254,12 @@ struct PhaseTimer {
     svm_model* m;
     int phase;
     bool on;
-    PhaseTimer(svm_model* m_, int phase_);
+    PhaseTimer(svm_model* m_, int phase_, int kernels = 1);
     ~PhaseTimer();
 };
 // launch helpers shared across translation units (svm_model.cu)
 int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
-int launch_t1_apply(svm_model* m);
+int launch_t1_apply(svm_model* m, int bump);
 int check_launch();
 }  // namespace svm

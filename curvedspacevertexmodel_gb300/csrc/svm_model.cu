@@ -42,17 +42,19 @@ static void profile_drain(svm_model* m) {
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, m->profEvents[ph][k], m->profEvents[ph][k + 1]) == cudaSuccess) {
                 m->profMs[ph] += ms;
-                m->profLaunches[ph] += 1;
+                m->profLaunches[ph] += m->profKernels[ph][k / 2];
             }
         }
         m->profUsed[ph] = 0;
+        m->profKernels[ph].clear();
     }
 }
 
-PhaseTimer::PhaseTimer(svm_model* m_, int phase_) : m(m_), phase(phase_), on(m_->prof && !capturing(m_->stream)) {
+PhaseTimer::PhaseTimer(svm_model* m_, int phase_, int kernels) : m(m_), phase(phase_), on(m_->prof && !capturing(m_->stream)) {
     if (!on) return;
     auto& ev = m->profEvents[phase];
     if (m->profUsed[phase] + 2 > 512) profile_drain(m);
+    m->profKernels[phase].push_back(kernels);
     while ((int)ev.size() < m->profUsed[phase] + 2) {
         cudaEvent_t e;
         cudaEventCreate(&e);
@@ -101,7 +103,7 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
                           const int4* __restrict__ vcell, const int4* __restrict__ vlast,
                           const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
                           const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV,
-                          double R, int t1test, double t1Threshold, T1Scratch t1) {
+                          double R, int t1test, double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const D3 p = ld3(pos, v);
@@ -119,7 +121,7 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int u = comp(nb, s);
-            if (v < u && geodesic(p, ld3(pos, u), R) < t1Threshold) {
+            if (v < u && shorter_than(p, ld3(pos, u), R, t1Threshold, cosLo, cosHi)) {
                 const int q = 3 * v + s;
                 atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
                 atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -290,7 +292,7 @@ __global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__
 
 // Standalone T1 edge test (gpu_vm_test_edges_for_T1, sphericalVertexModel.cu:225-273).
 __global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __restrict__ vnbr, int nV, double R,
-                          double t1Threshold, T1Scratch t1) {
+                          double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const D3 p = ld3(pos, v);
@@ -298,7 +300,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __res
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int u = comp(nb, s);
-        if (v < u && geodesic(p, ld3(pos, u), R) < t1Threshold) {
+        if (v < u && shorter_than(p, ld3(pos, u), R, t1Threshold, cosLo, cosHi)) {
             const int q = 3 * v + s;
             atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
             atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -309,6 +311,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __res
 
 // ---- T1 apply ------------------------------------------------------------------------------
 struct ApplyArgs {
+    double cosLo, cosHi;   // shorter_than bracket of cos(t1Threshold / R)
     double4_32a* pos;
     double4_32a* vsph;
     int4 *vcell, *vnbr, *vlast, *vnext, *vrpos;
@@ -380,7 +383,8 @@ __device__ __forceinline__ D3 renorm_exact(D3 p, double R) {
 
 // One flip as testAndPerformT1TransitionsCPU does it (sphericalVertexModel.cpp:483-599).
 // Returns false when the flip is forbidden or does not fit the ring capacity.
-__device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs) {
+__device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo = nullptr,
+                        int* undoRings = nullptr) {
     const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
     cs.w = -1;
     for (int ff = 0; ff < 3; ++ff) {
@@ -404,6 +408,19 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs) 
     // forbid a T1 that would shrink a triangular cell (sphericalVertexModel.cpp:485-487)
     if (A.ringCount[cs.x] == 3 || A.ringCount[cs.z] == 3) return false;
     if (A.ringCount[cs.y] + 1 > A.Wc || A.ringCount[cs.w] + 1 > A.Wc) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    if (undo) {
+        undo->v1 = v1; undo->v2 = v2; undo->b = vs.y; undo->c = vs.z;
+        undo->cells[0] = cs.x; undo->cells[1] = cs.y; undo->cells[2] = cs.z; undo->cells[3] = cs.w;
+        undo->p1 = A.pos[v1]; undo->p2 = A.pos[v2];
+        undo->vc1 = A.vcell[v1]; undo->vc2 = A.vcell[v2];
+        undo->vn[0] = A.vnbr[v1]; undo->vn[1] = A.vnbr[v2]; undo->vn[2] = A.vnbr[vs.y]; undo->vn[3] = A.vnbr[vs.z];
+        for (int q = 0; q < 4; ++q) {
+            const int cell = undo->cells[q];
+            const int n = A.ringCount[cell];
+            undo->counts[q] = n;
+            for (int k = 0; k < n; ++k) undoRings[q * A.Wc + k] = A.ring[(long)cell * A.Wc + k];
+        }
+    }
     D3 p1 = ld3(A.pos, v1), p2 = ld3(A.pos, v2);
     D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
     mid = renorm_exact(mid, 1.0);
@@ -433,10 +450,48 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs) 
     return true;
 }
 
+// Ring bookkeeping (vrpos/vlast/vnext) and corners of the cells whose rings a T1 pass changed,
+// and fresh spherical coordinates of their vertices.  Grid-stride over (touched cell, ring
+// position); every written value depends only on the final rings and positions, so duplicate
+// entries and concurrent writers of the same vertex agree.
+__global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
+    const int nt = *(volatile int*)(t1.ctr + 5);
+    const long total = (long)nt * A.Wc;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int cell = t1.touched[e / A.Wc], k = (int)(e % A.Wc);
+        const int n = A.ringCount[cell];
+        if (k >= n) continue;
+        const int* rg = A.ring + (long)cell * A.Wc;
+        const int u = rg[k];
+        const int last = rg[k == 0 ? n - 1 : k - 1], next = rg[k + 1 == n ? 0 : k + 1];
+        for (int s = 0; s < 3; ++s)
+            if (compRef(A.vcell, u, s) == cell) {
+                compRef(A.vrpos, u, s) = k;
+                compRef(A.vlast, u, s) = last;
+                compRef(A.vnext, u, s) = next;
+            }
+        const D3 pl = ld3(A.pos, last), p = ld3(A.pos, u), px = ld3(A.pos, next);
+        A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
+        A.vsph[u] = sph_coords(p);
+    }
+}
+
+// Restores everything a committed flip overwrote.
+__device__ void t1_undo(const ApplyArgs& A, const UndoEntry& u, const int* undoRings) {
+    A.pos[u.v1] = u.p1; A.pos[u.v2] = u.p2;
+    A.vcell[u.v1] = u.vc1; A.vcell[u.v2] = u.vc2;
+    A.vnbr[u.v1] = u.vn[0]; A.vnbr[u.v2] = u.vn[1]; A.vnbr[u.b] = u.vn[2]; A.vnbr[u.c] = u.vn[3];
+    for (int q = 0; q < 4; ++q) {
+        const int cell = u.cells[q];
+        A.ringCount[cell] = u.counts[q];
+        for (int k = 0; k < u.counts[q]; ++k) A.ring[(long)cell * A.Wc + k] = undoRings[q * A.Wc + k];
+    }
+}
+
 __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
     const int v = q / 3, s = q - 3 * (q / 3);
     const int u = compRef(A.vnbr, v, s);
-    return v < u && geodesic(ld3(A.pos, v), ld3(A.pos, u), A.R) < A.t1Threshold;
+    return v < u && shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi);
 }
 
 // Applies the flagged T1 flips in the order of the CPU loop (ascending vertex1, then slot),
@@ -452,10 +507,14 @@ __global__ void __launch_bounds__(kApplyThreads) k_t1_apply(ApplyArgs A, T1Scrat
     const int tid = threadIdx.x;
     const int total = *t1.count;
     if (total == 0) {
-        if (tid == 0 && A.bumpStep) *A.stepCounter += 1ull;
+        if (tid == 0) {
+            *t1.pass += 1;
+            t1.stats[0] += 1;
+            if (A.bumpStep) *A.stepCounter += 1ull;
+        }
         return;
     }
-    if (tid == 0) { nbuf = 0; head = 0; nheap = 0; extractWord = 0; nTouched = 0; }
+    if (tid == 0) { nbuf = 0; head = 0; nheap = 0; extractWord = 0; nTouched = 0; t1.stats[6] = *t1.flipCount; }
     __syncthreads();
     int lastProcessed = -1;
     while (true) {
@@ -524,7 +583,10 @@ __global__ void __launch_bounds__(kApplyThreads) k_t1_apply(ApplyArgs A, T1Scrat
                     int4 cs, vs;
                     if (t1_flip(A, v1, v2, cs, vs)) {
                         const int fc = atomicAdd(t1.flipCount, 1);
-                        if (fc < t1.flipLogCap) { t1.flipLog[2 * fc] = v1; t1.flipLog[2 * fc + 1] = v2; }
+                        if (fc < t1.flipLogCap) {
+                            int* e = t1.flipLog + 4 * fc;
+                            e[0] = *t1.pass; e[1] = q; e[2] = v1; e[3] = v2;
+                        }
                         if (nTouched + 4 <= t1.touchedCap) {
                             t1.touched[nTouched++] = cs.x; t1.touched[nTouched++] = cs.y;
                             t1.touched[nTouched++] = cs.z; t1.touched[nTouched++] = cs.w;
@@ -554,42 +616,226 @@ __global__ void __launch_bounds__(kApplyThreads) k_t1_apply(ApplyArgs A, T1Scrat
         }
         __syncthreads();
     }
-    // Rebuild ring bookkeeping and corners of every touched cell.
-    __syncthreads();
-    const int nt = nTouched;
-    for (int e = tid; e < nt * A.Wc; e += blockDim.x) {
-        const int cell = t1.touched[e / A.Wc], k = e % A.Wc;
-        const int n = A.ringCount[cell];
-        if (k >= n) continue;
-        const int* rg = A.ring + (long)cell * A.Wc;
-        const int u = rg[k];
-        const int last = rg[k == 0 ? n - 1 : k - 1], next = rg[k + 1 == n ? 0 : k + 1];
-        for (int s = 0; s < 3; ++s)
-            if (compRef(A.vcell, u, s) == cell) {
-                compRef(A.vrpos, u, s) = k;
-                compRef(A.vlast, u, s) = last;
-                compRef(A.vnext, u, s) = next;
-            }
-    }
-    // moved vertices: spherical coordinates
-    const int nflip = nt / 4;
-    (void)nflip;
-    __syncthreads();
-    for (int e = tid; e < nt * A.Wc; e += blockDim.x) {
-        const int cell = t1.touched[e / A.Wc], k = e % A.Wc;
-        const int n = A.ringCount[cell];
-        if (k >= n) continue;
-        const int* rg = A.ring + (long)cell * A.Wc;
-        const D3 pl = ld3(A.pos, rg[k == 0 ? n - 1 : k - 1]), p = ld3(A.pos, rg[k]), px = ld3(A.pos, rg[k + 1 == n ? 0 : k + 1]);
-        A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
-        // every vertex of a touched cell gets fresh spherical coordinates (identical values when
-        // it did not move, so concurrent writers agree)
-        A.vsph[rg[k]] = sph_coords(p);
-    }
+    // ring bookkeeping and corners of the touched cells: k_t1_patch
     __syncthreads();
     if (tid == 0) {
+        t1.ctr[5] = nTouched;
         *t1.count = 0;
+        *t1.pass += 1;
+        t1.stats[0] += 1;
+        t1.stats[3] += *t1.flipCount - t1.stats[6];
         if (A.bumpStep) *A.stepCounter += 1ull;
+    }
+}
+
+
+// ---- parallel T1 pass -------------------------------------------------------------------------
+// Footprint of the edge at position p: every vertex and cell that testing, flipping and
+// re-testing after the flip can read or write (v1, v2 and their neighbours; the cells of v1 and
+// v2).  Two positions with disjoint footprints commute.
+__device__ __forceinline__ void t1_footprint(const ApplyArgs& A, int p, int* f) {
+    const int v1 = p / 3, v2 = compRef(A.vnbr, v1, p - 3 * v1);
+    const int4 n1 = A.vnbr[v1], n2 = A.vnbr[v2], c1 = A.vcell[v1], c2 = A.vcell[v2];
+    f[0] = v1; f[1] = v2; f[2] = n1.x; f[3] = n1.y; f[4] = n1.z; f[5] = n2.x; f[6] = n2.y; f[7] = n2.z;
+    f[8] = c1.x; f[9] = c1.y; f[10] = c1.z; f[11] = c2.x; f[12] = c2.y; f[13] = c2.z;
+}
+
+constexpr int kParThreads = 1024;
+
+// Block-wide exclusive scan of one int per thread; returns the block total in *total.
+__device__ int block_excl_scan(int v, int* total) {
+    __shared__ int warpTot[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warpTot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        int t = lane < nw ? warpTot[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) warpTot[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = (warp == 0 ? 0 : warpTot[warp - 1]) + incl - v;
+    *total = warpTot[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before;
+}
+
+// Applies the flagged flips with the result of the CPU's sequential order, in parallel rounds of
+// deterministic reservations: every pending position writes its own value into the footprint
+// cells (atomicMin); a position whose whole footprint holds its value runs (test, flip,
+// re-test of the affected edges), the others wait for the next round.  Overlapping positions
+// therefore run in ascending order and disjoint ones commute.  A position created by a re-test
+// that overlaps a higher position which has already run would need the CPU order broken; that is
+// detected through the per-vertex/per-cell record of the highest position that ran, and then
+// every flip of the pass is undone and the bitmap restored for k_t1_apply, which then applies
+// the flips one by one.  On success *t1.count is cleared so k_t1_apply returns at once.
+__global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scratch t1) {
+    __shared__ int nCur, nTouched, flip0, flag;
+    const int tid = threadIdx.x;
+    if (tid == 0) t1.ctr[5] = 0;  // touched cells of this pass (read by k_t1_patch)
+    if (*t1.count == 0) return;
+    int* cur = t1.listA;
+    int* nxt = t1.listB;
+    if (tid == 0) {
+        nCur = 0; nTouched = 0; flip0 = *t1.flipCount; flag = 0;
+        t1.ctr[1] = 0; t1.ctr[2] = 0; t1.ctr[3] = 0; t1.ctr[4] = 0;
+    }
+    __syncthreads();
+    // 1. the flagged positions, ascending (bits stay set: a set bit means "pending")
+    for (int base = 0; base < t1.nWords; base += blockDim.x) {
+        const int w = base + tid;
+        const unsigned word = w < t1.nWords ? t1.bits[w] : 0u;
+        int tot;
+        const int off = block_excl_scan(__popc(word), &tot);
+        if (nCur + tot > t1.cap) { if (tid == 0) flag = 1; __syncthreads(); break; }
+        unsigned x = word;
+        int at = nCur + off;
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1u;
+            cur[at] = w * 32 + b;
+            t1.listOrig[at] = w * 32 + b;
+            ++at;
+        }
+        __syncthreads();
+        if (tid == 0) nCur += tot;
+        __syncthreads();
+    }
+    if (flag) return;  // more candidates than the pass holds: k_t1_apply takes them all
+    const int nOrig = nCur;
+    int rounds = 0;
+    // 2. rounds
+    while (nCur > 0) {
+        ++rounds;
+        // reserve
+        for (int i = tid; i < nCur; i += blockDim.x) {
+            const int p = cur[i];
+            int* f = t1.fp + (long)i * kFootprint;
+            t1_footprint(A, p, f);
+            bool late = false;
+            for (int k = 0; k < 8; ++k) { late |= t1.comV[f[k]] > p; atomicMin(t1.resV + f[k], p); }
+            for (int k = 8; k < kFootprint; ++k) { late |= t1.comC[f[k]] > p; atomicMin(t1.resC + f[k], p); }
+            if (late) atomicExch(t1.ctr + 3, 1);
+        }
+        __syncthreads();
+        if (*(volatile int*)(t1.ctr + 3)) break;
+        // run the positions that hold their whole footprint
+        for (int i = tid; i < nCur; i += blockDim.x) {
+            const int p = cur[i];
+            const int* f = t1.fp + (long)i * kFootprint;
+            bool ready = true;
+            for (int k = 0; k < 8; ++k) ready &= t1.resV[f[k]] == p;
+            for (int k = 8; k < kFootprint; ++k) ready &= t1.resC[f[k]] == p;
+            if (!ready) {
+                const int ni = atomicAdd(t1.ctr + 1, 1);
+                if (ni < t1.cap) nxt[ni] = p;
+                else atomicExch(t1.ctr + 3, 1);
+                continue;
+            }
+            const int ci = atomicAdd(t1.ctr + 4, 1);
+            if (ci >= t1.cap) { atomicExch(t1.ctr + 3, 1); continue; }
+            for (int k = 0; k < kFootprint; ++k) t1.comList[(long)ci * kFootprint + k] = f[k];
+            for (int k = 0; k < 8; ++k) atomicMax(t1.comV + f[k], p);
+            for (int k = 8; k < kFootprint; ++k) atomicMax(t1.comC + f[k], p);
+            atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
+            if (!t1_candidate(A, p)) continue;
+            const int ui = atomicAdd(t1.ctr + 2, 1);
+            if (ui >= t1.undoCap) { atomicExch(t1.ctr + 3, 1); continue; }
+            const int v1 = p / 3, v2 = compRef(A.vnbr, v1, p - 3 * v1);
+            int4 cs, vs;
+            if (!t1_flip(A, v1, v2, cs, vs, t1.undo + ui, t1.undoRings + (long)ui * 4 * A.Wc)) {
+                t1.undo[ui].v1 = -1;  // nothing was written
+                continue;
+            }
+            const int fc = atomicAdd(t1.flipCount, 1);
+            if (fc < t1.flipLogCap) {
+                int* e = t1.flipLog + 4 * fc;
+                e[0] = *t1.pass; e[1] = p; e[2] = v1; e[3] = v2;
+            }
+            const int tc = atomicAdd(&nTouched, 4);
+            if (tc + 4 <= t1.touchedCap) {
+                t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
+            } else {
+                atomicExch(t1.ctr + 3, 1);
+            }
+            const int aff[6] = {v1, v2, vs.x, vs.y, vs.z, vs.w};
+            for (int a = 0; a < 6; ++a)
+                for (int sl = 0; sl < 3; ++sl) {
+                    const int r = 3 * aff[a] + sl;
+                    if (r <= p || !t1_candidate(A, r)) continue;
+                    const unsigned bit = 1u << (r & 31);
+                    if (!(atomicOr(t1.bits + (r >> 5), bit) & bit)) {
+                        atomicOr(t1.summary + (r >> 10), 1u << ((r >> 5) & 31));
+                        const int ni = atomicAdd(t1.ctr + 1, 1);
+                        if (ni < t1.cap) nxt[ni] = r;
+                        else atomicExch(t1.ctr + 3, 1);
+                    }
+                }
+        }
+        __syncthreads();
+        // release this round's reservations
+        for (int i = tid; i < nCur; i += blockDim.x) {
+            const int* f = t1.fp + (long)i * kFootprint;
+            for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
+            for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
+        }
+        __syncthreads();
+        if (tid == 0) { nCur = min(*(volatile int*)(t1.ctr + 1), t1.cap); t1.ctr[1] = 0; }
+        int* t = cur; cur = nxt; nxt = t;
+        __syncthreads();
+        if (*(volatile int*)(t1.ctr + 3)) break;
+    }
+    __syncthreads();
+    const bool rollback = *(volatile int*)(t1.ctr + 3) != 0;
+    if (rollback) {
+        // release reservations still held (a break after the reserve phase)
+        for (int i = tid; i < nCur; i += blockDim.x) {
+            const int* f = t1.fp + (long)i * kFootprint;
+            for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
+            for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
+        }
+        if (tid == 0) {
+            const int nu = min(*(volatile int*)(t1.ctr + 2), t1.undoCap);
+            for (int u = nu - 1; u >= 0; --u)
+                if (t1.undo[u].v1 >= 0) t1_undo(A, t1.undo[u], t1.undoRings + (long)u * 4 * A.Wc);
+            *t1.flipCount = flip0;
+        }
+        __syncthreads();
+        for (int w = tid; w < t1.nWords; w += blockDim.x) t1.bits[w] = 0u;
+        for (int w = tid; w < t1.nSummary; w += blockDim.x) t1.summary[w] = 0u;
+        __syncthreads();
+        for (int i = tid; i < nOrig; i += blockDim.x) {
+            const int q = t1.listOrig[i];
+            atomicOr(t1.bits + (q >> 5), 1u << (q & 31));
+            atomicOr(t1.summary + (q >> 10), 1u << ((q >> 5) & 31));
+        }
+    } else {
+        if (tid == 0) t1.ctr[5] = min(nTouched, t1.touchedCap);  // for k_t1_patch
+        // the bitmap is empty again; clear the summary words
+        for (int w = tid; w < t1.nSummary; w += blockDim.x) t1.summary[w] = 0u;
+    }
+    __syncthreads();
+    const int ne = min(*(volatile int*)(t1.ctr + 4), t1.cap);
+    for (int i = tid; i < ne; i += blockDim.x) {
+        const int* f = t1.comList + (long)i * kFootprint;
+        for (int k = 0; k < 8; ++k) t1.comV[f[k]] = -1;
+        for (int k = 8; k < kFootprint; ++k) t1.comC[f[k]] = -1;
+    }
+    if (tid == 0) {
+        t1.stats[1] += nOrig;
+        t1.stats[2] += ne;
+        t1.stats[4] += rounds;
+        if (rollback) t1.stats[5] += 1;
+        else { t1.stats[3] += *t1.flipCount - flip0; *t1.count = 0; }
     }
 }
 
@@ -652,14 +898,17 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
     A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
+    t1_bracket(m->t1Threshold, m->R, &A.cosLo, &A.cosHi);
     return A;
 }
 
 int launch_corners(svm_model* m, bool t1test) {
     PhaseTimer pt(m, SVM_PHASE_CORNERS);
+    double lo, hi;
+    t1_bracket(m->t1Threshold, m->R, &lo, &hi);
     k_corners<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
         m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
-        m->R, t1test ? 1 : 0, m->t1Threshold, m->t1);
+        m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
     m->cornersValid = true;
     return check_launch();
 }
@@ -667,7 +916,7 @@ int launch_corners(svm_model* m, bool t1test) {
 static int launch_cells(svm_model* m) {
     const int nb = blocksFor(m->nCells);
     {
-        PhaseTimer pt(m, SVM_PHASE_CELLS);
+        PhaseTimer pt(m, SVM_PHASE_CELLS, 1);
         k_cells<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R,
                                                m->cellPos, m->cellSph, m->ap, m->partials, m->ticket, m->scalars,
                                                m->fallbackFlag);
@@ -685,9 +934,11 @@ int launch_geometry(svm_model* m) {
     return launch_cells(m);
 }
 
-int launch_t1_apply(svm_model* m) {
-    PhaseTimer pt(m, SVM_PHASE_T1APPLY);
-    k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, 1), m->t1);
+int launch_t1_apply(svm_model* m, int bump) {
+    PhaseTimer pt(m, SVM_PHASE_T1APPLY, 3);
+    k_t1_parallel<<<1, kParThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
+    k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
+    k_t1_patch<<<2 * 152, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
     return check_launch();
 }
 
@@ -712,7 +963,7 @@ static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, 
     // corners of the moved state, with the T1 edge test fused in
     rc = launch_corners(m, !m->restricted);
     if (rc) return rc;
-    return launch_t1_apply(m);
+    return launch_t1_apply(m, 1);
 }
 
 }  // namespace svm
@@ -840,14 +1091,34 @@ int svm_model_create(int nCells, int nVertices, int Wc, double radius, void* str
     m->t1.nWords = (int)((3 * nV + 31) / 32);
     m->t1.nSummary = (m->t1.nWords + 31) / 32;
     m->t1.flipLogCap = 1 << 16;
-    m->t1.touchedCap = 4 * 8192;
+    m->t1.touchedCap = 4 * 65536;
+    m->t1.cap = (int)(3 * nV / 2 + 1024);
+    m->t1.undoCap = 65536;
     alloc((void**)&m->t1.bits, (size_t)m->t1.nSummary * 32 * sizeof(unsigned));
     alloc((void**)&m->t1.summary, (size_t)m->t1.nSummary * sizeof(unsigned));
     alloc((void**)&m->t1.count, sizeof(int));
-    alloc((void**)&m->t1.flipLog, 2 * (size_t)m->t1.flipLogCap * sizeof(int));
+    alloc((void**)&m->t1.flipLog, 4 * (size_t)m->t1.flipLogCap * sizeof(int));
+    alloc((void**)&m->t1.pass, sizeof(int));
+    alloc((void**)&m->t1.listA, (size_t)m->t1.cap * sizeof(int));
+    alloc((void**)&m->t1.listB, (size_t)m->t1.cap * sizeof(int));
+    alloc((void**)&m->t1.listOrig, (size_t)m->t1.cap * sizeof(int));
+    alloc((void**)&m->t1.fp, (size_t)m->t1.cap * svm::kFootprint * sizeof(int));
+    alloc((void**)&m->t1.comList, (size_t)m->t1.cap * svm::kFootprint * sizeof(int));
+    alloc((void**)&m->t1.resV, nV * sizeof(int));
+    alloc((void**)&m->t1.resC, nC * sizeof(int));
+    alloc((void**)&m->t1.comV, nV * sizeof(int));
+    alloc((void**)&m->t1.comC, nC * sizeof(int));
+    alloc((void**)&m->t1.undo, (size_t)m->t1.undoCap * sizeof(svm::UndoEntry));
+    alloc((void**)&m->t1.undoRings, (size_t)m->t1.undoCap * 4 * Wc * sizeof(int));
+    alloc((void**)&m->t1.ctr, 8 * sizeof(int));
+    alloc((void**)&m->t1.stats, 8 * sizeof(int));
     alloc((void**)&m->t1.flipCount, sizeof(int));
     alloc((void**)&m->t1.touched, (size_t)m->t1.touchedCap * sizeof(int));
     if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
+    cudaMemset(m->t1.resV, 0x7f, nV * sizeof(int));   // kResFree
+    cudaMemset(m->t1.resC, 0x7f, nC * sizeof(int));
+    cudaMemset(m->t1.comV, 0xff, nV * sizeof(int));   // -1
+    cudaMemset(m->t1.comC, 0xff, nC * sizeof(int));
     std::vector<double2> pref(nC, make_double2(1.0, 3.8));
     cudaMemcpy(m->pref, pref.data(), nC * sizeof(double2), cudaMemcpyHostToDevice);
     if (cudaDeviceSynchronize() != cudaSuccess) { svm_model_destroy(m); return SVM_ERR_CUDA; }
@@ -861,7 +1132,9 @@ int svm_model_destroy(svm_model* m) {
     void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
-                    m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched};
+                    m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
+                    m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
+                    m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
     for (auto& v : m->profEvents) for (cudaEvent_t e : v) cudaEventDestroy(e);
@@ -989,13 +1262,15 @@ int svm_model_compute_energy(svm_model* m, double* e) {
 
 int svm_model_enforce_topology(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
+    double lo, hi;
+    svm::t1_bracket(m->t1Threshold, m->R, &lo, &hi);
     k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnbr, m->nVertices, m->R,
-                                                                             m->t1Threshold, m->t1);
+                                                                             m->t1Threshold, lo, hi, m->t1);
     if (svm::check_launch()) return SVM_ERR_CUDA;
-    // corners must exist for the patching in k_t1_apply to be meaningful; recompute afterwards
-    k_t1_apply<<<1, svm::kApplyThreads, 0, m->stream>>>(svm::apply_args(m, 0), m->t1);
+    // the patch of touched cells writes corners; all of them are recomputed before their next use
+    int rc = svm::launch_t1_apply(m, 0);
     m->cornersValid = false;
-    return svm::check_launch();
+    return rc;
 }
 
 int svm_model_move_particles(svm_model* m, const double* disp, double scale) {
@@ -1095,8 +1370,16 @@ int svm_model_take_flips(svm_model* m, int* pairs, int cap, int* count) {
     SVM_CUDA(cudaStreamSynchronize(m->stream));
     SVM_CUDA(cudaMemcpy(&n, m->t1.flipCount, sizeof(int), cudaMemcpyDeviceToHost));
     *count = n;
-    const int k = std::min(std::min(n, cap), m->t1.flipLogCap);
-    if (pairs && k > 0) SVM_CUDA(cudaMemcpy(pairs, m->t1.flipLog, sizeof(int) * 2 * k, cudaMemcpyDeviceToHost));
+    const int k = std::min(n, m->t1.flipLogCap);
+    if (pairs && k > 0) {
+        std::vector<int4> e(k);
+        SVM_CUDA(cudaMemcpy(e.data(), m->t1.flipLog, sizeof(int4) * k, cudaMemcpyDeviceToHost));
+        // the CPU order: pass by pass, ascending edge position within a pass
+        std::stable_sort(e.begin(), e.end(), [](const int4& a, const int4& b) {
+            return a.x != b.x ? a.x < b.x : a.y < b.y;
+        });
+        for (int i = 0; i < std::min(k, cap); ++i) { pairs[2 * i] = e[i].z; pairs[2 * i + 1] = e[i].w; }
+    }
     SVM_CUDA(cudaMemset(m->t1.flipCount, 0, sizeof(int)));
     return SVM_OK;
 }
@@ -1118,6 +1401,16 @@ int svm_model_profile_read(svm_model* m, double* ms, int* launches) {
         m->profMs[ph] = 0;
         m->profLaunches[ph] = 0;
     }
+    return SVM_OK;
+}
+
+int svm_model_t1_stats(svm_model* m, int* st) {
+    if (!m || !st) return SVM_ERR_ARG;
+    int h[8];
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    SVM_CUDA(cudaMemcpy(h, m->t1.stats, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 6; ++i) st[i] = h[i];
+    SVM_CUDA(cudaMemset(m->t1.stats, 0, 6 * sizeof(int)));
     return SVM_OK;
 }
 

@@ -250,6 +250,14 @@ class sphericalVertexModel:
         call("svm_model_stream", self._h, C.byref(s))
         return s.value or 0
 
+    def t1Stats(self) -> dict:
+        """T1 counters since the last call: passes, flagged edges, edges run in parallel rounds,
+        flips, rounds, passes replayed sequentially after a rollback."""
+        out = np.zeros(6, dtype=np.int32)
+        call("svm_model_t1_stats", self._h, out)
+        return dict(passes=int(out[0]), flagged=int(out[1]), executed=int(out[2]), flips=int(out[3]),
+                    rounds=int(out[4]), rollbacks=int(out[5]))
+
     def synchronize(self):
         call("svm_model_synchronize", self._h)
 

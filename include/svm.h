@@ -132,6 +132,10 @@ int svm_model_status(svm_model* m, int* deviceStatus);
 /* T1 flips performed since the last call, as (vertex1, vertex2) pairs in the order they were
  * applied; *count receives the total (pairs beyond `capacity` are dropped). */
 int svm_model_take_flips(svm_model* m, int* pairs, int capacity, int* count);
+/* T1 statistics accumulated since the last call (then cleared), 6 ints: passes, edges flagged by
+ * the test, edges that ran in the parallel rounds, flips, parallel rounds, passes replayed one flip
+ * at a time after a rollback.  (The reference's T1 loop keeps no such counters.) */
+int svm_model_t1_stats(svm_model* m, int* stats6);
 int svm_model_synchronize(svm_model* m);
 /* Device pointers of the model's arrays (double4 positions / forces, etc.) for callers that
  * keep data on the GPU.  Valid until svm_model_destroy. */
@@ -143,12 +147,12 @@ int svm_model_stream(svm_model* m, void** stream);
  * geoProf / forceProf / moveProf profilers, sphericalVertexModel.h:87-89 and
  * src/utilities/profiler.h:8-45).  While enabled, every launch of a phase outside graph capture
  * is bracketed by events; svm_model_profile_read synchronises and returns, per phase, the total
- * milliseconds and the number of launches since the last read.  Phases: */
+ * milliseconds and the number of kernel launches since the last read.  Phases: */
 #define SVM_PHASE_CORNERS 0    /* per-vertex corner arcs/angles (+ fused T1 edge test) */
 #define SVM_PHASE_CELLS 1      /* per-cell centroid, area, perimeter, total-area check */
 #define SVM_PHASE_FALLBACK 2   /* triangle-fan area fallback */
 #define SVM_PHASE_FORCE 3      /* forces (+ fused Brownian integrate and move, or FIRE half-kick) */
-#define SVM_PHASE_T1APPLY 4    /* ordered T1 flips */
+#define SVM_PHASE_T1APPLY 4    /* ordered T1 flips (parallel pass, sequential replay, patch: 3 kernels) */
 #define SVM_PHASE_MOVE 5       /* standalone moves and velocity-Verlet drift */
 #define SVM_PHASE_COUNT 6
 int svm_model_profile(svm_model* m, int enable);

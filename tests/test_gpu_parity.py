@@ -35,6 +35,26 @@ def gold():
     return load_gold()
 
 
+def stabilised(svm, n, seed=5, stab=100, steps=200):
+    """The reference driver's preparation (sphericalVertex.cpp:104-125): T = 0 with P0 = 1, then
+    Brownian steps at T = 0.01, P0 = 3.8 (a raw random-Voronoi start diverges at large N in the
+    reference itself)."""
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(seed)
+    m = svm.sphericalVertexModel(n, noise)
+    m.setT1Threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.noise.setReproducibleSeed(seed + 1)
+    bd.setT(0.0)
+    m.setPreferredParameters(1.0, 1.0)
+    bd.run(stab)
+    bd.setT(0.01)
+    m.setPreferredParameters(1.0, 3.8)
+    bd.run(steps)
+    return m, bd
+
+
 def test_geometry_forces_energy_match_golden(svm, gold):
     m = gpu_model(svm, gold)
     m.computeForces()
@@ -245,26 +265,6 @@ def test_philox_noise_statistics(svm):
     assert abs(var / (2 * dt * T) - 1.0) < 0.03
 
 
-def stabilised(svm, n, seed=5, stab=100, steps=200):
-    """The reference driver's preparation (sphericalVertex.cpp:104-125): T = 0 with P0 = 1, then
-    Brownian steps at T = 0.01, P0 = 3.8 (a raw random-Voronoi start diverges at large N in the
-    reference itself)."""
-    noise = svm.noiseSource()
-    noise.setReproducibleSeed(seed)
-    m = svm.sphericalVertexModel(n, noise)
-    m.setT1Threshold(0.04)
-    bd = svm.brownianDynamics()
-    bd.setModel(m)
-    bd.noise.setReproducibleSeed(seed + 1)
-    bd.setT(0.0)
-    m.setPreferredParameters(1.0, 1.0)
-    bd.run(stab)
-    bd.setT(0.01)
-    m.setPreferredParameters(1.0, 3.8)
-    bd.run(steps)
-    return m, bd
-
-
 def test_large_sphere_invariants(svm):
     """Size-independent properties at N = 20k after the stabilised preparation and 200 noisy steps
     with T1: total area 4 pi R^2, tangential forces, trivalent connectivity, rings consistent with
@@ -308,3 +308,69 @@ def test_area_fallback_matches_oracle(svm, oracle_mod):
     assert abs(excess - om.excess_area()) < 1e-9 * abs(om.excess_area())
     assert rel_err(gm.areaPerimeter(), om.area_perimeter()) < 1e-12
     assert rel_err(gm.returnForces(), om.forces()) < RTOL_FORCE
+
+
+def test_mass_t1_matches_oracle(svm, oracle_mod):
+    """Hundreds of shortened edges, many sharing vertices and cells, in one enforceTopology pass:
+    the parallel pass must give the flips, connectivity and positions of the CPU's sequential loop."""
+    n = 2000
+    pts = svm.random_cell_centres(17, n)
+    topo = svm.Topology(pts)
+    R = np.sqrt(n / (4 * np.pi))
+    rng = np.random.default_rng(3)
+    pos = topo.vertexPositions.copy()
+    for v in rng.choice(topo.nVertices, 600, replace=False):
+        u = int(topo.vertexNeighbors[v][rng.integers(3)])
+        pos[u] = pos[v] + rng.uniform(0.01, 0.05) * (pos[u] - pos[v])
+        pos[u] *= R / np.linalg.norm(pos[u])
+    gm = svm.sphericalVertexModel(n, topology=topo, radius=R)
+    gm.setT1Threshold(0.04)
+    gm.setPositions(pos)
+    om = oracle_mod.OracleModel(pos, topo.rings, topo.ringCounts, topo.vertexCells, topo.vertexNeighbors, R)
+    om.set_t1_threshold(0.04)
+    gm.enforceTopology()
+    om.lib.orc_enforce_topology(om.h)
+    fg, fo = gm.takeFlips(), om.flips()
+    assert len(fo) > 100
+    assert np.array_equal(fg, fo)
+    assert same_rings(gm, om, 32)
+    assert np.array_equal(gm.vertexCellNeighbors(), om.vertex_cells())
+    assert np.array_equal(gm.vertexNeighbors(), om.vertex_neighbors())
+    assert rel_err(gm.returnPositions(), om.positions(), R) < 1e-14
+    assert gm.deviceStatus() == 0
+
+
+def test_t1_trajectory_n20k_matches_oracle(svm, oracle_mod):
+    """N = 20k from the stabilised preparation: 30 Brownian steps with the reference's noise stream
+    on both sides; the T1 flips (CPU order) and the connectivity agree at every step; the median
+    vertex stays at the last-bit level and the tail near collapsing edges below 1e-3 R."""
+    n = 20000
+    m, _ = stabilised(svm, n, seed=8, stab=100, steps=100)
+    R = m.radius
+    rings, counts = m.rings(32)
+    om = oracle_mod.OracleModel(m.returnPositions(), rings, counts, m.vertexCellNeighbors(), m.vertexNeighbors(), R)
+    om.set_preferred(1.0, 3.8)
+    om.set_t1_threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.setT(0.01)
+    noise = oracle_mod.OracleNoise(99)
+    m.takeFlips(1 << 20)  # drop the preparation's flips
+    total = 0
+    for step in range(30):
+        xi = noise.normals(3 * m.nVertices)
+        bd.injectNoise(xi)
+        bd.integrateEquationOfMotion()
+        om.brownian_step_noise(xi, 0.01, 0.01, 1.0)
+        fg, fo = m.takeFlips(1 << 20), om.flips()
+        assert np.array_equal(fg, fo), step
+        total += len(fo)
+    assert total > 30
+    assert same_rings(m, om, 32)
+    assert np.array_equal(m.vertexNeighbors(), om.vertex_neighbors())
+    # At R = 40 the arcs are ten times shorter than at N = 200, so the 1/theta^2 conditioning of
+    # the reference's gradients is ~100 times stronger: the few vertices at collapsing edges
+    # separate visibly while the bulk stays at the last-bit level.
+    d = np.abs(m.returnPositions() - om.positions()).max(axis=1) / R
+    q = {p: float(np.quantile(d, p)) for p in (0.5, 0.99, 0.999, 1.0)}
+    assert q[0.5] < 1e-9 and q[0.99] < 1e-5 and q[1.0] < 1e-3, q
