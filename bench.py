@@ -271,6 +271,12 @@ def run_ours(args):
     status = model.deviceStatus()
     model.computeGeometry()
     energy_per_cell = model.computeEnergy() / nc
+    cpu_state = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_state = dict(pos=model.returnPositions(), radius=model.radius)
+        cpu_state["rings"], cpu_state["counts"] = model.rings()
+        cpu_state["vcells"], cpu_state["vnbrs"] = model.vertexCellNeighbors(), model.vertexNeighbors()
+    mixed = None if args.no_mixed else time_mixed_form(args, model, bd, stream, flush, nv, nc)
     if rank != 0:
         return
     # ---- roofline of the dominant kernel ----
@@ -285,11 +291,8 @@ def run_ours(args):
     achieved = alg / (avg_launch_ms / 1e3) / 1e9
     traffic = FORCE_BD_DRAM_BYTES_PER_VERTEX * nv if names[dom] == "force" else None
     cpu = None
-    if world == 1 and not args.no_cpu_baseline:
-        state = dict(pos=model.returnPositions(), radius=model.radius)
-        state["rings"], state["counts"] = model.rings()
-        state["vcells"], state["vnbrs"] = model.vertexCellNeighbors(), model.vertexNeighbors()
-        v, secs = cpu_baseline_sample(state, args.cpu_steps)
+    if cpu_state is not None:
+        v, secs = cpu_baseline_sample(cpu_state, args.cpu_steps)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{args.cpu_steps} Brownian steps of the same N=100k workload from the same equilibrated "
                          f"state on one host core ({secs:.1f} s), the reference's serial CPU path restated"}
@@ -318,8 +321,64 @@ def run_ours(args):
         "energy_per_cell": energy_per_cell,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "mixed_form": mixed,
     }
     print(json.dumps(out), flush=True)
+
+
+def algorithmic_bytes_force_mixed(nv: int, nc: int) -> int:
+    """Compulsory bytes of one launch of the mixed-form force + Brownian + move kernel: FP32
+    positions in and out and forces out (3 x 16 B), the three slot triples (36 B), and per cell the
+    FP32 centroid (16 B), (A, P) (16 B) and (A0, P0) (16 B)."""
+    return nv * (16 * 3 + 36) + nc * (16 + 16 + 16)
+
+
+def time_mixed_form(args, model, bd, stream, flush, nv, nc):
+    """The same step in the mixed-precision form (FP32 positions, forces and integration; FP64
+    included angles, areas, energy and renormalisation) from the same equilibrated state, timed the
+    same way.  A secondary line: the headline metric is the FP64 form."""
+    import numpy as np
+    import torch
+    from curvedspacevertexmodel_gb300 import _lib
+    model.precision = "mixed"
+    for _ in range(max(3, args.warmup)):
+        bd.integrateEquationOfMotion()
+    torch.cuda.synchronize()
+    model.t1Stats()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _lib.call("svm_model_profile", model.handle, 1)
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[i].record(stream)
+        bd.integrateEquationOfMotion()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    ms = np.zeros(len(_lib.PHASES), dtype=np.float64)
+    launches = np.zeros(len(_lib.PHASES), dtype=np.int32)
+    _lib.call("svm_model_profile_read", model.handle, ms, launches)
+    _lib.call("svm_model_profile", model.handle, 0)
+    t1 = model.t1Stats()
+    total_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
+    status = model.deviceStatus()
+    model.computeGeometry()
+    e = model.computeEnergy() / nc
+    _, _, fallback = model.areaCheck()
+    model.precision = "fp64"
+    fi = _lib.PHASES.index("force")
+    force_ms = ms[fi] / max(1, launches[fi])
+    alg = algorithmic_bytes_force_mixed(nv, nc)
+    peak, peak_kind = peaks()
+    return {"ms_per_step": total_ms / args.steps, "value": nv * args.steps / (total_ms / 1e3), "unit": UNIT,
+            "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(_lib.PHASES, ms)},
+            "force_kernel": {"kernel": "k32_force_bd", "avg_launch_ms": force_ms, "algorithmic_bytes_per_launch": alg,
+                             "achieved_gbs": alg / (force_ms / 1e3) / 1e9,
+                             "frac_of_" + peak_kind + "_hbm": alg / (force_ms / 1e3) / 1e9 / peak},
+            "t1_per_step": {k: v / args.steps for k, v in t1.items()},
+            "energy_per_cell": e, "area_fallback_taken": bool(fallback), "device_status": status,
+            "gpu_launches": int(launches.sum())}
 
 
 def _lib_phase_count():
@@ -403,6 +462,7 @@ def main():
     ap.add_argument("--equil", type=int, default=200, help="untimed equilibration steps before warm-up")
     ap.add_argument("--cpu-steps", type=int, default=25, help="steps of the one-core CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form's secondary timing")
     ap.add_argument("--ref-cores", type=int, default=0)
     ap.add_argument("--ref-stab", type=int, default=30, help="stabilisation steps of each reference replica")
     args = ap.parse_args()

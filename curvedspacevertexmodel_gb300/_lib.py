@@ -30,6 +30,8 @@ PHASES = ("corners", "cells", "fallback", "force", "t1_apply", "move")
 SVM_NOALLOC_MAX_CELLS = 2097152
 SVM_FIRE_RMS_OVER_N = 0
 SVM_FIRE_MAX_FORCE = 1
+SVM_PRECISION_FP64 = 0
+SVM_PRECISION_MIXED = 1
 
 def _nullable(ptr):
     """An ndpointer type that also accepts None (NULL) for optional outputs."""
@@ -67,6 +69,7 @@ SIGNATURES = {
     "svm_model_set_scalar_model_parameter": (i32, [vp, f64]),
     "svm_model_set_t1_threshold": (i32, [vp, f64]),
     "svm_model_set_restricted_motion": (i32, [vp, i32]),
+    "svm_model_set_precision": (i32, [vp, i32]),
     "svm_model_compute_geometry": (i32, [vp]),
     "svm_model_compute_forces": (i32, [vp]),
     "svm_model_compute_energy": (i32, [vp, C.POINTER(f64)]),

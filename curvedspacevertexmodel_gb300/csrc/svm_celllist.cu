@@ -88,6 +88,10 @@ struct ModelPoints {
     const double4_32a* p;
     __device__ void operator()(int i, double& x, double& y, double& z) const { const double4_32a q = p[i]; x = q.x; y = q.y; z = q.z; }
 };
+struct ModelPoints32 {
+    const float4* p;
+    __device__ void operator()(int i, double& x, double& y, double& z) const { const float4 q = p[i]; x = q.x; y = q.y; z = q.z; }
+};
 struct AosPoints {
     const double* p;
     __device__ void operator()(int i, double& x, double& y, double& z) const { x = p[3 * i]; y = p[3 * i + 1]; z = p[3 * i + 2]; }
@@ -158,6 +162,7 @@ int svm_cell_list_compute_model(svm_cell_list* cl, svm_model* m) {
         cudaStreamWaitEvent(cl->stream, e, 0);
         cudaEventDestroy(e);
     }
+    if (m->precision == SVM_PRECISION_MIXED) return compute(cl, ModelPoints32{m->pos32[m->cur]}, m->nVertices);
     return compute(cl, ModelPoints{m->pos[m->cur]}, m->nVertices);
 }
 

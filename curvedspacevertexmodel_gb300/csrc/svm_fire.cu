@@ -249,6 +249,7 @@ int svm_fire_destroy(svm_fire* F) {
 int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value) {
     if (!F) return SVM_ERR_ARG;
     svm_model* m = F->m;
+    if (m->precision != SVM_PRECISION_FP64) return SVM_ERR_ARG;  // FIRE runs in the FP64 form
     FireState S;
     if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
         cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;

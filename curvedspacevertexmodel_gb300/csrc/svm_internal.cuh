@@ -32,6 +32,14 @@ __device__ __forceinline__ D3 ld3(const double4_32a* p, int i) {
     return D3{t.x, t.y, t.z};
 }
 __device__ __forceinline__ void st3(double4_32a* p, int i, D3 v) { p[i] = make_double4_32a(v.x, v.y, v.z, 0.0); }
+// FP32 positions (mixed-precision form): widened exactly on load, rounded to nearest on store.
+__device__ __forceinline__ D3 ld3(const float4* p, int i) {
+    const float4 t = p[i];
+    return D3{(double)t.x, (double)t.y, (double)t.z};
+}
+__device__ __forceinline__ void st3(float4* p, int i, D3 v) {
+    p[i] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), 0.f);
+}
 __device__ __forceinline__ D3 add3(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ D3 sub3(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ D3 scl3(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
@@ -77,6 +85,13 @@ __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, d
     if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
     if (c < cosLo) return false;
     return R * acos(c) < t;
+}
+// Arc length in the mixed-precision form: 2 R asin(|q - p| / 2R) in FP32 from the raw chord
+// (exact for nearby FP32 points), well conditioned for the short arcs of the model (the acos form
+// loses half its digits there).
+__device__ __forceinline__ float arc32(float4 p, float4 q, float R) {
+    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+    return 2.0f * R * asinf(sqrtf(dx * dx + dy * dy + dz * dz) / (2.0f * R));
 }
 // includedAngle (sphericalDomain.h:114-133)
 __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
@@ -219,6 +234,11 @@ struct svm_model {
     double2* pref = nullptr;
     double4_32a* force = nullptr;
     double4_32a* vel = nullptr;
+    // mixed-precision form (SVM_PRECISION_MIXED): FP32 positions, centroids and forces
+    int precision = SVM_PRECISION_FP64;
+    float4* pos32[2] = {nullptr, nullptr};
+    float4* cellPos32 = nullptr;
+    float4* force32 = nullptr;
     double* noiseBuf = nullptr;        // [3*Nv] staging for host-supplied noise / displacements
     double* dispBuf = nullptr;         // [3*Nv]
     // reductions: per-block partials + ticket (last-block-done pattern)
@@ -262,4 +282,12 @@ int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
 int launch_t1_apply(svm_model* m, int bump);
 int check_launch();
+// mixed-precision kernels (svm_mixed.cu)
+int mixed_launch_corners(svm_model* m, bool t1test);
+int mixed_launch_force(svm_model* m);
+int mixed_launch_force_bd(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise,
+                          uint64_t seed, int nxt);
+int mixed_launch_move(svm_model* m, const double* disp, double scale);
+int mixed_upload_positions(svm_model* m, const double* deviceAos);
+int mixed_download(svm_model* m, const float4* src, int n, double* deviceAos);
 }  // namespace svm

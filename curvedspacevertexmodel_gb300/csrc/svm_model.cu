@@ -135,9 +135,10 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
 // in the CPU's order (ring positions n-2, n-1, 0, ..., n-3), area = (sum - (n-2) pi) wrapped
 // by floor(area / pi), times R^2 (sphericalVertexModel.cpp:228-303).  The last block to finish
 // totals the areas and raises the fallback flag when |sum A - 4 pi R^2| > 1e-6 (304-310).
-__global__ void k_cells(const double4_32a* __restrict__ pos, const int* __restrict__ ring,
+template <class PT>
+__global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring,
                         const int* __restrict__ ringCount, const double2* __restrict__ corner, int Wc, int nC,
-                        double R, double4_32a* __restrict__ cellPos, double4_32a* __restrict__ cellSph,
+                        double R, PT* __restrict__ cellPos, double4_32a* __restrict__ cellSph,
                         double2* __restrict__ ap, double* __restrict__ partials, unsigned* __restrict__ ticket,
                         double* __restrict__ scalars, int* __restrict__ fallbackFlag) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -149,7 +150,7 @@ __global__ void k_cells(const double4_32a* __restrict__ pos, const int* __restri
         for (int k = 0; k < n; ++k) cp = add3(cp, ld3(pos, rg[k]));
         cp = renorm(cp, R);
         st3(cellPos, c, cp);
-        cellSph[c] = sph_coords(cp);
+        if (cellSph) cellSph[c] = sph_coords(cp);
         const double2* cr = corner + (long)c * Wc;
         double per = 0.0, ang = 0.0;
         int k = n - 2;
@@ -189,8 +190,9 @@ __global__ void k_cells(const double4_32a* __restrict__ pos, const int* __restri
 
 // recomputeAreasCPU (sphericalVertexModel.cpp:162-207): area as a sum of spherical triangles
 // (centroid, ring[k-1], ring[k]) starting from (ring[n-2], ring[n-1]).
-__global__ void k_fallback(const double4_32a* __restrict__ pos, const int* __restrict__ ring,
-                           const int* __restrict__ ringCount, const double4_32a* __restrict__ cellPos, int Wc, int nC,
+template <class PT>
+__global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ ring,
+                           const int* __restrict__ ringCount, const PT* __restrict__ cellPos, int Wc, int nC,
                            double R, const int* __restrict__ fallbackFlag, double2* __restrict__ ap) {
     if (*fallbackFlag == 0) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -291,16 +293,18 @@ __global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__
 }
 
 // Standalone T1 edge test (gpu_vm_test_edges_for_T1, sphericalVertexModel.cu:225-273).
-__global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __restrict__ vnbr, int nV, double R,
-                          double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
+__global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __restrict__ pos32,
+                          const int4* __restrict__ vnbr, int nV, double R, double t1Threshold, double cosLo,
+                          double cosHi, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
-    const D3 p = ld3(pos, v);
     const int4 nb = vnbr[v];
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int u = comp(nb, s);
-        if (v < u && shorter_than(p, ld3(pos, u), R, t1Threshold, cosLo, cosHi)) {
+        const bool shortEdge = pos32 ? arc32(pos32[v], pos32[u], (float)R) < (float)t1Threshold
+                                     : shorter_than(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi);
+        if (v < u && shortEdge) {
             const int q = 3 * v + s;
             atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
             atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -312,6 +316,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const int4* __res
 // ---- T1 apply ------------------------------------------------------------------------------
 struct ApplyArgs {
     double cosLo, cosHi;   // shorter_than bracket of cos(t1Threshold / R)
+    float4* pos32;         // FP32 positions in the mixed-precision form, else null
     double4_32a* pos;
     double4_32a* vsph;
     int4 *vcell, *vnbr, *vlast, *vnext, *vrpos;
@@ -326,6 +331,15 @@ struct ApplyArgs {
 };
 
 __device__ __forceinline__ int& compRef(int4* a, int v, int s) { return reinterpret_cast<int*>(a + v)[s]; }
+__device__ __forceinline__ D3 apos(const ApplyArgs& A, int i) { return A.pos32 ? ld3(A.pos32, i) : ld3(A.pos, i); }
+__device__ __forceinline__ void apos_st(const ApplyArgs& A, int i, D3 v) {
+    if (A.pos32) st3(A.pos32, i, v);
+    else st3(A.pos, i, v);
+}
+__device__ __forceinline__ double4_32a apos4(const ApplyArgs& A, int i) {
+    const D3 p = apos(A, i);
+    return make_double4_32a(p.x, p.y, p.z, 0.0);
+}
 
 // Locate `target` in ring `cell` the way getCellVertexSetForT1 does
 // (sphericalVertexModel.cpp:642-652): returns its predecessor and successor.
@@ -411,7 +425,7 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
     if (undo) {
         undo->v1 = v1; undo->v2 = v2; undo->b = vs.y; undo->c = vs.z;
         undo->cells[0] = cs.x; undo->cells[1] = cs.y; undo->cells[2] = cs.z; undo->cells[3] = cs.w;
-        undo->p1 = A.pos[v1]; undo->p2 = A.pos[v2];
+        undo->p1 = apos4(A, v1); undo->p2 = apos4(A, v2);
         undo->vc1 = A.vcell[v1]; undo->vc2 = A.vcell[v2];
         undo->vn[0] = A.vnbr[v1]; undo->vn[1] = A.vnbr[v2]; undo->vn[2] = A.vnbr[vs.y]; undo->vn[3] = A.vnbr[vs.z];
         for (int q = 0; q < 4; ++q) {
@@ -421,10 +435,10 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
             for (int k = 0; k < n; ++k) undoRings[q * A.Wc + k] = A.ring[(long)cell * A.Wc + k];
         }
     }
-    D3 p1 = ld3(A.pos, v1), p2 = ld3(A.pos, v2);
+    D3 p1 = apos(A, v1), p2 = apos(A, v2);
     D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
     mid = renorm_exact(mid, 1.0);
-    const D3 vC = ld3(A.pos, vs.z);
+    const D3 vC = apos(A, vs.z);
     double det = vC.x * (p1.y * p2.z - p1.z * p2.y) + vC.y * (p1.z * p2.x - p1.x * p2.z) + vC.z * (p1.x * p2.y - p1.y * p2.x);
     det = det > 0 ? 1. : -1.;
     const double theta = -0.5 * det * kPI;
@@ -433,8 +447,8 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
     const D3 diff{__dmul_rn(0.5, __dsub_rn(p1.x, p2.x)), __dmul_rn(0.5, __dsub_rn(p1.y, p2.y)), __dmul_rn(0.5, __dsub_rn(p1.z, p2.z))};
     p1 = D3{__dadd_rn(p1.x, diff.x), __dadd_rn(p1.y, diff.y), __dadd_rn(p1.z, diff.z)};
     p2 = D3{__dsub_rn(p2.x, diff.x), __dsub_rn(p2.y, diff.y), __dsub_rn(p2.z, diff.z)};
-    st3(A.pos, v1, renorm_exact(p1, A.R));
-    st3(A.pos, v2, renorm_exact(p2, A.R));
+    apos_st(A, v1, renorm_exact(p1, A.R));
+    apos_st(A, v2, renorm_exact(p2, A.R));
     for (int k = 0; k < 3; ++k) {
         if (compRef(A.vcell, v1, k) == cs.z) compRef(A.vcell, v1, k) = cs.w;
         if (compRef(A.vcell, v2, k) == cs.x) compRef(A.vcell, v2, k) = cs.y;
@@ -470,15 +484,21 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
                 compRef(A.vlast, u, s) = last;
                 compRef(A.vnext, u, s) = next;
             }
-        const D3 pl = ld3(A.pos, last), p = ld3(A.pos, u), px = ld3(A.pos, next);
-        A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
-        A.vsph[u] = sph_coords(p);
+        const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
+        if (A.pos32) {
+            A.corner[(long)cell * A.Wc + k] =
+                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)A.R), included_angle(pl, p, px));
+        } else {
+            A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
+            A.vsph[u] = sph_coords(p);
+        }
     }
 }
 
 // Restores everything a committed flip overwrote.
 __device__ void t1_undo(const ApplyArgs& A, const UndoEntry& u, const int* undoRings) {
-    A.pos[u.v1] = u.p1; A.pos[u.v2] = u.p2;
+    apos_st(A, u.v1, D3{u.p1.x, u.p1.y, u.p1.z});
+    apos_st(A, u.v2, D3{u.p2.x, u.p2.y, u.p2.z});
     A.vcell[u.v1] = u.vc1; A.vcell[u.v2] = u.vc2;
     A.vnbr[u.v1] = u.vn[0]; A.vnbr[u.v2] = u.vn[1]; A.vnbr[u.b] = u.vn[2]; A.vnbr[u.c] = u.vn[3];
     for (int q = 0; q < 4; ++q) {
@@ -491,7 +511,9 @@ __device__ void t1_undo(const ApplyArgs& A, const UndoEntry& u, const int* undoR
 __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
     const int v = q / 3, s = q - 3 * (q / 3);
     const int u = compRef(A.vnbr, v, s);
-    return v < u && shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi);
+    if (!(v < u)) return false;
+    if (A.pos32) return arc32(A.pos32[v], A.pos32[u], (float)A.R) < (float)A.t1Threshold;
+    return shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi);
 }
 
 // Applies the flagged T1 flips in the order of the CPU loop (ascending vertex1, then slot),
@@ -894,6 +916,7 @@ static ForceArgs force_args(svm_model* m, int buf) {
 }
 static ApplyArgs apply_args(svm_model* m, int bump) {
     ApplyArgs A;
+    A.pos32 = m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr;
     A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vnbr = m->vnbr; A.vlast = m->vlast;
     A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
@@ -904,6 +927,10 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
 
 int launch_corners(svm_model* m, bool t1test) {
     PhaseTimer pt(m, SVM_PHASE_CORNERS);
+    if (m->precision == SVM_PRECISION_MIXED) {
+        m->cornersValid = true;
+        return mixed_launch_corners(m, t1test);
+    }
     double lo, hi;
     t1_bracket(m->t1Threshold, m->R, &lo, &hi);
     k_corners<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
@@ -915,15 +942,25 @@ int launch_corners(svm_model* m, bool t1test) {
 
 static int launch_cells(svm_model* m) {
     const int nb = blocksFor(m->nCells);
+    const bool mixed = m->precision == SVM_PRECISION_MIXED;
     {
         PhaseTimer pt(m, SVM_PHASE_CELLS, 1);
-        k_cells<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R,
-                                               m->cellPos, m->cellSph, m->ap, m->partials, m->ticket, m->scalars,
-                                               m->fallbackFlag);
+        if (mixed)
+            k_cells<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc,
+                                                          m->nCells, m->R, m->cellPos32, nullptr, m->ap, m->partials,
+                                                          m->ticket, m->scalars, m->fallbackFlag);
+        else
+            k_cells<double4_32a><<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc,
+                                                               m->nCells, m->R, m->cellPos, m->cellSph, m->ap,
+                                                               m->partials, m->ticket, m->scalars, m->fallbackFlag);
     }
     PhaseTimer pt(m, SVM_PHASE_FALLBACK);
-    k_fallback<<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc, m->nCells,
-                                              m->R, m->fallbackFlag, m->ap);
+    if (mixed)
+        k_fallback<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc,
+                                                         m->nCells, m->R, m->fallbackFlag, m->ap);
+    else
+        k_fallback<double4_32a><<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc,
+                                                              m->nCells, m->R, m->fallbackFlag, m->ap);
     return check_launch();
 }
 
@@ -951,14 +988,16 @@ static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, 
     const int nxt = 1 - m->cur;
     {
     PhaseTimer pt(m, SVM_PHASE_FORCE);
-    if (noiseMode == SVM_NOISE_BUFFER)
+    if (m->precision == SVM_PRECISION_MIXED)
+        rc = mixed_launch_force_bd(m, T, dt, mu, noiseMode, noise, seed, nxt);
+    else if (noiseMode == SVM_NOISE_BUFFER)
         k_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
             force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     else
         k_force_bd<SVM_NOISE_PHILOX><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
             force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     }
-    if ((rc = check_launch())) return rc;
+    if (rc || (rc = check_launch())) return rc;
     m->cur = nxt;
     // corners of the moved state, with the T1 edge test fused in
     rc = launch_corners(m, !m->restricted);
@@ -1134,7 +1173,8 @@ int svm_model_destroy(svm_model* m) {
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
                     m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
-                    m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats};
+                    m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
+                    m->pos32[0], m->pos32[1], m->cellPos32, m->force32};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
     for (auto& v : m->profEvents) for (cudaEvent_t e : v) cudaEventDestroy(e);
@@ -1164,6 +1204,11 @@ static int upload_vec(svm_model* m, const double* in, double4_32a* dst, int n) {
 
 static int upload_positions(svm_model* m, const double* in) {
     int rc = upload_vec(m, in, m->pos[m->cur], m->nVertices);
+    if (!rc && m->precision == SVM_PRECISION_MIXED) {
+        // dispBuf still holds the AoS copy; round it to the FP32 positions
+        if (svm::mixed_upload_positions(m, m->dispBuf)) return SVM_ERR_CUDA;
+        SVM_CUDA(cudaStreamSynchronize(m->stream));
+    }
     m->cornersValid = false;
     return rc;
 }
@@ -1245,6 +1290,7 @@ int svm_model_compute_forces(svm_model* m) {
     int rc = svm_model_compute_geometry(m);
     if (rc) return rc;
     svm::PhaseTimer pt(m, SVM_PHASE_FORCE);
+    if (m->precision == SVM_PRECISION_MIXED) return svm::mixed_launch_force(m);
     k_force<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(svm::force_args(m, m->cur), m->nVertices, m->force);
     return svm::check_launch();
 }
@@ -1264,8 +1310,9 @@ int svm_model_enforce_topology(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     double lo, hi;
     svm::t1_bracket(m->t1Threshold, m->R, &lo, &hi);
-    k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnbr, m->nVertices, m->R,
-                                                                             m->t1Threshold, lo, hi, m->t1);
+    k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
+        m->pos[m->cur], m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr, m->vnbr, m->nVertices, m->R,
+        m->t1Threshold, lo, hi, m->t1);
     if (svm::check_launch()) return SVM_ERR_CUDA;
     // the patch of touched cells writes corners; all of them are recomputed before their next use
     int rc = svm::launch_t1_apply(m, 0);
@@ -1277,7 +1324,11 @@ int svm_model_move_particles(svm_model* m, const double* disp, double scale) {
     if (!m || !disp) return SVM_ERR_ARG;
     {
     svm::PhaseTimer pt(m, SVM_PHASE_MOVE);
-    k_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], disp, scale, m->nVertices, m->R);
+    if (m->precision == SVM_PRECISION_MIXED) {
+        if (svm::mixed_launch_move(m, disp, scale)) return SVM_ERR_CUDA;
+    } else {
+        k_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], disp, scale, m->nVertices, m->R);
+    }
     }
     if (svm::check_launch()) return SVM_ERR_CUDA;
     m->cornersValid = false;
@@ -1301,11 +1352,31 @@ static int get_vec4(svm_model* m, const double4_32a* src, int n, double* out) {
     return SVM_OK;
 }
 
-int svm_model_get_positions(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->pos[m->cur], m->nVertices, out); }
+// FP32 device vectors (mixed form) -> host AoS double[3n], widened exactly
+static int get_vec4f(svm_model* m, const float4* src, int n, double* out) {
+    if (n > m->nVertices) return SVM_ERR_ARG;
+    if (svm::mixed_download(m, src, n, m->dispBuf)) return SVM_ERR_CUDA;
+    SVM_CUDA(cudaMemcpyAsync(out, m->dispBuf, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+static bool mixed(const svm_model* m) { return m->precision == SVM_PRECISION_MIXED; }
+
+int svm_model_get_positions(svm_model* m, double* out) {
+    if (!m || !out) return SVM_ERR_ARG;
+    return mixed(m) ? get_vec4f(m, m->pos32[m->cur], m->nVertices, out) : get_vec4(m, m->pos[m->cur], m->nVertices, out);
+}
 int svm_model_set_positions(svm_model* m, const double* in) { if (!m || !in) return SVM_ERR_ARG; return upload_positions(m, in); }
-int svm_model_get_forces(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->force, m->nVertices, out); }
+int svm_model_get_forces(svm_model* m, double* out) {
+    if (!m || !out) return SVM_ERR_ARG;
+    return mixed(m) ? get_vec4f(m, m->force32, m->nVertices, out) : get_vec4(m, m->force, m->nVertices, out);
+}
 int svm_model_get_velocities(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->vel, m->nVertices, out); }
-int svm_model_get_cell_positions(svm_model* m, double* out) { if (!m || !out) return SVM_ERR_ARG; return get_vec4(m, m->cellPos, m->nCells, out); }
+int svm_model_get_cell_positions(svm_model* m, double* out) {
+    if (!m || !out) return SVM_ERR_ARG;
+    return mixed(m) ? get_vec4f(m, m->cellPos32, m->nCells, out) : get_vec4(m, m->cellPos, m->nCells, out);
+}
 
 int svm_model_set_velocities(svm_model* m, const double* in) {
     if (!m || !in) return SVM_ERR_ARG;
@@ -1428,7 +1499,7 @@ int svm_model_stream(svm_model* m, void** s) {
 
 int svm_model_device_positions(svm_model* m, void** p) {
     if (!m || !p) return SVM_ERR_ARG;
-    *p = m->pos[m->cur];
+    *p = m->precision == SVM_PRECISION_MIXED ? (void*)m->pos32[m->cur] : (void*)m->pos[m->cur];
     return SVM_OK;
 }
 

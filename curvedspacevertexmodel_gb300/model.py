@@ -151,6 +151,18 @@ class sphericalVertexModel:
         call("svm_model_set_t1_threshold", self._h, self.t1Threshold)
 
     @property
+    def precision(self) -> str:
+        """'fp64' (every quantity in FP64) or 'mixed' (FP32 positions, forces and integration;
+        FP64 included angles, areas, energy and renormalisation)."""
+        return getattr(self, "_precision", "fp64")
+
+    @precision.setter
+    def precision(self, p: str):
+        code = {"fp64": _lib.SVM_PRECISION_FP64, "mixed": _lib.SVM_PRECISION_MIXED}[p]
+        call("svm_model_set_precision", self._h, code)
+        self._precision = p
+
+    @property
     def restrictedMotion(self) -> bool:
         return self._restricted
 

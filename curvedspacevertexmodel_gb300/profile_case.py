@@ -5,6 +5,7 @@
 Builds a model of N cells from the seeded recipe, runs `stab` stabilisation steps (T = 0, P0 = 1,
 as the reference driver does) and then `steps` Brownian steps at T = 0.01, P0 = 3.8, dt = 0.01
 (T1 threshold 0.04), one launch per kernel per step (no graph), and prints the energy per cell.
+With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*).
 """
 from __future__ import annotations
 
@@ -20,6 +21,7 @@ def main():
     ap.add_argument("--stab", type=int, default=2)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--seed", type=int, default=1137)
+    ap.add_argument("--mixed", action="store_true", help="run the timed steps in the mixed-precision form")
     args = ap.parse_args()
     t0 = time.time()
     noise = svm.noiseSource()
@@ -35,6 +37,8 @@ def main():
         bd.integrateEquationOfMotion()
     bd.setT(0.01)
     m.setPreferredParameters(1.0, 3.8)
+    if args.mixed:
+        m.precision = "mixed"
     for _ in range(args.steps):
         bd.integrateEquationOfMotion()
     m.computeGeometry()

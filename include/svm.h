@@ -84,6 +84,17 @@ void svm_topology_free(svm_topology* t);
 typedef struct svm_model svm_model;
 int svm_model_create(int nCells, int nVertices, int ringCapacity, double radius, void* stream, svm_model** out);
 int svm_model_destroy(svm_model* m);
+/* Arithmetic of the step (no counterpart in the reference, whose scalar type is fixed at compile
+ * time, inc/std_include.h:49-78):
+ *   SVM_PRECISION_FP64  - the plain form: every quantity in FP64 (default);
+ *   SVM_PRECISION_MIXED - FP32 positions, forces and integration, with the included angles and
+ *                         the spherical-excess areas, the energy accumulation and the
+ *                         renormalisation onto the sphere in FP64.
+ * Switching converts the current positions.  FIRE runs in the FP64 form only. */
+#define SVM_PRECISION_FP64 0
+#define SVM_PRECISION_MIXED 1
+int svm_model_set_precision(svm_model* m, int precision);
+
 /* Upload topology and positions (host arrays, reference layouts). */
 int svm_model_set_topology(svm_model* m, const double* vertexPos, const int* rings, int ringStride,
                            const unsigned* ringCounts, const int* vertexCells, const int* vertexNeighbors);
@@ -137,8 +148,9 @@ int svm_model_take_flips(svm_model* m, int* pairs, int capacity, int* count);
  * at a time after a rollback.  (The reference's T1 loop keeps no such counters.) */
 int svm_model_t1_stats(svm_model* m, int* stats6);
 int svm_model_synchronize(svm_model* m);
-/* Device pointers of the model's arrays (double4 positions / forces, etc.) for callers that
- * keep data on the GPU.  Valid until svm_model_destroy. */
+/* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
+ * z, unused) per vertex in the FP64 form, float4 in the mixed form.  Valid until the next step,
+ * precision switch or svm_model_destroy. */
 int svm_model_device_positions(svm_model* m, void** ptr);
 /* The CUDA stream (cudaStream_t) all of the model's work is ordered on. */
 int svm_model_stream(svm_model* m, void** stream);

@@ -45,3 +45,66 @@ def same_rings(gm, om, W=16):
     r1, c1 = gm.rings(W)
     r2, c2 = om.rings(W)
     return np.array_equal(c1, c2) and np.array_equal(r1, r2)
+
+
+def stabilised(svm, n, seed=5, stab=100, steps=200):
+    """The reference driver's preparation (sphericalVertex.cpp:104-125): T = 0 with P0 = 1, then
+    Brownian steps at T = 0.01, P0 = 3.8 (a raw random-Voronoi start diverges at large N in the
+    reference itself)."""
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(seed)
+    m = svm.sphericalVertexModel(n, noise)
+    m.setT1Threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.noise.setReproducibleSeed(seed + 1)
+    bd.setT(0.0)
+    m.setPreferredParameters(1.0, 1.0)
+    bd.run(stab)
+    bd.setT(0.01)
+    m.setPreferredParameters(1.0, 3.8)
+    bd.run(steps)
+    return m, bd
+
+
+def vector_forces(pos, rings, counts, ap, pref, cellpos, R, kr=1.0):
+    """Host FP64 evaluation of the model force -dE/dv as vectors of position differences (the
+    formulas of the mixed-precision kernels, written independently in numpy): per (vertex, cell)
+    slot, -2 dP [g(v, last) + g(v, next)] - 2 Kr dA [t(v, last, c) + t(v, c, next)] with g the
+    geodesic-length gradient and t the signed spherical-triangle-area gradient (Van Oosterom and
+    Strackee's tan(E/2) = N / D, differentiated)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    v_l, c_l, l_l, x_l = [], [], [], []
+    for c in range(rings.shape[0]):
+        ring = rings[c, : counts[c]]
+        v_l.append(ring)
+        l_l.append(np.roll(ring, 1))
+        x_l.append(np.roll(ring, -1))
+        c_l.append(np.full(len(ring), c))
+    v, c, last, nxt = (np.concatenate(a) for a in (v_l, c_l, l_l, x_l))
+    P = pos[v]
+    r = np.linalg.norm(P, axis=1, keepdims=True)
+    a = P / r
+
+    def dot(x, y):
+        return np.sum(x * y, axis=1, keepdims=True)
+
+    def geo(d):
+        t = d - dot(d, a) * a
+        return -t / np.linalg.norm(t, axis=1, keepdims=True)
+
+    def tri(beta, gamma):
+        bg = np.cross(beta, gamma)
+        bxc = np.cross(a, gamma) + np.cross(beta, a) + bg
+        N = dot(a, bg)
+        D = 4.0 - dot(beta, beta) - dot(gamma, gamma) + dot(beta, gamma)
+        g = 2.0 * (D * bxc - N * (beta + gamma)) / (N * N + D * D)
+        return R * (g - dot(g, a) * a)
+
+    dl, dx, dc = pos[last] - P, pos[nxt] - P, cellpos[c] - P
+    dA = (ap[c, 0] - pref[c, 0])[:, None]
+    dP = (ap[c, 1] - pref[c, 1])[:, None]
+    fs = -2.0 * dP * (geo(dl) + geo(dx)) - 2.0 * kr * dA * (tri(dl / r, dc / r) + tri(dc / r, dx / r))
+    f = np.zeros_like(pos)
+    np.add.at(f, v, fs)
+    return f

@@ -4,7 +4,7 @@ exactly."""
 import numpy as np
 import pytest
 
-from gpu_helpers import gpu_model, load_gold, oracle_model, params, rel_err, same_rings
+from gpu_helpers import gpu_model, load_gold, oracle_model, params, rel_err, same_rings, stabilised
 
 pytestmark = pytest.mark.gpu
 
@@ -33,26 +33,6 @@ def svm(svm_lib):
 @pytest.fixture(scope="module")
 def gold():
     return load_gold()
-
-
-def stabilised(svm, n, seed=5, stab=100, steps=200):
-    """The reference driver's preparation (sphericalVertex.cpp:104-125): T = 0 with P0 = 1, then
-    Brownian steps at T = 0.01, P0 = 3.8 (a raw random-Voronoi start diverges at large N in the
-    reference itself)."""
-    noise = svm.noiseSource()
-    noise.setReproducibleSeed(seed)
-    m = svm.sphericalVertexModel(n, noise)
-    m.setT1Threshold(0.04)
-    bd = svm.brownianDynamics()
-    bd.setModel(m)
-    bd.noise.setReproducibleSeed(seed + 1)
-    bd.setT(0.0)
-    m.setPreferredParameters(1.0, 1.0)
-    bd.run(stab)
-    bd.setT(0.01)
-    m.setPreferredParameters(1.0, 3.8)
-    bd.run(steps)
-    return m, bd
 
 
 def test_geometry_forces_energy_match_golden(svm, gold):

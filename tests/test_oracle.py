@@ -153,3 +153,64 @@ def test_area_fallback_against_reference(oracle_mod):
     ref.compute_forces()
     m.compute_forces()
     assert np.array_equal(ref.forces(), m.forces())
+
+
+def test_vector_form_forces_match_reference(oracle_mod, gold):
+    """The host FP64 vector-form force (the mixed-precision kernels' formulas) against the
+    reference's closed-form forces on the golden N = 200 state and on an N = 2000 state after the
+    stabilised preparation: agreement to rounding except where the reference's triangle-gradient
+    formula loses digits on a nearly degenerate centroid-fan triangle, and there the vector form
+    matches a central finite difference of the reference energy."""
+    from gpu_helpers import vector_forces
+    from curvedspacevertexmodel_gb300 import Topology, random_cell_centres
+
+    g = gold
+    m = oracle_from(oracle_mod, g)
+    m.compute_forces()
+    N, SEED, BD_SEED, A0, P0, KR, T, MU, DT, T1 = g["params"]
+    pref = np.tile([A0, P0], (int(N), 1))
+    rings, counts = m.rings(32)
+    f = vector_forces(m.positions(), rings, counts, m.area_perimeter(), pref, m.cell_positions(),
+                      float(g["init_radius"]), KR)
+    fref = m.forces()
+    err = np.linalg.norm(f - fref, axis=1) / np.max(np.linalg.norm(fref, axis=1))
+    assert err.max() < 1e-9
+
+    n = 2000
+    topo = Topology(random_cell_centres(5, n))
+    R = np.sqrt(n / (4 * np.pi))
+    om = oracle_mod.OracleModel(topo.vertexPositions, topo.rings, topo.ringCounts, topo.vertexCells,
+                                topo.vertexNeighbors, R)
+    om.set_t1_threshold(0.04)
+    noise = oracle_mod.OracleNoise(6)
+    om.set_preferred(1.0, 1.0)
+    for _ in range(100):
+        om.brownian_step(noise, 0.0, 0.01)
+    om.set_preferred(1.0, 3.8)
+    for _ in range(300):
+        om.brownian_step(noise, 0.01, 0.01)
+    om.compute_forces()
+    pos, fref = om.positions(), om.forces()
+    rings, counts = om.rings(32)
+    f = vector_forces(pos, rings, counts, om.area_perimeter(), np.tile([1.0, 3.8], (n, 1)), om.cell_positions(), R)
+    fmax = np.max(np.linalg.norm(fref, axis=1))
+    err = np.linalg.norm(f - fref, axis=1) / fmax
+    assert np.quantile(err, 0.99) < 1e-9
+    assert err.max() < 1e-4
+    w = int(np.argmax(err))
+    p = pos[w]
+    a = p / np.linalg.norm(p)
+    e1 = np.cross(a, [0.0, 0.0, 1.0])
+    e1 /= np.linalg.norm(e1)
+    for e in (e1, np.cross(a, e1)):
+        en = []
+        for sgn in (1.0, -1.0):
+            q = pos.copy()
+            q[w] = p + sgn * 1e-6 * e
+            q[w] *= R / np.linalg.norm(q[w])
+            om.set_positions(q)
+            om.compute_geometry()
+            en.append(om.energy())
+        fd = -(en[0] - en[1]) / 2e-6
+        assert abs(f[w] @ e - fd) <= abs(fref[w] @ e - fd) + 1e-7 * fmax
+    om.set_positions(pos)
