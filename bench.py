@@ -46,6 +46,7 @@ N_CELLS = 100_000
 PARAMS = dict(a0=1.0, p0=3.8, kr=1.0, T=0.01, mu=1.0, dt=0.01, t1=0.04)
 SEED = 1137
 BD_SEED = 4242
+BATCH_SEED = 5150
 WORKLOAD = ("spherical vertex model, overdamped Brownian step, FP64 plain form, N=100000 cells "
             "(199996 vertices), A0=1 P0=3.8 KA=KP=1 T=0.01 mu=1 dt=0.01 T1 threshold 0.04, "
             "seeded Voronoi start")
@@ -277,6 +278,7 @@ def run_ours(args):
         cpu_state["rings"], cpu_state["counts"] = model.rings()
         cpu_state["vcells"], cpu_state["vnbrs"] = model.vertexCellNeighbors(), model.vertexNeighbors()
     mixed = None if args.no_mixed else time_mixed_form(args, model, bd, stream, flush, nv, nc)
+    batched = None if args.no_batch else time_batched_replicas(args, rank)
     if rank != 0:
         return
     # ---- roofline of the dominant kernel ----
@@ -322,8 +324,63 @@ def run_ours(args):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "mixed_form": mixed,
+        "batched_replicas": batched,
     }
     print(json.dumps(out), flush=True)
+
+
+def time_batched_replicas(args, rank):
+    """Batched replicas: 512 independent spheres, N per replica log-uniform in [100, 5000] cells,
+    P0 uniform in [3.6, 3.95], T log-uniform in [1e-4, 1e-1], dt = 0.01, T1 threshold 0.04,
+    mixed-precision form, all replicas in each launch and the steps replayed from a captured
+    graph; block sizes from the autotuner.  Prepared like the single sphere (100 steps at T = 0,
+    P0 = 1, then 100 steps at the run parameters).  The state (~150 MB) exceeds L2, so no flush."""
+    import numpy as np
+    import torch
+    import curvedspacevertexmodel_gb300 as svm
+    rng = np.random.default_rng(BATCH_SEED + rank)
+    n_rep = args.replicas
+    sizes = np.exp(rng.uniform(np.log(100), np.log(5000), n_rep)).astype(int)
+    p0s = rng.uniform(3.6, 3.95, n_rep)
+    temps = np.exp(rng.uniform(np.log(1e-4), np.log(1e-1), n_rep))
+    seeds = BATCH_SEED + 1000 * (rank + 1) + np.arange(n_rep)
+    t0 = time.perf_counter()
+    b = svm.sphericalVertexModelBatch(sizes, seeds, p0=1.0)
+    setup_s = time.perf_counter() - t0
+    b.setT1Threshold(PARAMS["t1"])
+    bd = svm.brownianDynamics()
+    bd.setModel(b)
+    bd.setDeltaT(PARAMS["dt"])
+    bd.noise.setReproducibleSeed(BATCH_SEED + 7 + rank)
+    b.setTemperatures(np.zeros(n_rep))
+    bd.run(100)
+    b.setPreferredParameters(1.0, p0s)
+    b.setTemperatures(temps)
+    b.autotune(64, 1024, 64, 3, 100000)
+    bd.run(100)  # tuner sampling (steps run one by one) + equilibration
+    bd.run(args.steps)  # graph capture outside the timed region
+    stream = torch.cuda.ExternalStream(b.streamHandle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b.t1Stats()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bd.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    t1 = b.t1Stats()
+    b.computeGeometry()
+    e = b.replicaEnergies() / sizes
+    _, _, taken = b.replicaAreaCheck()
+    out = {"workload": f"{n_rep} replicas, N log-uniform [100, 5000] cells (total {int(sizes.sum())} cells, "
+                       f"{b.nVertices} vertices), P0 U[3.6, 3.95], T logU[1e-4, 1e-1], dt 0.01, mixed form, T1 on",
+           "seed": BATCH_SEED, "ms_per_step": ms, "value": b.nVertices / (ms / 1e3), "unit": UNIT,
+           "block_sizes": b.blockSizes(), "t1_per_step": {k: v / args.steps for k, v in t1.items()},
+           "energy_per_cell_min_median_max": [float(e.min()), float(np.median(e)), float(e.max())],
+           "area_fallback_replicas": int(taken.sum()), "device_status": b.deviceStatus(),
+           "setup_s": setup_s, "l2": "state ~150 MB > 129 MB L2; steps back to back from one graph"}
+    b.close()
+    return out
 
 
 def algorithmic_bytes_force_mixed(nv: int, nc: int) -> int:
@@ -463,6 +520,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=25, help="steps of the one-core CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form's secondary timing")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-replica secondary timing")
+    ap.add_argument("--replicas", type=int, default=512)
     ap.add_argument("--ref-cores", type=int, default=0)
     ap.add_argument("--ref-stab", type=int, default=30, help="stabilisation steps of each reference replica")
     args = ap.parse_args()

@@ -11,9 +11,11 @@ from .model import (  # noqa: F401
     noiseSource,
     random_cell_centres,
     sphericalVertexModel,
+    sphericalVertexModelBatch,
 )
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
     "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "sphericalVertexModel",
+    "sphericalVertexModelBatch",
 ]

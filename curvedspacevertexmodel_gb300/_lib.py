@@ -45,6 +45,7 @@ def _nullable(ptr):
 dp = _nullable(np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS"))
 ip = _nullable(np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS"))
 up = _nullable(np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS"))
+fp = _nullable(np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS"))
 vp = C.c_void_p
 i32 = C.c_int
 f64 = C.c_double
@@ -109,6 +110,22 @@ SIGNATURES = {
     "svm_cell_list_compute": (i32, [vp, vp, i32]),
     "svm_cell_list_get": (i32, [vp, C.POINTER(i32), C.POINTER(i32), up, ip, C.c_long]),
     "svm_cell_list_bins": (i32, [vp, ip]),
+    "svm_batch_create": (i32, [i32, ip, ip, i32, dp, vp, pvp]),
+    "svm_batch_replicas": (i32, [vp, C.POINTER(i32)]),
+    "svm_batch_offsets": (i32, [vp, ip, ip]),
+    "svm_batch_set_temperatures": (i32, [vp, dp]),
+    "svm_batch_energies": (i32, [vp, dp]),
+    "svm_batch_area_check": (i32, [vp, dp, dp, ip]),
+    "svm_batch_autotune": (i32, [vp, i32, i32, i32, i32, i32]),
+    "svm_batch_block_sizes": (i32, [vp, ip, C.POINTER(i32)]),
+    "svm_tuner_create": (i32, [i32, i32, i32, i32, i32, vp, pvp]),
+    "svm_tuner_destroy": (i32, [vp]),
+    "svm_tuner_begin": (i32, [vp]),
+    "svm_tuner_end": (i32, [vp]),
+    "svm_tuner_record": (i32, [vp, C.c_float]),
+    "svm_tuner_parameter": (i32, [vp, C.POINTER(i32)]),
+    "svm_tuner_sampling_complete": (i32, [vp, C.POINTER(i32)]),
+    "svm_tuner_timing_data": (i32, [vp, ip, fp, i32, C.POINTER(i32)]),
 }
 
 

@@ -69,7 +69,8 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if _needs(obj, [src] + headers):
-            jobs.append([shutil.which("g++") or "g++", *CXX_FLAGS, "-c", src, "-o", obj])
+            cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+            jobs.append([shutil.which("g++") or "g++", *CXX_FLAGS, "-I" + cuda_inc, "-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:

@@ -11,6 +11,7 @@
 //                  the last block reduces them in a fixed order and runs the FIRE control
 //                  (power test, dt / alpha adaptation, stopping test)
 // The host launches captured batches of iterations and reads only the `done` flag between them.
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 #include "svm_internal.cuh"
@@ -211,6 +212,10 @@ int fire_iteration(svm_fire* F) {
 
 }  // namespace
 
+namespace svm {
+void fire_detach(svm_fire* F) { F->m = nullptr; }
+}  // namespace svm
+
 extern "C" {
 
 int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, double dtInc, double dtDec,
@@ -218,6 +223,7 @@ int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, do
     if (!m || !out || !(dt > 0) || maxIterations < 0) return SVM_ERR_ARG;
     svm_fire* F = new svm_fire();
     F->m = m;
+    m->fires.push_back(F);
     FireState& S = F->h;
     S = FireState{};
     S.dt = dt; S.dtMin = dt * .01; S.alphaStart = alphaStart; S.alpha = alphaStart; S.dtMax = dtMax;
@@ -237,7 +243,11 @@ int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, do
 
 int svm_fire_destroy(svm_fire* F) {
     if (!F) return SVM_ERR_ARG;
-    if (F->m && F->m->stream) cudaStreamSynchronize(F->m->stream);
+    if (F->m) {
+        auto& v = F->m->fires;
+        v.erase(std::remove(v.begin(), v.end(), F), v.end());
+        if (F->m->stream) cudaStreamSynchronize(F->m->stream);
+    }
     if (F->graph) cudaGraphExecDestroy(F->graph);
     if (F->d) cudaFree(F->d);
     if (F->partials) cudaFree(F->partials);
@@ -247,7 +257,7 @@ int svm_fire_destroy(svm_fire* F) {
 }
 
 int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value) {
-    if (!F) return SVM_ERR_ARG;
+    if (!F || !F->m) return SVM_ERR_ARG;
     svm_model* m = F->m;
     if (m->precision != SVM_PRECISION_FP64) return SVM_ERR_ARG;  // FIRE runs in the FP64 form
     FireState S;
@@ -301,7 +311,7 @@ int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value
 }
 
 int svm_fire_state(svm_fire* F, double* s7) {
-    if (!F || !s7) return SVM_ERR_ARG;
+    if (!F || !F->m || !s7) return SVM_ERR_ARG;
     FireState S;
     if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, F->m->stream) != cudaSuccess ||
         cudaStreamSynchronize(F->m->stream) != cudaSuccess) return SVM_ERR_CUDA;

@@ -40,6 +40,13 @@ __device__ __forceinline__ D3 ld3(const float4* p, int i) {
 __device__ __forceinline__ void st3(float4* p, int i, D3 v) {
     p[i] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), 0.f);
 }
+// In the mixed form the w component of a vertex's FP32 position holds its replica index (0 for a
+// single sphere); rounded stores of a vertex keep it.
+__device__ __forceinline__ void st3_keep(float4* p, int i, D3 v) {
+    p[i] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), p[i].w);
+}
+__device__ __forceinline__ int rep_of(const float4& p) { return (int)p.w; }
+__device__ __forceinline__ int rep_of(const double4_32a&) { return 0; }
 __device__ __forceinline__ D3 add3(D3 a, D3 b) { return D3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ D3 sub3(D3 a, D3 b) { return D3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ D3 scl3(double s, D3 a) { return D3{s * a.x, s * a.y, s * a.z}; }
@@ -239,6 +246,24 @@ struct svm_model {
     float4* pos32[2] = {nullptr, nullptr};
     float4* cellPos32 = nullptr;
     float4* force32 = nullptr;
+    // replicas (mixed form): per-replica radius, noise amplitude and reductions.  A single sphere
+    // is one replica; vertex v of replica r has pos32[v].w = r, replica r owns cells
+    // [repCellOff[r], repCellOff[r+1]) and vertices [repVertOff[r], repVertOff[r+1]).
+    int nRep = 1;
+    double* repR = nullptr;            // device [nRep]
+    float* repNp = nullptr;            // device [nRep], sqrt(2 dt mu T_r) of the batch's last step
+    int* repCellOff = nullptr;         // device [nRep + 1]
+    int* repFlag = nullptr;            // device [nRep], area-check fallback flags
+    double* repScal = nullptr;         // device [3 nRep]: total area, excess, energy
+    std::vector<double> repT;          // host, per-replica temperatures of a batch
+    std::vector<int> hRepCellOff, hRepVertOff;
+    double repNpDt = -1, repNpMu = -1; // (dt, mu) repNp was computed for
+    unsigned repTVersion = 0, repNpVersion = ~0u;
+    // block sizes of the batch's per-element kernels (picked by the autotuner)
+    int blkCorners = 256, blkCells = 256, blkForce = 256;
+    void* tuners = nullptr;            // svm::BatchTuners when autotuning is on
+    // FIRE minimizers created on this model; destroying the model detaches them
+    std::vector<svm_fire*> fires;
     double* noiseBuf = nullptr;        // [3*Nv] staging for host-supplied noise / displacements
     double* dispBuf = nullptr;         // [3*Nv]
     // reductions: per-block partials + ticket (last-block-done pattern)
@@ -282,6 +307,18 @@ int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
 int launch_t1_apply(svm_model* m, int bump);
 int check_launch();
+void fire_detach(svm_fire* F);          // svm_fire.cu: the model is going away
+int model_alloc(int nCells, int nVertices, int Wc, const double* radius, int nRep, void* stream, svm_model** out);
+// replicas (svm_batch.cu)
+int launch_rep_check(svm_model* m);
+int update_rep_noise(svm_model* m, double dt, double mu);
+void batch_release(svm_model* m);
+int batch_tuned_corners(svm_model* m, bool t1test);
+int batch_tuned_cells(svm_model* m, int (*launch)(svm_model*));
+int batch_tuned_force_bd(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise,
+                         uint64_t seed, int nxt);
+bool batch_tuning(svm_model* m);
+void batch_tuner_untimed(svm_model* m, int calls);
 // mixed-precision kernels (svm_mixed.cu)
 int mixed_launch_corners(svm_model* m, bool t1test);
 int mixed_launch_force(svm_model* m);

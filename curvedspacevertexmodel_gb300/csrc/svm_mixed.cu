@@ -63,13 +63,14 @@ struct Args32 {
     const float4* cellPos;
     const double2* ap;
     const double2* pref;
-    float Kr, R;
+    const double* repR;    // per-replica radius, indexed by pos[v].w
+    float Kr;
 };
 
 __device__ __forceinline__ int comp(const int4& a, int s) { return s == 0 ? a.x : (s == 1 ? a.y : a.z); }
 
 // Per-vertex force of the quadratic model (the sum of sphericalVertexModel.cpp:380-417) in FP32.
-__device__ __forceinline__ F3 vertex_force32(const Args32& A, int v) {
+__device__ __forceinline__ F3 vertex_force32(const Args32& A, int v, float R) {
     const F3 P = f3(A.pos[v]);
     const float inv = 1.0f / sqrtf(dotf(P, P));
     const F3 a = inv * P;
@@ -85,19 +86,20 @@ __device__ __forceinline__ F3 vertex_force32(const Args32& A, int v) {
         const float pp = 2.0f * dP, aa = 2.0f * A.Kr * dA;
         const F3 bl = inv * dl, bc = inv * dc, bx = inv * dx;
         const F3 fs = (-pp) * (grad_geo32(a, dl) + grad_geo32(a, dx)) +
-                      (-aa) * (grad_tri32(a, bl, bc, A.R) + grad_tri32(a, bc, bx, A.R));
+                      (-aa) * (grad_tri32(a, bl, bc, R) + grad_tri32(a, bc, bx, R));
         if (!isnan(fs.x)) f = f + fs;
     }
     return f;
 }
 
-// p <- R (p + P_p d) / |p + P_p d| in FP64 from FP32 p and d, rounded to FP32.
+// p <- R (p + P_p d) / |p + P_p d| in FP64 from FP32 p and d, rounded to FP32 (w, the replica,
+// carried over).
 __device__ __forceinline__ float4 move_fp64(float4 p, F3 d, double R) {
     const double px = p.x, py = p.y, pz = p.z, dx = d.x, dy = d.y, dz = d.z;
     const double s = (dx * px + dy * py + dz * pz) / (px * px + py * py + pz * pz);
     const double qx = px + (dx - s * px), qy = py + (dy - s * py), qz = pz + (dz - s * pz);
     const double k = R / sqrt(qx * qx + qy * qy + qz * qz);
-    return make_float4(__double2float_rn(k * qx), __double2float_rn(k * qy), __double2float_rn(k * qz), 0.f);
+    return make_float4(__double2float_rn(k * qx), __double2float_rn(k * qy), __double2float_rn(k * qz), p.w);
 }
 
 // Philox4x32-10 (Salmon et al., SC'11), as in the FP64 form.
@@ -126,11 +128,12 @@ __device__ __forceinline__ F3 normals32(uint64_t seed, unsigned long long step, 
 __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restrict__ vcell,
                             const int4* __restrict__ vlast, const int4* __restrict__ vnext,
                             const int4* __restrict__ vrpos, const int4* __restrict__ vnbr,
-                            double2* __restrict__ corner, int Wc, int nV, float R, int t1test, float t1Threshold,
-                            T1Scratch t1) {
+                            double2* __restrict__ corner, int Wc, int nV, const double* __restrict__ repR,
+                            int t1test, float t1Threshold, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const float4 p = pos[v];
+    const float R = (float)repR[rep_of(p)];
     const D3 pd = ld3(pos, v);
     const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
 #pragma unroll
@@ -158,29 +161,37 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
 __global__ void k32_force(Args32 A, int nV, float4* __restrict__ force) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
-    const F3 f = vertex_force32(A, v);
+    const F3 f = vertex_force32(A, v, (float)A.repR[rep_of(A.pos[v])]);
     force[v] = make_float4(f.x, f.y, f.z, 0.f);
 }
 
+// Noise amplitude: `repNp[replica]` for a batch of replicas, else `np`.
 template <int kNoise>
 __global__ void k32_force_bd(Args32 A, int nV, float4* __restrict__ force, float4* __restrict__ posNext,
                              const double* __restrict__ noise, uint64_t seed,
-                             const unsigned long long* __restrict__ stepCounter, float np, float fp) {
+                             const unsigned long long* __restrict__ stepCounter, float np,
+                             const float* __restrict__ repNp, float fp) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
-    const F3 f = vertex_force32(A, v);
+    const float4 p = A.pos[v];
+    const int rep = rep_of(p);
+    const double R = A.repR[rep];
+    const F3 f = vertex_force32(A, v, (float)R);
     force[v] = make_float4(f.x, f.y, f.z, 0.f);
     F3 xi;
     if (kNoise == SVM_NOISE_BUFFER) xi = F3{(float)noise[3 * v], (float)noise[3 * v + 1], (float)noise[3 * v + 2]};
     else xi = normals32(seed, *stepCounter, v);
-    posNext[v] = move_fp64(A.pos[v], np * xi + fp * f, A.R);
+    const float a = repNp ? repNp[rep] : np;
+    posNext[v] = move_fp64(p, a * xi + fp * f, R);
 }
 
-__global__ void k32_move(float4* __restrict__ pos, const double* __restrict__ disp, double scale, int nV, double R) {
+__global__ void k32_move(float4* __restrict__ pos, const double* __restrict__ disp, double scale, int nV,
+                         const double* __restrict__ repR) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const F3 d{(float)(scale * disp[3 * v]), (float)(scale * disp[3 * v + 1]), (float)(scale * disp[3 * v + 2])};
-    pos[v] = move_fp64(pos[v], d, R);
+    const float4 p = pos[v];
+    pos[v] = move_fp64(p, d, repR[rep_of(p)]);
 }
 
 __global__ void k_d4_to_f4(const double4_32a* __restrict__ in, float4* __restrict__ out, int n) {
@@ -193,7 +204,7 @@ __global__ void k_f4_to_d4(const float4* __restrict__ in, double4_32a* __restric
 }
 __global__ void k_aos_to_f4(const double* __restrict__ in, float4* __restrict__ out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) st3(out, i, D3{in[3 * i], in[3 * i + 1], in[3 * i + 2]});
+    if (i < n) st3_keep(out, i, D3{in[3 * i], in[3 * i + 1], in[3 * i + 2]});
 }
 __global__ void k_f4_to_aos(const float4* __restrict__ in, double* __restrict__ out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -203,7 +214,7 @@ __global__ void k_f4_to_aos(const float4* __restrict__ in, double* __restrict__ 
 Args32 args32(svm_model* m, int buf) {
     Args32 A;
     A.pos = m->pos32[buf]; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext; A.cellPos = m->cellPos32;
-    A.ap = m->ap; A.pref = m->pref; A.Kr = (float)m->Kr; A.R = (float)m->R;
+    A.ap = m->ap; A.pref = m->pref; A.repR = m->repR; A.Kr = (float)m->Kr;
     return A;
 }
 
@@ -212,9 +223,10 @@ Args32 args32(svm_model* m, int buf) {
 namespace svm {
 
 int mixed_launch_corners(svm_model* m, bool t1test) {
-    k32_corners<<<blocksFor(m->nVertices), kB, 0, m->stream>>>(m->pos32[m->cur], m->vcell, m->vlast, m->vnext, m->vrpos,
-                                                               m->vnbr, m->corner, m->Wc, m->nVertices, (float)m->R,
-                                                               t1test ? 1 : 0, (float)m->t1Threshold, m->t1);
+    const int bs = m->blkCorners;
+    k32_corners<<<(m->nVertices + bs - 1) / bs, bs, 0, m->stream>>>(m->pos32[m->cur], m->vcell, m->vlast, m->vnext,
+                                                                  m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+                                                                  m->repR, t1test ? 1 : 0, (float)m->t1Threshold, m->t1);
     return check_launch();
 }
 
@@ -226,17 +238,21 @@ int mixed_launch_force(svm_model* m) {
 int mixed_launch_force_bd(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise,
                           uint64_t seed, int nxt) {
     const double fp = dt * mu, np = sqrt(2.0 * fp * T);
+    const float* repNp = m->nRep > 1 ? m->repNp : nullptr;
+    const int bs = m->blkForce, nb = (m->nVertices + bs - 1) / bs;
     if (noiseMode == SVM_NOISE_BUFFER)
-        k32_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kB, 0, m->stream>>>(
-            args32(m, m->cur), m->nVertices, m->force32, m->pos32[nxt], noise, seed, m->stepCounter, (float)np, (float)fp);
+        k32_force_bd<SVM_NOISE_BUFFER><<<nb, bs, 0, m->stream>>>(args32(m, m->cur), m->nVertices, m->force32,
+                                                                m->pos32[nxt], noise, seed, m->stepCounter, (float)np,
+                                                                repNp, (float)fp);
     else
-        k32_force_bd<SVM_NOISE_PHILOX><<<blocksFor(m->nVertices), kB, 0, m->stream>>>(
-            args32(m, m->cur), m->nVertices, m->force32, m->pos32[nxt], noise, seed, m->stepCounter, (float)np, (float)fp);
+        k32_force_bd<SVM_NOISE_PHILOX><<<nb, bs, 0, m->stream>>>(args32(m, m->cur), m->nVertices, m->force32,
+                                                                m->pos32[nxt], noise, seed, m->stepCounter, (float)np,
+                                                                repNp, (float)fp);
     return check_launch();
 }
 
 int mixed_launch_move(svm_model* m, const double* disp, double scale) {
-    k32_move<<<blocksFor(m->nVertices), kB, 0, m->stream>>>(m->pos32[m->cur], disp, scale, m->nVertices, m->R);
+    k32_move<<<blocksFor(m->nVertices), kB, 0, m->stream>>>(m->pos32[m->cur], disp, scale, m->nVertices, m->repR);
     return check_launch();
 }
 
@@ -254,6 +270,7 @@ int mixed_download(svm_model* m, const float4* src, int n, double* deviceAos) {
 
 extern "C" int svm_model_set_precision(svm_model* m, int precision) {
     if (!m || (precision != SVM_PRECISION_FP64 && precision != SVM_PRECISION_MIXED)) return SVM_ERR_ARG;
+    if (m->nRep > 1 && precision != SVM_PRECISION_MIXED) return SVM_ERR_ARG;  // batches run mixed
     if (precision == m->precision) return SVM_OK;
     const size_t nV = m->nVertices, nC = m->nCells;
     if (precision == SVM_PRECISION_MIXED) {

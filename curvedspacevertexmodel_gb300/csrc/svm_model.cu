@@ -135,17 +135,21 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
 // in the CPU's order (ring positions n-2, n-1, 0, ..., n-3), area = (sum - (n-2) pi) wrapped
 // by floor(area / pi), times R^2 (sphericalVertexModel.cpp:228-303).  The last block to finish
 // totals the areas and raises the fallback flag when |sum A - 4 pi R^2| > 1e-6 (304-310).
+//
+// Replicas (mixed form, repR non-null): the radius is the replica's, read through the first ring
+// vertex; with `ticket` null the area check is left to k_rep_check (per replica).
 template <class PT>
 __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring,
                         const int* __restrict__ ringCount, const double2* __restrict__ corner, int Wc, int nC,
-                        double R, PT* __restrict__ cellPos, double4_32a* __restrict__ cellSph,
-                        double2* __restrict__ ap, double* __restrict__ partials, unsigned* __restrict__ ticket,
-                        double* __restrict__ scalars, int* __restrict__ fallbackFlag) {
+                        double R0, const double* __restrict__ repR, PT* __restrict__ cellPos,
+                        double4_32a* __restrict__ cellSph, double2* __restrict__ ap, double* __restrict__ partials,
+                        unsigned* __restrict__ ticket, double* __restrict__ scalars, int* __restrict__ fallbackFlag) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double area = 0.0;
     if (c < nC) {
         const int n = ringCount[c];
         const int* rg = ring + (long)c * Wc;
+        const double R = repR ? repR[rep_of(pos[rg[0]])] : R0;
         D3 cp{0.0, 0.0, 0.0};
         for (int k = 0; k < n; ++k) cp = add3(cp, ld3(pos, rg[k]));
         cp = renorm(cp, R);
@@ -166,6 +170,8 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
         area = __dmul_rn(__dmul_rn(area, R), R);
         ap[c] = make_double2(area, per);
     }
+    if (!ticket) return;
+    const double R = R0;
     const double bs = block_sum(area);
     __shared__ bool amLast;
     if (threadIdx.x == 0) {
@@ -190,15 +196,20 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
 
 // recomputeAreasCPU (sphericalVertexModel.cpp:162-207): area as a sum of spherical triangles
 // (centroid, ring[k-1], ring[k]) starting from (ring[n-2], ring[n-1]).
+// Replicas (repFlag non-null): the flag and the radius are the cell's replica's.
 template <class PT>
 __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ ring,
                            const int* __restrict__ ringCount, const PT* __restrict__ cellPos, int Wc, int nC,
-                           double R, const int* __restrict__ fallbackFlag, double2* __restrict__ ap) {
-    if (*fallbackFlag == 0) return;
+                           double R0, const int* __restrict__ fallbackFlag, const int* __restrict__ repFlag,
+                           const double* __restrict__ repR, double2* __restrict__ ap) {
+    if (!repFlag && *fallbackFlag == 0) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nC) return;
     const int n = ringCount[c];
     const int* rg = ring + (long)c * Wc;
+    const int rep = rep_of(pos[rg[0]]);
+    if (repFlag && repFlag[rep] == 0) return;
+    const double R = repR ? repR[rep] : R0;
     const D3 cp = ld3(cellPos, c);
     D3 last = ld3(pos, rg[n - 2]), cur = ld3(pos, rg[n - 1]);
     double area = 0.0;
@@ -294,15 +305,15 @@ __global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__
 
 // Standalone T1 edge test (gpu_vm_test_edges_for_T1, sphericalVertexModel.cu:225-273).
 __global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __restrict__ pos32,
-                          const int4* __restrict__ vnbr, int nV, double R, double t1Threshold, double cosLo,
-                          double cosHi, T1Scratch t1) {
+                          const double* __restrict__ repR, const int4* __restrict__ vnbr, int nV, double R,
+                          double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const int4 nb = vnbr[v];
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int u = comp(nb, s);
-        const bool shortEdge = pos32 ? arc32(pos32[v], pos32[u], (float)R) < (float)t1Threshold
+        const bool shortEdge = pos32 ? arc32(pos32[v], pos32[u], (float)repR[rep_of(pos32[v])]) < (float)t1Threshold
                                      : shorter_than(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi);
         if (v < u && shortEdge) {
             const int q = 3 * v + s;
@@ -317,6 +328,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __r
 struct ApplyArgs {
     double cosLo, cosHi;   // shorter_than bracket of cos(t1Threshold / R)
     float4* pos32;         // FP32 positions in the mixed-precision form, else null
+    const double* repR;    // per-replica radius (mixed form)
     double4_32a* pos;
     double4_32a* vsph;
     int4 *vcell, *vnbr, *vlast, *vnext, *vrpos;
@@ -333,9 +345,11 @@ struct ApplyArgs {
 __device__ __forceinline__ int& compRef(int4* a, int v, int s) { return reinterpret_cast<int*>(a + v)[s]; }
 __device__ __forceinline__ D3 apos(const ApplyArgs& A, int i) { return A.pos32 ? ld3(A.pos32, i) : ld3(A.pos, i); }
 __device__ __forceinline__ void apos_st(const ApplyArgs& A, int i, D3 v) {
-    if (A.pos32) st3(A.pos32, i, v);
+    if (A.pos32) st3_keep(A.pos32, i, v);
     else st3(A.pos, i, v);
 }
+// radius of the sphere vertex i lives on
+__device__ __forceinline__ double aR(const ApplyArgs& A, int i) { return A.pos32 ? A.repR[rep_of(A.pos32[i])] : A.R; }
 __device__ __forceinline__ double4_32a apos4(const ApplyArgs& A, int i) {
     const D3 p = apos(A, i);
     return make_double4_32a(p.x, p.y, p.z, 0.0);
@@ -447,8 +461,9 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
     const D3 diff{__dmul_rn(0.5, __dsub_rn(p1.x, p2.x)), __dmul_rn(0.5, __dsub_rn(p1.y, p2.y)), __dmul_rn(0.5, __dsub_rn(p1.z, p2.z))};
     p1 = D3{__dadd_rn(p1.x, diff.x), __dadd_rn(p1.y, diff.y), __dadd_rn(p1.z, diff.z)};
     p2 = D3{__dsub_rn(p2.x, diff.x), __dsub_rn(p2.y, diff.y), __dsub_rn(p2.z, diff.z)};
-    apos_st(A, v1, renorm_exact(p1, A.R));
-    apos_st(A, v2, renorm_exact(p2, A.R));
+    const double R = aR(A, v1);
+    apos_st(A, v1, renorm_exact(p1, R));
+    apos_st(A, v2, renorm_exact(p2, R));
     for (int k = 0; k < 3; ++k) {
         if (compRef(A.vcell, v1, k) == cs.z) compRef(A.vcell, v1, k) = cs.w;
         if (compRef(A.vcell, v2, k) == cs.x) compRef(A.vcell, v2, k) = cs.y;
@@ -487,7 +502,7 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
         const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
         if (A.pos32) {
             A.corner[(long)cell * A.Wc + k] =
-                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)A.R), included_angle(pl, p, px));
+                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle(pl, p, px));
         } else {
             A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
             A.vsph[u] = sph_coords(p);
@@ -512,7 +527,7 @@ __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
     const int v = q / 3, s = q - 3 * (q / 3);
     const int u = compRef(A.vnbr, v, s);
     if (!(v < u)) return false;
-    if (A.pos32) return arc32(A.pos32[v], A.pos32[u], (float)A.R) < (float)A.t1Threshold;
+    if (A.pos32) return arc32(A.pos32[v], A.pos32[u], (float)aR(A, v)) < (float)A.t1Threshold;
     return shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi);
 }
 
@@ -917,6 +932,7 @@ static ForceArgs force_args(svm_model* m, int buf) {
 static ApplyArgs apply_args(svm_model* m, int bump) {
     ApplyArgs A;
     A.pos32 = m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr;
+    A.repR = m->repR;
     A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vnbr = m->vnbr; A.vlast = m->vlast;
     A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
@@ -929,7 +945,7 @@ int launch_corners(svm_model* m, bool t1test) {
     PhaseTimer pt(m, SVM_PHASE_CORNERS);
     if (m->precision == SVM_PRECISION_MIXED) {
         m->cornersValid = true;
-        return mixed_launch_corners(m, t1test);
+        return m->nRep > 1 ? batch_tuned_corners(m, t1test) : mixed_launch_corners(m, t1test);
     }
     double lo, hi;
     t1_bracket(m->t1Threshold, m->R, &lo, &hi);
@@ -940,27 +956,41 @@ int launch_corners(svm_model* m, bool t1test) {
     return check_launch();
 }
 
+static int launch_cells_batch(svm_model* m) {
+    const int bs = m->blkCells;
+    k_cells<float4><<<(m->nCells + bs - 1) / bs, bs, 0, m->stream>>>(
+        m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, m->repR, m->cellPos32, nullptr,
+        m->ap, nullptr, nullptr, nullptr, nullptr);
+    return check_launch();
+}
+
 static int launch_cells(svm_model* m) {
-    const int nb = blocksFor(m->nCells);
     const bool mixed = m->precision == SVM_PRECISION_MIXED;
+    const bool batch = m->nRep > 1;
     {
-        PhaseTimer pt(m, SVM_PHASE_CELLS, 1);
-        if (mixed)
-            k_cells<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc,
-                                                          m->nCells, m->R, m->cellPos32, nullptr, m->ap, m->partials,
-                                                          m->ticket, m->scalars, m->fallbackFlag);
-        else
-            k_cells<double4_32a><<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc,
-                                                               m->nCells, m->R, m->cellPos, m->cellSph, m->ap,
-                                                               m->partials, m->ticket, m->scalars, m->fallbackFlag);
+        PhaseTimer pt(m, SVM_PHASE_CELLS, batch ? 2 : 1);
+        if (batch) {
+            if (int rc = batch_tuned_cells(m, launch_cells_batch)) return rc;
+            if (int rc = launch_rep_check(m)) return rc;
+        } else if (mixed) {
+            k_cells<float4><<<blocksFor(m->nCells), kBlock, 0, m->stream>>>(
+                m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, m->repR, m->cellPos32,
+                nullptr, m->ap, m->partials, m->ticket, m->scalars, m->fallbackFlag);
+        } else {
+            k_cells<double4_32a><<<blocksFor(m->nCells), kBlock, 0, m->stream>>>(
+                m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, nullptr, m->cellPos,
+                m->cellSph, m->ap, m->partials, m->ticket, m->scalars, m->fallbackFlag);
+        }
     }
     PhaseTimer pt(m, SVM_PHASE_FALLBACK);
+    const int nb = blocksFor(m->nCells);
     if (mixed)
         k_fallback<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc,
-                                                         m->nCells, m->R, m->fallbackFlag, m->ap);
+                                                         m->nCells, m->R, m->fallbackFlag, batch ? m->repFlag : nullptr,
+                                                         m->repR, m->ap);
     else
         k_fallback<double4_32a><<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc,
-                                                              m->nCells, m->R, m->fallbackFlag, m->ap);
+                                                              m->nCells, m->R, m->fallbackFlag, nullptr, nullptr, m->ap);
     return check_launch();
 }
 
@@ -981,14 +1011,18 @@ int launch_t1_apply(svm_model* m, int bump) {
 
 // One fused Brownian timestep (see the file header).
 static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise, uint64_t seed) {
-    int rc = launch_geometry(m);
+    int rc = SVM_OK;
+    if (m->nRep > 1 && !capturing(m->stream) && (rc = update_rep_noise(m, dt, mu))) return rc;
+    rc = launch_geometry(m);
     if (rc) return rc;
     const double fp = dt * mu;
     const double np = sqrt(2.0 * fp * T);
     const int nxt = 1 - m->cur;
     {
     PhaseTimer pt(m, SVM_PHASE_FORCE);
-    if (m->precision == SVM_PRECISION_MIXED)
+    if (m->precision == SVM_PRECISION_MIXED && m->nRep > 1)
+        rc = batch_tuned_force_bd(m, T, dt, mu, noiseMode, noise, seed, nxt);
+    else if (m->precision == SVM_PRECISION_MIXED)
         rc = mixed_launch_force_bd(m, T, dt, mu, noiseMode, noise, seed, nxt);
     else if (noiseMode == SVM_NOISE_BUFFER)
         k_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
@@ -1089,10 +1123,18 @@ void svm_topology_free(svm_topology* t) { delete t; }
 
 int svm_model_create(int nCells, int nVertices, int Wc, double radius, void* stream, svm_model** out) {
     if (nCells < 4 || nVertices != 2 * nCells - 4 || Wc < 3 || Wc > 64 || !(radius > 0) || !out) return SVM_ERR_ARG;
+    return svm::model_alloc(nCells, nVertices, Wc, &radius, 1, stream, out);
+}
+
+}  // extern "C"
+
+// Allocation of a model (one sphere, or nRep replicas concatenated: replica r's radius radius[r]).
+int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, int nRep, void* stream,
+                     svm_model** out) {
     int ndev = 0;
     if (svm_device_count(&ndev) != SVM_OK) return SVM_ERR_NO_DEVICE;
     svm_model* m = new svm_model();
-    m->nCells = nCells; m->nVertices = nVertices; m->Wc = Wc; m->R = radius;
+    m->nCells = nCells; m->nVertices = nVertices; m->Wc = Wc; m->R = radius[0]; m->nRep = nRep;
     if (stream) { m->stream = (cudaStream_t)stream; }
     else {
         if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) { delete m; return SVM_ERR_CUDA; }
@@ -1153,7 +1195,14 @@ int svm_model_create(int nCells, int nVertices, int Wc, double radius, void* str
     alloc((void**)&m->t1.stats, 8 * sizeof(int));
     alloc((void**)&m->t1.flipCount, sizeof(int));
     alloc((void**)&m->t1.touched, (size_t)m->t1.touchedCap * sizeof(int));
+    alloc((void**)&m->repR, nRep * sizeof(double));
+    alloc((void**)&m->repNp, nRep * sizeof(float));
+    alloc((void**)&m->repCellOff, (nRep + 1) * sizeof(int));
+    alloc((void**)&m->repFlag, nRep * sizeof(int));
+    alloc((void**)&m->repScal, 3 * nRep * sizeof(double));
     if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
+    cudaMemcpy(m->repR, radius, nRep * sizeof(double), cudaMemcpyHostToDevice);
+    m->repT.assign(nRep, 0.0);
     cudaMemset(m->t1.resV, 0x7f, nV * sizeof(int));   // kResFree
     cudaMemset(m->t1.resC, 0x7f, nC * sizeof(int));
     cudaMemset(m->t1.comV, 0xff, nV * sizeof(int));   // -1
@@ -1165,18 +1214,23 @@ int svm_model_create(int nCells, int nVertices, int Wc, double radius, void* str
     return SVM_OK;
 }
 
+extern "C" {
+
 int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
+    for (svm_fire* F : m->fires) svm::fire_detach(F);
     void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
                     m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
-                    m->pos32[0], m->pos32[1], m->cellPos32, m->force32};
+                    m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->repR, m->repNp, m->repCellOff,
+                    m->repFlag, m->repScal};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
+    svm::batch_release(m);
     for (auto& v : m->profEvents) for (cudaEvent_t e : v) cudaEventDestroy(e);
     if (m->ownStream && m->stream) cudaStreamDestroy(m->stream);
     delete m;
@@ -1311,7 +1365,8 @@ int svm_model_enforce_topology(svm_model* m) {
     double lo, hi;
     svm::t1_bracket(m->t1Threshold, m->R, &lo, &hi);
     k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
-        m->pos[m->cur], m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr, m->vnbr, m->nVertices, m->R,
+        m->pos[m->cur], m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr, m->repR, m->vnbr,
+        m->nVertices, m->R,
         m->t1Threshold, lo, hi, m->t1);
     if (svm::check_launch()) return SVM_ERR_CUDA;
     // the patch of touched cells writes corners; all of them are recomputed before their next use
@@ -1516,7 +1571,16 @@ int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, c
 
 int svm_brownian_run(svm_model* m, double T, double dt, double mu, uint64_t seed, int nSteps) {
     if (!m || nSteps < 0) return SVM_ERR_ARG;
-    int rc = svm::launch_geometry(m);  // make corners valid outside the capture
+    int rc = svm::update_rep_noise(m, dt, mu);  // a batch's noise amplitudes, outside the capture
+    if (rc) return rc;
+    // while a batch's autotuner samples, steps run one by one with their kernels timed
+    while (nSteps > 0 && m->nRep > 1 && svm::batch_tuning(m)) {
+        if ((rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed))) return rc;
+        --nSteps;
+    }
+    if (nSteps == 0) return SVM_OK;
+    svm::batch_tuner_untimed(m, nSteps);
+    rc = svm::launch_geometry(m);  // make corners valid outside the capture
     if (rc) return rc;
     const bool reuse = m->bdGraph && m->bdT == T && m->bdDt == dt && m->bdMu == mu && m->bdSeed == seed &&
                        m->bdGraphCur == m->cur && m->bdGraphVersion == m->paramsVersion;

@@ -274,6 +274,112 @@ class sphericalVertexModel:
         call("svm_model_synchronize", self._h)
 
 
+class sphericalVertexModelBatch(sphericalVertexModel):
+    """Independent spheres (replicas) of uneven size in one model (svm_batch_* in include/svm.h):
+    every step of the batch is one set of launches over all replicas.  Replica r has nCells[r]
+    cells whose centres come from seeds[r] (random_cell_centres, the reference's recipe), radius
+    sqrt(nCells[r] / 4 pi), and its own P0 and temperature.  Runs the mixed-precision form.
+    State accessors of the base class return the concatenated arrays; `cellSlice(r)` and
+    `vertexSlice(r)` cut replica r out of them."""
+
+    def __init__(self, nCells, seeds, a0: float = 1.0, p0=3.8, ringCapacity: int = 16, stream=None,
+                 topologies=None):
+        nCells = [int(n) for n in nCells]
+        R = len(nCells)
+        if topologies is None:
+            topologies = [Topology(random_cell_centres(int(sd), n)) for n, sd in zip(nCells, seeds)]
+        self.topologies = topologies
+        self.nReplicas = R
+        self.radii = np.array([math.sqrt(n / (4.0 * PI)) for n in nCells])
+        self.radius = self.radii
+        self.replicaCells = np.array(nCells, dtype=np.int32)
+        self.replicaVertices = np.array([t.nVertices for t in topologies], dtype=np.int32)
+        self.cellOffsets = np.concatenate([[0], np.cumsum(self.replicaCells)]).astype(np.int64)
+        self.vertexOffsets = np.concatenate([[0], np.cumsum(self.replicaVertices)]).astype(np.int64)
+        self.nCells = int(self.cellOffsets[-1])
+        self.nVertices = int(self.vertexOffsets[-1])
+        cap = max(int(ringCapacity), max(t.maxRing for t in topologies) + 1)
+        self.ringCapacity = cap
+        h = C.c_void_p()
+        call("svm_batch_create", R, self.replicaCells, self.replicaVertices, cap, self.radii,
+             C.c_void_p(stream) if stream else None, C.byref(h))
+        self._h = h
+        self._precision = "mixed"
+        rings = np.full((self.nCells, cap), -1, dtype=np.int32)
+        pos = np.empty((self.nVertices, 3))
+        counts = np.empty(self.nCells, dtype=np.uint32)
+        vc = np.empty((self.nVertices, 3), dtype=np.int32)
+        vn = np.empty((self.nVertices, 3), dtype=np.int32)
+        for r, t in enumerate(topologies):
+            c0, c1 = self.cellOffsets[r], self.cellOffsets[r + 1]
+            v0, v1 = self.vertexOffsets[r], self.vertexOffsets[r + 1]
+            w = t.rings.shape[1]
+            rings[c0:c1, :w] = np.where(t.rings >= 0, t.rings + v0, -1)
+            counts[c0:c1] = t.ringCounts
+            pos[v0:v1] = t.vertexPositions
+            vc[v0:v1] = t.vertexCells + c0
+            vn[v0:v1] = t.vertexNeighbors + v0
+        call("svm_model_set_topology", h, pos.reshape(-1), rings.reshape(-1), cap, counts, vc.reshape(-1),
+             vn.reshape(-1))
+        self._restricted = False
+        self.t1Threshold = 0.1
+        call("svm_model_set_t1_threshold", h, 0.1)
+        self.setPreferredParameters(a0, p0)
+        self.setScalarModelParameter(1.0)
+        self.temperatures = np.zeros(R)
+        self.computeGeometry()
+
+    def cellSlice(self, r: int) -> slice:
+        return slice(int(self.cellOffsets[r]), int(self.cellOffsets[r + 1]))
+
+    def vertexSlice(self, r: int) -> slice:
+        return slice(int(self.vertexOffsets[r]), int(self.vertexOffsets[r + 1]))
+
+    def setPreferredParameters(self, a0, p0):
+        """A0 and P0: scalars, or one value per replica."""
+        a = np.broadcast_to(np.asarray(a0, dtype=np.float64), (self.nReplicas,))
+        p = np.broadcast_to(np.asarray(p0, dtype=np.float64), (self.nReplicas,))
+        pref = np.empty((self.nCells, 2))
+        pref[:, 0] = np.repeat(a, self.replicaCells)
+        pref[:, 1] = np.repeat(p, self.replicaCells)
+        self.setPreferredParameterArray(pref)
+
+    def setTemperatures(self, T):
+        self.temperatures = np.ascontiguousarray(np.broadcast_to(np.asarray(T, dtype=np.float64),
+                                                                 (self.nReplicas,)))
+        call("svm_batch_set_temperatures", self._h, self.temperatures)
+
+    def replicaEnergies(self) -> np.ndarray:
+        out = np.empty(self.nReplicas)
+        call("svm_batch_energies", self._h, out)
+        return out
+
+    def replicaAreaCheck(self):
+        """Per replica: total area, excess over 4 pi R^2, fallback taken (last geometry pass)."""
+        t, e, f = np.empty(self.nReplicas), np.empty(self.nReplicas), np.empty(self.nReplicas, dtype=np.int32)
+        call("svm_batch_area_check", self._h, t, e, f)
+        return t, e, f.astype(bool)
+
+    def autotune(self, lo: int = 64, hi: int = 1024, step: int = 64, nSamples: int = 3, period: int = 1000):
+        """Block sizes of the batch kernels picked by kernelTuner-style sampling (lo <= 0: off)."""
+        call("svm_batch_autotune", self._h, int(lo), int(hi), int(step), int(nSamples), int(period))
+
+    def blockSizes(self):
+        out = np.zeros(3, dtype=np.int32)
+        done = C.c_int()
+        call("svm_batch_block_sizes", self._h, out, C.byref(done))
+        return dict(corners=int(out[0]), cells=int(out[1]), force=int(out[2]), samplingComplete=bool(done.value))
+
+    @property
+    def precision(self) -> str:
+        return "mixed"
+
+    @precision.setter
+    def precision(self, p: str):
+        if p != "mixed":
+            raise ValueError("batches run the mixed-precision form")
+
+
 class brownianDynamics:
     """Overdamped Brownian updater (brownianDynamics.h:11-29)."""
 

@@ -208,6 +208,8 @@ typedef struct svm_fire svm_fire;
 int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, double dtInc, double dtDec,
                     double alphaDec, int nMin, double forceCutoff, double alphaMin, int maxIterations,
                     svm_fire** out);
+/* A minimizer may outlive its model: svm_model_destroy detaches it, after which minimize and
+ * state return SVM_ERR_ARG and destroy only frees it. */
 int svm_fire_destroy(svm_fire* f);
 /* Runs until the criterion drops to forceCutoff or maxIterations; returns the iterations done
  * by this call and the final value of the criterion. */
@@ -231,6 +233,52 @@ int svm_cell_list_compute(svm_cell_list* cl, const double* pointsDevice, int n);
  * [nside^3 * Nmax] (ascending point index, -1 past the count); synchronises. */
 int svm_cell_list_get(svm_cell_list* cl, int* nside, int* nmax, unsigned* counts, int* slots, long slotsCapacity);
 int svm_cell_list_bins(svm_cell_list* cl, int* binOfPoint);
+
+/* ---- batches of replicas -------------------------------------------------------------------
+ * No counterpart in the reference, which runs one sphere per process (its seed loops,
+ * minimization.cpp:98-132, run instances one after another).  A batch is one svm_model holding
+ * nReplicas independent spheres back to back: replica r has nCells[r] cells (cells
+ * [cellOff[r], cellOff[r+1])), nVertices[r] = 2 nCells[r] - 4 vertices (vertices
+ * [vertOff[r], vertOff[r+1])) and radius radius[r].  Every svm_model_* call applies to the whole
+ * batch; rings, vertex lists and per-cell arrays passed to them use global indices, and per-cell
+ * (A0, P0) (svm_model_set_preferred_array) sweeps P0 across replicas.  Batches run the
+ * mixed-precision form (switching to FP64 returns SVM_ERR_ARG).  A Brownian step (svm_brownian_step
+ * or _run) of a batch uses the per-replica temperatures of svm_batch_set_temperatures (default 0;
+ * its T argument is ignored), the area check is per replica, and each replica's T1 flips are the
+ * ones the single-sphere loop would make. */
+int svm_batch_create(int nReplicas, const int* nCells, const int* nVertices, int ringCapacity, const double* radius,
+                     void* stream, svm_model** out);
+int svm_batch_replicas(svm_model* m, int* nReplicas);
+/* cellOffsets, vertexOffsets: nReplicas + 1 ints each (either may be NULL). */
+int svm_batch_offsets(svm_model* m, int* cellOffsets, int* vertexOffsets);
+int svm_batch_set_temperatures(svm_model* m, const double* temperatures);
+/* Per-replica energy sum_c Kr (A - A0)^2 + (P - P0)^2 of the current geometry. */
+int svm_batch_energies(svm_model* m, double* energies);
+/* Per-replica total area, excess over 4 pi R^2 and fallback flag of the last geometry. */
+int svm_batch_area_check(svm_model* m, double* totals, double* excess, int* fallbackTaken);
+/* Autotuning of the block size of the batch's corner, cell and force kernels, one KernelTuner
+ * each over block sizes lo, lo+step, ..., hi (multiples of 32, at most 1024): the reference's
+ * kernelTuner(start, end, step, nSamples, period) (src/utilities/kernelTuner.{h,cpp}).  While a
+ * tuner samples, svm_brownian_run runs steps one by one with those kernels timed; graph-replayed
+ * steps count as untimed calls toward the rescan period.  lo <= 0 turns tuning off (block 256). */
+int svm_batch_autotune(svm_model* m, int lo, int hi, int step, int nSamples, int period);
+/* Current block sizes (corners, cells, force) and whether the initial sampling is complete. */
+int svm_batch_block_sizes(svm_model* m, int* sizes3, int* samplingComplete);
+
+/* ---- kernel tuner ----------------------------------------------------------------------------
+ * kernelTuner (src/utilities/kernelTuner.{h,cpp}) over CUDA events on `stream`: bracket a launch
+ * with begin/end (end synchronises when the call is timed) and use svm_tuner_parameter for the
+ * next launch.  svm_tuner_record feeds a time measured by other means (one end() call). */
+typedef struct svm_tuner svm_tuner;
+int svm_tuner_create(int start, int end, int step, int nSamples, int period, void* stream, svm_tuner** out);
+int svm_tuner_destroy(svm_tuner* t);
+int svm_tuner_begin(svm_tuner* t);
+int svm_tuner_end(svm_tuner* t);
+int svm_tuner_record(svm_tuner* t, float milliseconds);
+int svm_tuner_parameter(svm_tuner* t, int* value);
+int svm_tuner_sampling_complete(svm_tuner* t, int* complete);
+/* candidates and their median times (printTimingData, kernelTuner.h:25-32) */
+int svm_tuner_timing_data(svm_tuner* t, int* candidates, float* medians, int capacity, int* count);
 
 #ifdef __cplusplus
 }

@@ -354,3 +354,16 @@ def test_t1_trajectory_n20k_matches_oracle(svm, oracle_mod):
     d = np.abs(m.returnPositions() - om.positions()).max(axis=1) / R
     q = {p: float(np.quantile(d, p)) for p in (0.5, 0.99, 0.999, 1.0)}
     assert q[0.5] < 1e-9 and q[0.99] < 1e-5 and q[1.0] < 1e-3, q
+
+
+def test_fire_outliving_its_model(svm, gold):
+    """A FIRE minimizer whose model was destroyed first reports an argument error instead of
+    touching the freed model; destroying it afterwards is safe."""
+    m = gpu_model(svm, gold)
+    fire = svm.energyMinimizerFIRE(m)
+    fire.setMaximumIterations(5)
+    fire.minimize()
+    m.close()
+    with pytest.raises(svm.SVMError):
+        fire.minimize()
+    del fire
