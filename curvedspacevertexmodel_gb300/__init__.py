@@ -12,10 +12,11 @@ from .model import (  # noqa: F401
     random_cell_centres,
     sphericalVertexModel,
     sphericalVertexModelBatch,
+    warmStartNetwork,
 )
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
     "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "sphericalVertexModel",
-    "sphericalVertexModelBatch",
+    "sphericalVertexModelBatch", "warmStartNetwork",
 ]

@@ -32,6 +32,7 @@ SVM_FIRE_RMS_OVER_N = 0
 SVM_FIRE_MAX_FORCE = 1
 SVM_PRECISION_FP64 = 0
 SVM_PRECISION_MIXED = 1
+SVM_PRECISION_FP64_VECTOR = 2
 
 def _nullable(ptr):
     """An ndpointer type that also accepts None (NULL) for optional outputs."""
@@ -104,6 +105,7 @@ SIGNATURES = {
     "svm_fire_destroy": (i32, [vp]),
     "svm_fire_minimize": (i32, [vp, i32, C.POINTER(i32), C.POINTER(f64)]),
     "svm_fire_state": (i32, [vp, dp]),
+    "svm_fire_set_max_iterations": (i32, [vp, i32]),
     "svm_cell_list_create": (i32, [f64, f64, i32, i32, vp, pvp]),
     "svm_cell_list_destroy": (i32, [vp]),
     "svm_cell_list_compute_model": (i32, [vp, vp]),
@@ -126,6 +128,17 @@ SIGNATURES = {
     "svm_tuner_parameter": (i32, [vp, C.POINTER(i32)]),
     "svm_tuner_sampling_complete": (i32, [vp, C.POINTER(i32)]),
     "svm_tuner_timing_data": (i32, [vp, ip, fp, i32, C.POINTER(i32)]),
+    "svm_mlp_create": (i32, [C.c_uint, vp, pvp]),
+    "svm_mlp_destroy": (i32, [vp]),
+    "svm_mlp_parameter_count": (i32, [C.POINTER(i32)]),
+    "svm_mlp_set_weights": (i32, [vp, fp]),
+    "svm_mlp_get_weights": (i32, [vp, fp]),
+    "svm_mlp_set_output_scale": (i32, [vp, f64]),
+    "svm_mlp_features": (i32, [vp, vp, vp]),
+    "svm_mlp_gradient": (i32, [vp, vp, vp, i32, fp, C.POINTER(f64)]),
+    "svm_mlp_train": (i32, [vp, vp, vp, vp, i32, i32, C.c_float, C.POINTER(f64)]),
+    "svm_mlp_predict": (i32, [vp, vp, i32, vp]),
+    "svm_mlp_warm_start": (i32, [vp, vp]),
 }
 
 

@@ -184,6 +184,7 @@ ForceArgs fargs(svm_model* m) {
     ForceArgs A;
     A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
     A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
+    A.vec = m->precision == SVM_PRECISION_FP64_VECTOR ? 1 : 0;
     return A;
 }
 
@@ -259,7 +260,7 @@ int svm_fire_destroy(svm_fire* F) {
 int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value) {
     if (!F || !F->m) return SVM_ERR_ARG;
     svm_model* m = F->m;
-    if (m->precision != SVM_PRECISION_FP64) return SVM_ERR_ARG;  // FIRE runs in the FP64 form
+    if (m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;  // FIRE runs in the FP64 forms
     FireState S;
     if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
         cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
@@ -307,6 +308,19 @@ int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value
     F->h = S;
     if (iterations) *iterations = S.iterations - it0;
     if (value) *value = criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
+    return SVM_OK;
+}
+
+int svm_fire_set_max_iterations(svm_fire* F, int maxIterations) {
+    if (!F || !F->m || maxIterations < 0) return SVM_ERR_ARG;
+    svm_model* m = F->m;
+    FireState S;
+    if (cudaMemcpyAsync(&S, F->d, sizeof(FireState), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    S.maxIterations = maxIterations;
+    F->h.maxIterations = maxIterations;
+    if (cudaMemcpyAsync(F->d, &S, sizeof(FireState), cudaMemcpyHostToDevice, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
     return SVM_OK;
 }
 

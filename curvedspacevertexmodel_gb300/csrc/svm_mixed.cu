@@ -269,11 +269,12 @@ int mixed_download(svm_model* m, const float4* src, int n, double* deviceAos) {
 }  // namespace svm
 
 extern "C" int svm_model_set_precision(svm_model* m, int precision) {
-    if (!m || (precision != SVM_PRECISION_FP64 && precision != SVM_PRECISION_MIXED)) return SVM_ERR_ARG;
+    if (!m || precision < SVM_PRECISION_FP64 || precision > SVM_PRECISION_FP64_VECTOR) return SVM_ERR_ARG;
     if (m->nRep > 1 && precision != SVM_PRECISION_MIXED) return SVM_ERR_ARG;  // batches run mixed
     if (precision == m->precision) return SVM_OK;
+    const bool toMixed = precision == SVM_PRECISION_MIXED, fromMixed = m->precision == SVM_PRECISION_MIXED;
     const size_t nV = m->nVertices, nC = m->nCells;
-    if (precision == SVM_PRECISION_MIXED) {
+    if (toMixed) {
         if (!m->pos32[0]) {
             bool ok = cudaMalloc(&m->pos32[0], nV * sizeof(float4)) == cudaSuccess &&
                       cudaMalloc(&m->pos32[1], nV * sizeof(float4)) == cudaSuccess &&
@@ -283,7 +284,7 @@ extern "C" int svm_model_set_precision(svm_model* m, int precision) {
             cudaMemsetAsync(m->force32, 0, nV * sizeof(float4), m->stream);
         }
         k_d4_to_f4<<<blocksFor(nV), kB, 0, m->stream>>>(m->pos[m->cur], m->pos32[m->cur], (int)nV);
-    } else {
+    } else if (fromMixed) {
         k_f4_to_d4<<<blocksFor(nV), kB, 0, m->stream>>>(m->pos32[m->cur], m->pos[m->cur], (int)nV);
     }
     if (svm::check_launch()) return SVM_ERR_CUDA;

@@ -927,6 +927,7 @@ static ForceArgs force_args(svm_model* m, int buf) {
     ForceArgs A;
     A.pos = m->pos[buf]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
     A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
+    A.vec = m->precision == SVM_PRECISION_FP64_VECTOR ? 1 : 0;
     return A;
 }
 static ApplyArgs apply_args(svm_model* m, int bump) {

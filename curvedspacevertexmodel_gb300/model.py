@@ -152,13 +152,16 @@ class sphericalVertexModel:
 
     @property
     def precision(self) -> str:
-        """'fp64' (every quantity in FP64) or 'mixed' (FP32 positions, forces and integration;
-        FP64 included angles, areas, energy and renormalisation)."""
+        """'fp64' (every quantity in FP64, the reference's formulas), 'mixed' (FP32 positions,
+        forces and integration; FP64 included angles, areas, energy and renormalisation) or
+        'fp64_vector' (FP64 with the forces as the exact gradient in vector form, for tight
+        minimisation)."""
         return getattr(self, "_precision", "fp64")
 
     @precision.setter
     def precision(self, p: str):
-        code = {"fp64": _lib.SVM_PRECISION_FP64, "mixed": _lib.SVM_PRECISION_MIXED}[p]
+        code = {"fp64": _lib.SVM_PRECISION_FP64, "mixed": _lib.SVM_PRECISION_MIXED,
+                "fp64_vector": _lib.SVM_PRECISION_FP64_VECTOR}[p]
         call("svm_model_set_precision", self._h, code)
         self._precision = p
 
@@ -443,8 +446,10 @@ class energyMinimizerFIRE:
         self._reset()
 
     def setMaximumIterations(self, n: int):
+        """Cap on the total iteration count; an existing minimizer keeps its dt, alpha and counters."""
         self.maxIterations = int(n)
-        self._reset()
+        if self._h:
+            call("svm_fire_set_max_iterations", self._h, self.maxIterations)
 
     def setForceCutoff(self, fc: float):
         self.params["forceCutoff"] = float(fc)
@@ -490,6 +495,89 @@ class energyMinimizerFIRE:
 
     def __del__(self):
         self._reset()
+
+
+class warmStartNetwork:
+    """The per-vertex MLP of the learned FIRE warm start (svm_mlp_* in include/svm.h).  Device
+    arrays are torch CUDA tensors (used for their memory only); every computation runs in libsvm's
+    kernels."""
+
+    def __init__(self, seed: int = 1, stream=None):
+        h = C.c_void_p()
+        call("svm_mlp_create", int(seed), C.c_void_p(stream) if stream else None, C.byref(h))
+        self._h = h
+        n = C.c_int()
+        call("svm_mlp_parameter_count", C.byref(n))
+        self.parameterCount = n.value
+        self.outputScale = 1.0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().svm_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def weights(self) -> np.ndarray:
+        w = np.empty(self.parameterCount, dtype=np.float32)
+        call("svm_mlp_get_weights", self._h, w)
+        return w
+
+    def setWeights(self, w: np.ndarray):
+        call("svm_mlp_set_weights", self._h, np.ascontiguousarray(w, dtype=np.float32))
+
+    def setOutputScale(self, scale: float):
+        self.outputScale = float(scale)
+        call("svm_mlp_set_output_scale", self._h, self.outputScale)
+
+    @staticmethod
+    def features(model: sphericalVertexModel, frames: bool = False):
+        """Features [nV, 24] (and frames [nV, 6]) of an FP64 model's current state after
+        computeForces."""
+        import torch
+        X = torch.empty((model.nVertices, 24), dtype=torch.float32, device="cuda")
+        F = torch.empty((model.nVertices, 6), dtype=torch.float64, device="cuda") if frames else None
+        torch.cuda.synchronize()
+        call("svm_mlp_features", model.handle, C.c_void_p(X.data_ptr()),
+             C.c_void_p(F.data_ptr()) if F is not None else None)
+        return (X, F) if frames else X
+
+    def gradient(self, X, T):
+        """(mean squared error, gradient) over the samples X [n, 24], T [n, 2] (CUDA tensors)."""
+        import torch
+        torch.cuda.synchronize()
+        g = np.empty(self.parameterCount, dtype=np.float32)
+        loss = C.c_double()
+        call("svm_mlp_gradient", self._h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()), int(X.shape[0]), g,
+             C.byref(loss))
+        return loss.value, g
+
+    def train(self, X, T, epochs: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0):
+        """Adam epochs over (X, T) in a fresh seeded permutation each epoch; mean losses."""
+        import torch
+        rng = np.random.default_rng(seed)
+        n = int(X.shape[0])
+        losses = []
+        for _ in range(epochs):
+            order = torch.from_numpy(rng.permutation(n).astype(np.int32)).cuda()
+            torch.cuda.synchronize()
+            loss = C.c_double()
+            call("svm_mlp_train", self._h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()),
+                 C.c_void_p(order.data_ptr()), n, int(batch), C.c_float(lr), C.byref(loss))
+            losses.append(loss.value)
+        return losses
+
+    def predict(self, X):
+        import torch
+        Y = torch.empty((X.shape[0], 2), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        call("svm_mlp_predict", self._h, C.c_void_p(X.data_ptr()), int(X.shape[0]), C.c_void_p(Y.data_ptr()))
+        return Y
+
+    def warmStart(self, model: sphericalVertexModel):
+        """Moves every vertex of an FP64 model by the network's predicted displacement."""
+        call("svm_mlp_warm_start", self._h, model.handle)
 
 
 class Simulation:

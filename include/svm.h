@@ -89,10 +89,17 @@ int svm_model_destroy(svm_model* m);
  *   SVM_PRECISION_FP64  - the plain form: every quantity in FP64 (default);
  *   SVM_PRECISION_MIXED - FP32 positions, forces and integration, with the included angles and
  *                         the spherical-excess areas, the energy accumulation and the
- *                         renormalisation onto the sphere in FP64.
- * Switching converts the current positions.  FIRE runs in the FP64 form only. */
+ *                         renormalisation onto the sphere in FP64;
+ *   SVM_PRECISION_FP64_VECTOR - FP64 throughout, with the forces evaluated as the exact energy
+ *                         gradient in vectors of position differences instead of the reference's
+ *                         closed forms in spherical coordinates (sphericalDomain.h:248-411), whose
+ *                         triangle term loses digits on nearly degenerate centroid-fan triangles
+ *                         and floors max|F| near 1e-8 at N = 20k.  For minimisation to tight force
+ *                         tolerances.
+ * Switching converts the current positions.  FIRE runs in the two FP64 forms. */
 #define SVM_PRECISION_FP64 0
 #define SVM_PRECISION_MIXED 1
+#define SVM_PRECISION_FP64_VECTOR 2
 int svm_model_set_precision(svm_model* m, int precision);
 
 /* Upload topology and positions (host arrays, reference layouts). */
@@ -214,6 +221,9 @@ int svm_fire_destroy(svm_fire* f);
 /* Runs until the criterion drops to forceCutoff or maxIterations; returns the iterations done
  * by this call and the final value of the criterion. */
 int svm_fire_minimize(svm_fire* f, int criterion, int* iterations, double* criterionValue);
+/* setMaximumIterations (energyMinimizerFIRE.h:37): the cap on the total iteration count, keeping
+ * dt, alpha and the counters (a later minimize continues from there). */
+int svm_fire_set_max_iterations(svm_fire* f, int maxIterations);
 /* state: dt, alpha, power, rms_over_n, max_force, n_since, iterations (7 doubles). */
 int svm_fire_state(svm_fire* f, double* state7);
 
@@ -279,6 +289,35 @@ int svm_tuner_parameter(svm_tuner* t, int* value);
 int svm_tuner_sampling_complete(svm_tuner* t, int* complete);
 /* candidates and their median times (printTimingData, kernelTuner.h:25-32) */
 int svm_tuner_timing_data(svm_tuner* t, int* candidates, float* medians, int capacity, int* count);
+
+/* ---- learned warm start for FIRE ------------------------------------------------------------
+ * No counterpart in the reference.  A per-vertex MLP 24 -> 64 -> 64 -> 2 (ReLU, BF16 weights,
+ * FP32 accumulation) reads the local tangent-frame geometry of a vertex (offsets to its three
+ * neighbours and three cell centroids, the cells' A - A0, P - P0 and ring sizes, the force) and
+ * predicts its displacement to the relaxed state in that frame.  Weights: FP32 master copy of
+ * svm_mlp_parameter_count floats (W1[64][24], b1, W2[64][64], b2, W3[2][64], b3), Adam on the
+ * master copy, forward on its BF16 rounding. */
+typedef struct svm_mlp svm_mlp;
+int svm_mlp_create(unsigned seed, void* stream, svm_mlp** out);
+int svm_mlp_destroy(svm_mlp* mlp);
+int svm_mlp_parameter_count(int* count);
+int svm_mlp_set_weights(svm_mlp* mlp, const float* weights);   /* host; resets Adam */
+int svm_mlp_get_weights(svm_mlp* mlp, float* weights);         /* host */
+/* multiplies the network output into a displacement (the training targets' unit) */
+int svm_mlp_set_output_scale(svm_mlp* mlp, double scale);
+/* Features of every vertex of an FP64 model after geometry and forces: DEVICE float[24 nV], and
+ * optionally the frames (e1, e2) as DEVICE double[6 nV]. */
+int svm_mlp_features(svm_model* m, float* featuresDevice, double* framesDevice);
+/* Gradient of mean_i |y_i - t_i|^2 over n samples (DEVICE X[24 n], T[2 n]) into HOST grad, and
+ * the loss. */
+int svm_mlp_gradient(svm_mlp* mlp, const float* X, const float* T, int n, float* grad, double* loss);
+/* One epoch: Adam steps over mini-batches of `batch` samples taken in the DEVICE order[n]. */
+int svm_mlp_train(svm_mlp* mlp, const float* X, const float* T, const int* order, int n, int batch,
+                  float learningRate, double* meanLoss);
+int svm_mlp_predict(svm_mlp* mlp, const float* X, int n, float* Y);   /* DEVICE arrays */
+/* Fused inference on an FP64 model: geometry and forces, then per vertex features -> network ->
+ * move by outputScale * (y0 e1 + y1 e2) onto the sphere (all vertices from the same state). */
+int svm_mlp_warm_start(svm_mlp* mlp, svm_model* m);
 
 #ifdef __cplusplus
 }

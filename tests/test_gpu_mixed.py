@@ -229,3 +229,45 @@ def test_fire_rejects_mixed(svm):
     fire.setMaximumIterations(10)
     with pytest.raises(svm.SVMError):
         fire.minimize()
+
+
+def test_fp64_vector_form_forces(svm, state20k):
+    """The FP64 vector-form force equals the host FP64 evaluation of the same formulas to rounding,
+    and the reference-formula force away from its ill-conditioned triangles."""
+    m, _, pos = state20k
+    m.precision = "fp64"
+    m.setPositions(pos)
+    m.computeForces()
+    f_ref = m.returnForces()
+    m.precision = "fp64_vector"
+    m.computeForces()
+    f_vec, ap, cp = m.returnForces(), m.areaPerimeter(), m.cellPositions()
+    m.precision = "fp64"
+    rings, counts = m.rings()
+    fhost = vector_forces(pos, rings, counts, ap, np.tile([1.0, 3.8], (m.nCells, 1)), cp, m.radius, m.Kr)
+    fmax = np.max(np.linalg.norm(f_ref, axis=1))
+    assert np.max(np.linalg.norm(f_vec - fhost, axis=1)) < 1e-12 * fmax
+    # the reference's closed forms divide by 1 - s^2 and by a cancelled Gram determinant: at
+    # N = 20k their FP64 error is ~1e-8 of the largest force at the 99th percentile
+    err = np.linalg.norm(f_vec - f_ref, axis=1) / fmax
+    print(f"fp64 vector vs reference formulas: median {np.median(err):.2e} q99 {np.quantile(err, 0.99):.2e} "
+          f"max {err.max():.2e}")
+    assert np.quantile(err, 0.99) < 1e-7
+    assert np.median(err) < 1e-8
+
+
+def test_fire_fp64_vector_reaches_tight_tolerance(svm):
+    """FIRE with the vector-form forces converges to max|F| < 1e-9 (N = 2000, P0 = 3.6, T1 on)."""
+    from curvedspacevertexmodel_gb300 import _lib
+    m, _ = stabilised(svm, 2000, steps=300)
+    m.setPreferredParameters(1.0, 3.6)
+    m.precision = "fp64_vector"
+    fire = svm.energyMinimizerFIRE(m)
+    fire.setFIREParameters(0.01, 0.1, 0.1, 1.1, 0.5, 0.9, 5, 1e-9, 0.0)
+    fire.setCriterion(_lib.SVM_FIRE_MAX_FORCE)
+    fire.setMaximumIterations(200000)
+    fire.minimize()
+    st = fire.state()
+    assert st["max_force"] < 1e-9
+    m.computeForces()
+    assert np.max(np.linalg.norm(m.returnForces(), axis=1)) < 1e-9
