@@ -47,6 +47,7 @@ PARAMS = dict(a0=1.0, p0=3.8, kr=1.0, T=0.01, mu=1.0, dt=0.01, t1=0.04)
 SEED = 1137
 BD_SEED = 4242
 BATCH_SEED = 5150
+FIRE_SEED = 9100
 WORKLOAD = ("spherical vertex model, overdamped Brownian step, FP64 plain form, N=100000 cells "
             "(199996 vertices), A0=1 P0=3.8 KA=KP=1 T=0.01 mu=1 dt=0.01 T1 threshold 0.04, "
             "seeded Voronoi start")
@@ -279,6 +280,7 @@ def run_ours(args):
         cpu_state["vcells"], cpu_state["vnbrs"] = model.vertexCellNeighbors(), model.vertexNeighbors()
     mixed = None if args.no_mixed else time_mixed_form(args, model, bd, stream, flush, nv, nc)
     batched = None if args.no_batch else time_batched_replicas(args, rank)
+    fire = None if args.no_fire else time_fire(args, rank)
     if rank != 0:
         return
     # ---- roofline of the dominant kernel ----
@@ -325,8 +327,35 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "mixed_form": mixed,
         "batched_replicas": batched,
+        "fire_warm_start": fire,
     }
     print(json.dumps(out), flush=True)
+
+
+def time_fire(args, rank):
+    """FIRE to max|F| < 1e-9 at N = 20k cells, learned warm start against plain FIRE, on held-out
+    instances (P0 uniform in [3.6, 3.8], seeds not used in training).  Start states: stabilisation
+    then 500 Brownian steps at T = 0.01; FIRE dt0 0.01, alpha0 0.1, dtMax 0.1, finc 1.1, fdec 0.5,
+    alphaDec 0.9, NMin 5; FP64 vector-form forces; T1 on.  Wall time of each minimisation,
+    synchronised on both sides; the warm time includes the network's inference, the step-length
+    choice and any fallback."""
+    import numpy as np
+    from curvedspacevertexmodel_gb300 import warm_start as ws
+    net = ws.load(os.path.join(ROOT, "curvedspacevertexmodel_gb300", "data", "warm_start_n20k.npz"))
+    rng = np.random.default_rng(FIRE_SEED + rank)
+    rows = [ws.compare(net, 20000, float(p0), FIRE_SEED + 100 * rank + i)
+            for i, p0 in enumerate(rng.uniform(3.6, 3.8, args.fire_instances))]
+    net.close()
+    plain = sum(r["plain_s"] for r in rows)
+    warm = sum(r["warm_s"] for r in rows)
+    return {"metric": "FIRE wall time to max|F| < 1e-9, warm start / plain", "value": warm / plain,
+            "unit": "ratio (lower is better)", "plain_s": plain, "warm_s": warm,
+            "plain_ms_per_iteration": 1e3 * plain / sum(r["plain_iterations"] for r in rows),
+            "instances": [{k: r[k] for k in ("p0", "seed", "plain_s", "plain_iterations", "warm_s", "warm_iterations",
+                                             "fallback", "warm_step_length", "energy_start", "energy_after_warm_start",
+                                             "energy_per_cell_plain", "energy_per_cell_warm")} for r in rows],
+            "workload": "N=20000, P0 U[3.6, 3.8], start = stabilisation + 500 Brownian steps at T=0.01, "
+                        "FIRE dt0 0.01 alpha0 0.1 dtMax 0.1 finc 1.1 fdec 0.5, FP64 vector-form forces, T1 on"}
 
 
 def time_batched_replicas(args, rank):
@@ -522,6 +551,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form's secondary timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-replica secondary timing")
     ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--no-fire", action="store_true", help="skip the FIRE warm-start comparison")
+    ap.add_argument("--fire-instances", type=int, default=2)
     ap.add_argument("--ref-cores", type=int, default=0)
     ap.add_argument("--ref-stab", type=int, default=30, help="stabilisation steps of each reference replica")
     args = ap.parse_args()

@@ -276,6 +276,19 @@ class sphericalVertexModel:
     def synchronize(self):
         call("svm_model_synchronize", self._h)
 
+    def saveState(self) -> dict:
+        """Positions and connectivity (host copies) for loadState."""
+        rings, counts = self.rings()
+        return dict(pos=self.returnPositions(), rings=rings, counts=counts, vcells=self.vertexCellNeighbors(),
+                    vnbrs=self.vertexNeighbors())
+
+    def loadState(self, st: dict):
+        rings = np.ascontiguousarray(st["rings"], dtype=np.int32)
+        call("svm_model_set_topology", self._h, np.ascontiguousarray(st["pos"], dtype=np.float64).reshape(-1),
+             rings.reshape(-1), rings.shape[1], np.ascontiguousarray(st["counts"], dtype=np.uint32),
+             np.ascontiguousarray(st["vcells"], dtype=np.int32).reshape(-1),
+             np.ascontiguousarray(st["vnbrs"], dtype=np.int32).reshape(-1))
+
 
 class sphericalVertexModelBatch(sphericalVertexModel):
     """Independent spheres (replicas) of uneven size in one model (svm_batch_* in include/svm.h):
