@@ -59,6 +59,18 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def job_throughput(pg, local_seconds: float, units_per_step: int, steps: int, world: int):
+    """Whole-job throughput of `world` ranks that each processed units_per_step x steps units:
+    the slowest rank's time (max over ranks) and all units / that time."""
+    t = float(local_seconds)
+    if pg is not None:
+        import torch
+        x = torch.tensor([t], dtype=torch.float64)
+        pg.all_reduce(x, op=pg.ReduceOp.MAX)
+        t = float(x.item())
+    return t, world * units_per_step * steps / t
+
+
 # --------------------------------------------------------------------------------------------
 # clocks during the timed region
 class ClockSampler:
@@ -232,13 +244,9 @@ def run_ours(args):
     _lib.call("svm_model_profile_read", model.handle, ms, launches)
     t1stats = model.t1Stats()
     _lib.call("svm_model_profile", model.handle, 0)
-    total_ms = float(sum(step_ms))
-    if pg:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_s, value = job_throughput(pg, float(sum(step_ms)) / 1e3, nv, args.steps, world)
+    total_ms = 1e3 * total_s
     ms_per_step = total_ms / args.steps
-    value = world * nv * args.steps / (total_ms / 1e3)
 
     # warm-L2 reference point: K back-to-back steps in one captured run
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -263,12 +271,7 @@ def run_ours(args):
         _lib.call("svm_model_get_positions", model.handle, host_out)
         _lib.call("svm_model_compute_energy", model.handle, C.byref(energy))
         host_pos, host_out = host_out, host_pos
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * nv * args.steps / e2e_s
+    e2e_s, e2e_value = job_throughput(pg, time.perf_counter() - t0, nv, args.steps, world)
 
     status = model.deviceStatus()
     model.computeGeometry()
