@@ -13,6 +13,7 @@
 // Batches run the mixed-precision form.  Their per-element kernels (corners, cells, force) take
 // their block size from a KernelTuner each (the reference's kernelTuner, src/utilities/
 // kernelTuner.cpp) when autotuning is on; the result of a step does not depend on block sizes.
+#include <algorithm>
 #include <memory>
 #include "svm_internal.cuh"
 #include "svm_tuner.h"
@@ -73,12 +74,15 @@ __global__ void k_set_rep(float4* __restrict__ p0, float4* __restrict__ p1, cons
     }
 }
 
+// one tuner per kernel family, each over the block sizes lo, lo+step, ... up to the smaller of hi
+// and the largest block the kernel can launch with (its register use)
 struct BatchTuners {
     KernelTuner corners, cells, force;
     cudaEvent_t start = nullptr, stop = nullptr;
     BatchTuners(int lo, int hi, int step, int samples, int period)
-        : corners(lo, hi, step, samples, period), cells(lo, hi, step, samples, period),
-          force(lo, hi, step, samples, period) {}
+        : corners(lo, std::max(lo, std::min(hi, mixed_max_block_corners())), step, samples, period),
+          cells(lo, std::max(lo, std::min(hi, max_block_cells_batch())), step, samples, period),
+          force(lo, std::max(lo, std::min(hi, mixed_max_block_force())), step, samples, period) {}
     ~BatchTuners() {
         if (start) cudaEventDestroy(start);
         if (stop) cudaEventDestroy(stop);

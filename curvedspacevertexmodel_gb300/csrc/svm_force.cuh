@@ -75,6 +75,12 @@ __device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
     const D3 p = ld3(A.pos, v);
     const double4_32a sv = A.vsph[v];
     const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
+    // The ring predecessors (and successors) of v in its three cells are its three neighbours, so
+    // each neighbour's geodesic gradient serves two cells: evaluated once per neighbour, keyed by
+    // the neighbours' order in `lasts` (a successor is found among them).
+    D3 gG[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) gG[j] = from_basis(sv, grad_geodesic(sv, A.vsph[comp(lasts, j)]));
     D3 f{0.0, 0.0, 0.0};
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
@@ -87,10 +93,11 @@ __device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
         const double4_32a sl = A.vsph[L], sx = A.vsph[X];
         const double pp = 2.0 * dP;
         const double aa = 2.0 * A.Kr * dA;
+        const int jx = X == lasts.x ? 0 : (X == lasts.y ? 1 : (X == lasts.z ? 2 : -1));
         D3 fs{0.0, 0.0, 0.0}, t;
-        t = from_basis(sv, grad_geodesic(sv, sl));
+        t = gG[s];
         fs = sub3(fs, scl3(pp, t));
-        t = from_basis(sv, grad_geodesic(sv, sx));
+        t = jx >= 0 ? pick3(gG, jx) : from_basis(sv, grad_geodesic(sv, sx));
         fs = sub3(fs, scl3(pp, t));
         t = from_basis(sv, grad_triangle(sv, sl, sc, p, pl, cp, A.R));
         fs = sub3(fs, scl3(aa, t));

@@ -109,6 +109,22 @@ __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
     if (a < 0) a += 2. * kPI;
     return a;
 }
+// includedAngle(pl, p, px) from the cross products Cx = p x px and Cl = p x pl and their norms,
+// computed once per neighbour of p: cross(pl, p) = -(p x pl) exactly, the negations cancel exactly
+// in the dot product and the norms, and det(pl, p, px) = pl . (p x px) in the same operation
+// order, so the result is bitwise included_angle(pl, p, px).
+__device__ __forceinline__ double included_angle_pre(D3 Cx, D3 Cl, double nx, double nl, D3 pl) {
+    const double det = dot3(pl, Cx);
+    double a = acos(dot3(Cx, Cl) / (nx * nl));
+    if (det > 0) a = -a;
+    if (a < 0) a += 2. * kPI;
+    return a;
+}
+// element j of a three-element register array (selects, no local-memory indexing)
+template <class T>
+__device__ __forceinline__ T pick3(const T* a, int j) { return j == 0 ? a[0] : (j == 1 ? a[1] : a[2]); }
+// slot of vertex u among the three neighbour slots nb (-1 if absent)
+__device__ __forceinline__ int nbr_slot(int4 nb, int u) { return u == nb.x ? 0 : (u == nb.y ? 1 : (u == nb.z ? 2 : -1)); }
 // sphericalTriangleArea (sphericalDomain.h:135-166)
 __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
     D3 p1 = scl3(1.0 / sqrt(dot3(q1, q1)), q1), p2 = scl3(1.0 / sqrt(dot3(q2, q2)), q2),
@@ -246,6 +262,7 @@ struct svm_model {
     float4* pos32[2] = {nullptr, nullptr};
     float4* cellPos32 = nullptr;
     float4* force32 = nullptr;
+    float2* dap32 = nullptr;           // per cell (A - A0, P - P0) in FP32, written with the geometry
     // replicas (mixed form): per-replica radius, noise amplitude and reductions.  A single sphere
     // is one replica; vertex v of replica r has pos32[v].w = r, replica r owns cells
     // [repCellOff[r], repCellOff[r+1]) and vertices [repVertOff[r], repVertOff[r+1]).
@@ -318,6 +335,9 @@ int batch_tuned_cells(svm_model* m, int (*launch)(svm_model*));
 int batch_tuned_force_bd(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise,
                          uint64_t seed, int nxt);
 bool batch_tuning(svm_model* m);
+int mixed_max_block_corners();
+int mixed_max_block_force();
+int max_block_cells_batch();
 void batch_tuner_untimed(svm_model* m, int calls);
 // mixed-precision kernels (svm_mixed.cu)
 int mixed_launch_corners(svm_model* m, bool t1test);

@@ -14,6 +14,7 @@
 //     grad_v A = R P_a [ 2 (D (b x c) - N (beta + gamma)) / (N^2 + D^2) ].
 // The signed area matches the reference's gradient of the unsigned area times sign(det(v1, v2, v3))
 // (sphericalDomain.h:395-402).
+#include <algorithm>
 #include "svm_internal.cuh"
 
 namespace svm {
@@ -61,8 +62,7 @@ struct Args32 {
     const int4* vlast;
     const int4* vnext;
     const float4* cellPos;
-    const double2* ap;
-    const double2* pref;
+    const float2* dap;     // per cell (A - A0, P - P0)
     const double* repR;    // per-replica radius, indexed by pos[v].w
     float Kr;
 };
@@ -81,8 +81,8 @@ __device__ __forceinline__ F3 vertex_force32(const Args32& A, int v, float R) {
         const int c = comp(cells, s);
         const F3 dc = f3(A.cellPos[c]) - P;
         const F3 dl = f3(A.pos[comp(lasts, s)]) - P, dx = f3(A.pos[comp(nexts, s)]) - P;
-        const double2 apc = A.ap[c], pr = A.pref[c];
-        const float dA = (float)(apc.x - pr.x), dP = (float)(apc.y - pr.y);
+        const float2 d = A.dap[c];
+        const float dA = d.x, dP = d.y;
         const float pp = 2.0f * dP, aa = 2.0f * A.Kr * dA;
         const F3 bl = inv * dl, bc = inv * dc, bx = inv * dx;
         const F3 fs = (-pp) * (grad_geo32(a, dl) + grad_geo32(a, dx)) +
@@ -92,13 +92,14 @@ __device__ __forceinline__ F3 vertex_force32(const Args32& A, int v, float R) {
     return f;
 }
 
-// p <- R (p + P_p d) / |p + P_p d| in FP64 from FP32 p and d, rounded to FP32 (w, the replica,
-// carried over).
+// p <- R (p + P_p d) / |p + P_p d| (sphericalDomain::move): the tangential projection of the FP32
+// displacement in FP32, then p + d and the renormalisation onto the sphere in FP64, rounded to
+// FP32 (w, the replica, carried over).
 __device__ __forceinline__ float4 move_fp64(float4 p, F3 d, double R) {
-    const double px = p.x, py = p.y, pz = p.z, dx = d.x, dy = d.y, dz = d.z;
-    const double s = (dx * px + dy * py + dz * pz) / (px * px + py * py + pz * pz);
-    const double qx = px + (dx - s * px), qy = py + (dy - s * py), qz = pz + (dz - s * pz);
-    const double k = R / sqrt(qx * qx + qy * qy + qz * qz);
+    const F3 pf = f3(p);
+    const F3 dt = d - (dotf(d, pf) / dotf(pf, pf)) * pf;
+    const double qx = (double)p.x + (double)dt.x, qy = (double)p.y + (double)dt.y, qz = (double)p.z + (double)dt.z;
+    const double k = R * rsqrt(qx * qx + qy * qy + qz * qz);
     return make_float4(__double2float_rn(k * qx), __double2float_rn(k * qy), __double2float_rn(k * qz), p.w);
 }
 
@@ -135,20 +136,37 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
     const float4 p = pos[v];
     const float R = (float)repR[rep_of(p)];
     const D3 pd = ld3(pos, v);
-    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
+    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v], nb = vnbr[v];
+    // per neighbour: FP64 cross product with p and its norm (for the included angles), FP32 arc
+    D3 U[3], C[3];
+    double nC[3];
+    float arc[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const float4 q = pos[comp(nb, j)];
+        U[j] = D3{(double)q.x, (double)q.y, (double)q.z};
+        C[j] = cross3(pd, U[j]);
+        nC[j] = sqrt(dot3(C[j], C[j]));
+        arc[j] = arc32(q, p, R);
+    }
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-        const int L = comp(lasts, s), X = comp(nexts, s);
-        const float4 pl = pos[L];
-        const double ang = included_angle(ld3(pos, L), pd, ld3(pos, X));  // FP64
-        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = make_double2((double)arc32(pl, p, R), ang);
+        const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
+        double2 cr;
+        if (jl >= 0 && jx >= 0) {
+            cr = make_double2((double)pick3(arc, jl), included_angle_pre(pick3(C, jx), pick3(C, jl), pick3(nC, jx),
+                                                                         pick3(nC, jl), pick3(U, jl)));
+        } else {  // inconsistent lists: evaluate directly
+            const int L = comp(lasts, s), X = comp(nexts, s);
+            cr = make_double2((double)arc32(pos[L], p, R), included_angle(ld3(pos, L), pd, ld3(pos, X)));
+        }
+        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
     }
     if (t1test) {
-        const int4 nb = vnbr[v];
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int u = comp(nb, s);
-            if (v < u && arc32(p, pos[u], R) < t1Threshold) {
+            if (v < u && arc[s] < t1Threshold) {
                 const int q = 3 * v + s;
                 atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
                 atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -214,7 +232,7 @@ __global__ void k_f4_to_aos(const float4* __restrict__ in, double* __restrict__ 
 Args32 args32(svm_model* m, int buf) {
     Args32 A;
     A.pos = m->pos32[buf]; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext; A.cellPos = m->cellPos32;
-    A.ap = m->ap; A.pref = m->pref; A.repR = m->repR; A.Kr = (float)m->Kr;
+    A.dap = m->dap32; A.repR = m->repR; A.Kr = (float)m->Kr;
     return A;
 }
 
@@ -251,6 +269,18 @@ int mixed_launch_force_bd(svm_model* m, double T, double dt, double mu, int nois
     return check_launch();
 }
 
+// largest block size (a multiple of 32) the batch's tuned kernels can launch with
+static int max_block(const void* f) {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, f) != cudaSuccess) return 256;
+    return a.maxThreadsPerBlock / 32 * 32;
+}
+int mixed_max_block_corners() { return max_block((const void*)k32_corners); }
+int mixed_max_block_force() {
+    return std::min(max_block((const void*)k32_force_bd<SVM_NOISE_PHILOX>),
+                    max_block((const void*)k32_force_bd<SVM_NOISE_BUFFER>));
+}
+
 int mixed_launch_move(svm_model* m, const double* disp, double scale) {
     k32_move<<<blocksFor(m->nVertices), kB, 0, m->stream>>>(m->pos32[m->cur], disp, scale, m->nVertices, m->repR);
     return check_launch();
@@ -279,7 +309,8 @@ extern "C" int svm_model_set_precision(svm_model* m, int precision) {
             bool ok = cudaMalloc(&m->pos32[0], nV * sizeof(float4)) == cudaSuccess &&
                       cudaMalloc(&m->pos32[1], nV * sizeof(float4)) == cudaSuccess &&
                       cudaMalloc(&m->cellPos32, nC * sizeof(float4)) == cudaSuccess &&
-                      cudaMalloc(&m->force32, nV * sizeof(float4)) == cudaSuccess;
+                      cudaMalloc(&m->force32, nV * sizeof(float4)) == cudaSuccess &&
+                      cudaMalloc(&m->dap32, nC * sizeof(float2)) == cudaSuccess;
             if (!ok) return SVM_ERR_CUDA;
             cudaMemsetAsync(m->force32, 0, nV * sizeof(float4), m->stream);
         }

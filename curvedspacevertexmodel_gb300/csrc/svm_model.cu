@@ -108,20 +108,38 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
     if (v >= nV) return;
     const D3 p = ld3(pos, v);
     vsph[v] = sph_coords(p);
-    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
+    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v], nb = vnbr[v];
+    // per neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v
+    // in its three cells are its three neighbours, as are the successors)
+    D3 U[3], C[3];
+    double nC[3], arc[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        U[j] = ld3(pos, comp(nb, j));
+        C[j] = cross3(p, U[j]);
+        nC[j] = sqrt(dot3(C[j], C[j]));
+        arc[j] = geodesic(U[j], p, R);
+    }
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-        const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
-        const double arc = geodesic(pl, p, R);
-        const double ang = included_angle(pl, p, px);
-        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = make_double2(arc, ang);
+        const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
+        double2 cr;
+        if (jl >= 0 && jx >= 0) {
+            cr = make_double2(pick3(arc, jl), included_angle_pre(pick3(C, jx), pick3(C, jl), pick3(nC, jx),
+                                                                 pick3(nC, jl), pick3(U, jl)));
+        } else {  // inconsistent lists: evaluate directly
+            const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
+            cr = make_double2(geodesic(pl, p, R), included_angle(pl, p, px));
+        }
+        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
     }
     if (t1test) {
-        const int4 nb = vnbr[v];
+        // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475); arc[j] is
+        // that geodesic, bitwise (its cosine's products commute exactly)
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
             const int u = comp(nb, s);
-            if (v < u && shorter_than(p, ld3(pos, u), R, t1Threshold, cosLo, cosHi)) {
+            if (v < u && arc[s] < t1Threshold) {
                 const int q = 3 * v + s;
                 atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
                 atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -143,7 +161,8 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
                         const int* __restrict__ ringCount, const double2* __restrict__ corner, int Wc, int nC,
                         double R0, const double* __restrict__ repR, PT* __restrict__ cellPos,
                         double4_32a* __restrict__ cellSph, double2* __restrict__ ap, double* __restrict__ partials,
-                        unsigned* __restrict__ ticket, double* __restrict__ scalars, int* __restrict__ fallbackFlag) {
+                        unsigned* __restrict__ ticket, double* __restrict__ scalars, int* __restrict__ fallbackFlag,
+                        const double2* __restrict__ pref = nullptr, float2* __restrict__ dap32 = nullptr) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double area = 0.0;
     if (c < nC) {
@@ -169,6 +188,10 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
         if (extra > 0) area = __dsub_rn(area, __dmul_rn((double)extra, kPI));
         area = __dmul_rn(__dmul_rn(area, R), R);
         ap[c] = make_double2(area, per);
+        if (dap32) {
+            const double2 pr = pref[c];
+            dap32[c] = make_float2((float)(area - pr.x), (float)(per - pr.y));
+        }
     }
     if (!ticket) return;
     const double R = R0;
@@ -201,7 +224,8 @@ template <class PT>
 __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ ring,
                            const int* __restrict__ ringCount, const PT* __restrict__ cellPos, int Wc, int nC,
                            double R0, const int* __restrict__ fallbackFlag, const int* __restrict__ repFlag,
-                           const double* __restrict__ repR, double2* __restrict__ ap) {
+                           const double* __restrict__ repR, double2* __restrict__ ap,
+                           const double2* __restrict__ pref = nullptr, float2* __restrict__ dap32 = nullptr) {
     if (!repFlag && *fallbackFlag == 0) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nC) return;
@@ -220,6 +244,7 @@ __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ r
         cur = next;
     }
     ap[c].x = area;
+    if (dap32) dap32[c].x = (float)(area - pref[c].x);
 }
 
 // ---- forces and integration ------------------------------------------------------------------
@@ -957,11 +982,17 @@ int launch_corners(svm_model* m, bool t1test) {
     return check_launch();
 }
 
+int max_block_cells_batch() {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, (const void*)k_cells<float4>) != cudaSuccess) return 256;
+    return a.maxThreadsPerBlock / 32 * 32;
+}
+
 static int launch_cells_batch(svm_model* m) {
     const int bs = m->blkCells;
     k_cells<float4><<<(m->nCells + bs - 1) / bs, bs, 0, m->stream>>>(
         m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, m->repR, m->cellPos32, nullptr,
-        m->ap, nullptr, nullptr, nullptr, nullptr);
+        m->ap, nullptr, nullptr, nullptr, nullptr, m->pref, m->dap32);
     return check_launch();
 }
 
@@ -976,7 +1007,7 @@ static int launch_cells(svm_model* m) {
         } else if (mixed) {
             k_cells<float4><<<blocksFor(m->nCells), kBlock, 0, m->stream>>>(
                 m->pos32[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, m->repR, m->cellPos32,
-                nullptr, m->ap, m->partials, m->ticket, m->scalars, m->fallbackFlag);
+                nullptr, m->ap, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->pref, m->dap32);
         } else {
             k_cells<double4_32a><<<blocksFor(m->nCells), kBlock, 0, m->stream>>>(
                 m->pos[m->cur], m->ring, m->ringCount, m->corner, m->Wc, m->nCells, m->R, nullptr, m->cellPos,
@@ -988,7 +1019,7 @@ static int launch_cells(svm_model* m) {
     if (mixed)
         k_fallback<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc,
                                                          m->nCells, m->R, m->fallbackFlag, batch ? m->repFlag : nullptr,
-                                                         m->repR, m->ap);
+                                                         m->repR, m->ap, m->pref, m->dap32);
     else
         k_fallback<double4_32a><<<nb, kBlock, 0, m->stream>>>(m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc,
                                                               m->nCells, m->R, m->fallbackFlag, nullptr, nullptr, m->ap);
@@ -1227,7 +1258,7 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
                     m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
-                    m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->repR, m->repNp, m->repCellOff,
+                    m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->dap32, m->repR, m->repNp, m->repCellOff,
                     m->repFlag, m->repScal};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);

@@ -267,7 +267,8 @@ int svm_batch_energies(svm_model* m, double* energies);
 /* Per-replica total area, excess over 4 pi R^2 and fallback flag of the last geometry. */
 int svm_batch_area_check(svm_model* m, double* totals, double* excess, int* fallbackTaken);
 /* Autotuning of the block size of the batch's corner, cell and force kernels, one KernelTuner
- * each over block sizes lo, lo+step, ..., hi (multiples of 32, at most 1024): the reference's
+ * each over block sizes lo, lo+step, ..., hi (multiples of 32, at most 1024, and at most the
+ * largest block each kernel's register use allows): the reference's
  * kernelTuner(start, end, step, nSamples, period) (src/utilities/kernelTuner.{h,cpp}).  While a
  * tuner samples, svm_brownian_run runs steps one by one with those kernels timed; graph-replayed
  * steps count as untimed calls toward the rescan period.  lo <= 0 turns tuning off (block 256). */
