@@ -180,13 +180,7 @@ __global__ void k_fire_finish(FireState* __restrict__ Sp, double4_32a* __restric
 }
 __global__ void k_fire_clear_pending(FireState* Sp) { Sp->pending = 0; }
 
-ForceArgs fargs(svm_model* m) {
-    ForceArgs A;
-    A.pos = m->pos[m->cur]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
-    A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
-    A.vec = m->precision == SVM_PRECISION_FP64_VECTOR ? 1 : 0;
-    return A;
-}
+ForceArgs fargs(svm_model* m) { return force_args(m, m->cur); }
 
 int fire_iteration(svm_fire* F) {
     svm_model* m = F->m;

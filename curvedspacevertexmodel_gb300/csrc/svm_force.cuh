@@ -108,4 +108,61 @@ __device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
     return f;
 }
 
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11): ten rounds of two 32x32->64 multiplies with a Weyl-sequence key schedule.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
+    const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { key.x += W0; key.y += W1; }
+        const unsigned hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        const unsigned hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+    }
+    return ctr;
+}
+// 53-bit uniform in (0, 1) from two 32-bit words.
+__device__ __forceinline__ double u53(unsigned a, unsigned b) {
+    const unsigned long long x = ((unsigned long long)a << 21) ^ (unsigned long long)(b >> 11);
+    return ((double)(x & ((1ull << 53) - 1)) + 0.5) * 0x1.0p-53;
+}
+// Three standard normals for (vertex, step) by Box-Muller on two Philox draws.
+__device__ __forceinline__ D3 philox_normals3(uint64_t seed, unsigned long long step, int v) {
+    const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    const uint4 r0 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 0u), key);
+    const uint4 r1 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 1u), key);
+    const double a = sqrt(-2.0 * log(u53(r0.x, r0.y)));
+    double s0, c0;
+    sincospi(2.0 * u53(r0.z, r0.w), &s0, &c0);
+    const double b = sqrt(-2.0 * log(u53(r1.x, r1.y)));
+    const double c1 = cospi(2.0 * u53(r1.z, r1.w));
+    return D3{a * c0, a * s0, b * c1};
+}
+
+// disp_d = xi_d sqrt(2 dt mu T) + F_d dt mu (brownianDynamics.cpp:37-44), products rounded
+// before the sum as on the CPU.
+__device__ __forceinline__ double bd_disp(double xi, double np, double f, double fp) {
+    return __dadd_rn(__dmul_rn(xi, np), __dmul_rn(f, fp));
+}
+// sphericalDomain::move with every product and sum rounded separately (no contraction), so the
+// renormalised positions follow the CPU's sequence of roundings.
+__device__ __forceinline__ D3 move_exact(D3 p, D3 v, double R) {
+    const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
+    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
+    const double s = vp / pp;
+    D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
+         __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
+    const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
+    const double inv = 1.0 / sqrt(qq);
+    return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
+}
+
+
+inline ForceArgs force_args(svm_model* m, int buf) {
+    ForceArgs A;
+    A.pos = m->pos[buf]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
+    A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
+    A.vec = m->precision == SVM_PRECISION_FP64_VECTOR ? 1 : 0;
+    return A;
+}
 }  // namespace svm

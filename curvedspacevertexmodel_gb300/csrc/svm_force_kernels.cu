@@ -1,0 +1,61 @@
+// The FP64 force kernels of the plain form: computeForce (sphericalVertexModel.cpp:356-420) alone
+// and fused with the Brownian displacement and the move (brownianDynamics.cpp:37-44,
+// sphericalDomain.h:203-209).  This translation unit is the one compiled with FMA contraction:
+// the force's own arithmetic differs from the CPU's by rounding only (as CUDA's acos already
+// does), while the displacement and the move spell out every product and sum with __dmul_rn /
+// __dadd_rn, so the position update keeps the CPU's sequence of roundings.
+#include "svm_force.cuh"
+
+namespace svm {
+int check_launch();
+}
+
+namespace {
+using namespace svm;
+
+constexpr int kFB = 256;
+
+__global__ void k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    st3(force, v, vertex_force(A, v));
+}
+
+// Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
+template <int kNoise>
+__global__ void k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force, double4_32a* __restrict__ posNext,
+                           const double* __restrict__ noise, uint64_t seed,
+                           const unsigned long long* __restrict__ stepCounter, double np, double fp) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 f = vertex_force(A, v);
+    st3(force, v, f);
+    D3 xi;
+    if (kNoise == SVM_NOISE_BUFFER) xi = D3{noise[3 * v], noise[3 * v + 1], noise[3 * v + 2]};
+    else xi = philox_normals3(seed, *stepCounter, v);
+    const D3 d{bd_disp(xi.x, np, f.x, fp), bd_disp(xi.y, np, f.y, fp), bd_disp(xi.z, np, f.z, fp)};
+    st3(posNext, v, move_exact(ld3(A.pos, v), d, A.R));
+}
+
+}  // namespace
+
+namespace svm {
+
+int launch_force_fp64(svm_model* m) {
+    k_force<<<(m->nVertices + kFB - 1) / kFB, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force);
+    return check_launch();
+}
+
+int launch_force_bd_fp64(svm_model* m, double np, double fp, int noiseMode, const double* noise, uint64_t seed,
+                         int nxt) {
+    const int nb = (m->nVertices + kFB - 1) / kFB;
+    if (noiseMode == SVM_NOISE_BUFFER)
+        k_force_bd<SVM_NOISE_BUFFER><<<nb, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force,
+                                                               m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+    else
+        k_force_bd<SVM_NOISE_PHILOX><<<nb, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force,
+                                                               m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+    return check_launch();
+}
+
+}  // namespace svm

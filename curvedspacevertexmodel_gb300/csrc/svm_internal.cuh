@@ -339,6 +339,10 @@ int mixed_max_block_corners();
 int mixed_max_block_force();
 int max_block_cells_batch();
 void batch_tuner_untimed(svm_model* m, int calls);
+// FP64 force kernels (svm_force_kernels.cu)
+int launch_force_fp64(svm_model* m);
+int launch_force_bd_fp64(svm_model* m, double np, double fp, int noiseMode, const double* noise, uint64_t seed,
+                         int nxt);
 // mixed-precision kernels (svm_mixed.cu)
 int mixed_launch_corners(svm_model* m, bool t1test);
 int mixed_launch_force(svm_model* m);

@@ -249,77 +249,6 @@ __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ r
 
 // ---- forces and integration ------------------------------------------------------------------
 
-__global__ void k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    st3(force, v, vertex_force(A, v));
-}
-
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
-// SC'11): ten rounds of two 32x32->64 multiplies with a Weyl-sequence key schedule.
-__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
-    const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r) { key.x += W0; key.y += W1; }
-        const unsigned hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
-        const unsigned hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
-        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
-    }
-    return ctr;
-}
-// 53-bit uniform in (0, 1) from two 32-bit words.
-__device__ __forceinline__ double u53(unsigned a, unsigned b) {
-    const unsigned long long x = ((unsigned long long)a << 21) ^ (unsigned long long)(b >> 11);
-    return ((double)(x & ((1ull << 53) - 1)) + 0.5) * 0x1.0p-53;
-}
-// Three standard normals for (vertex, step) by Box-Muller on two Philox draws.
-__device__ __forceinline__ D3 philox_normals3(uint64_t seed, unsigned long long step, int v) {
-    const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
-    const uint4 r0 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 0u), key);
-    const uint4 r1 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 1u), key);
-    const double a = sqrt(-2.0 * log(u53(r0.x, r0.y)));
-    double s0, c0;
-    sincospi(2.0 * u53(r0.z, r0.w), &s0, &c0);
-    const double b = sqrt(-2.0 * log(u53(r1.x, r1.y)));
-    const double c1 = cospi(2.0 * u53(r1.z, r1.w));
-    return D3{a * c0, a * s0, b * c1};
-}
-
-// disp_d = xi_d sqrt(2 dt mu T) + F_d dt mu (brownianDynamics.cpp:37-44), products rounded
-// before the sum as on the CPU.
-__device__ __forceinline__ double bd_disp(double xi, double np, double f, double fp) {
-    return __dadd_rn(__dmul_rn(xi, np), __dmul_rn(f, fp));
-}
-// sphericalDomain::move with every product and sum rounded separately (no contraction), so the
-// renormalised positions follow the CPU's sequence of roundings.
-__device__ __forceinline__ D3 move_exact(D3 p, D3 v, double R) {
-    const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
-    const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
-    const double s = vp / pp;
-    D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
-         __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
-    const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
-    const double inv = 1.0 / sqrt(qq);
-    return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
-}
-
-// Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
-template <int kNoise>
-__global__ void k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force, double4_32a* __restrict__ posNext,
-                           const double* __restrict__ noise, uint64_t seed,
-                           const unsigned long long* __restrict__ stepCounter, double np, double fp) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    const D3 f = vertex_force(A, v);
-    st3(force, v, f);
-    D3 xi;
-    if (kNoise == SVM_NOISE_BUFFER) xi = D3{noise[3 * v], noise[3 * v + 1], noise[3 * v + 2]};
-    else xi = philox_normals3(seed, *stepCounter, v);
-    const D3 d{bd_disp(xi.x, np, f.x, fp), bd_disp(xi.y, np, f.y, fp), bd_disp(xi.z, np, f.z, fp)};
-    st3(posNext, v, move_exact(ld3(A.pos, v), d, A.R));
-}
-
 // moveParticles (sphericalVertexModel.cpp:111-148): p <- move(p, scale * disp), in place.
 __global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__ disp, double scale, int nV, double R) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -752,10 +681,35 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
         t1.ctr[1] = 0; t1.ctr[2] = 0; t1.ctr[3] = 0; t1.ctr[4] = 0;
     }
     __syncthreads();
-    // 1. the flagged positions, ascending (bits stay set: a set bit means "pending")
-    for (int base = 0; base < t1.nWords; base += blockDim.x) {
-        const int w = base + tid;
-        const unsigned word = w < t1.nWords ? t1.bits[w] : 0u;
+    // 1. the flagged positions, ascending (bits stay set: a set bit means "pending").  First the
+    //    bitmap words whose summary bit is set (a superset of the non-empty words), ascending,
+    //    into `nxt`; then the set bits of those words.
+    __shared__ int nWordsHit;
+    if (tid == 0) nWordsHit = 0;
+    __syncthreads();
+    for (int base = 0; base < t1.nSummary; base += blockDim.x) {
+        const int sw = base + tid;
+        const unsigned sword = sw < t1.nSummary ? t1.summary[sw] : 0u;
+        int tot;
+        const int off = block_excl_scan(__popc(sword), &tot);
+        unsigned x = sword;
+        int at = nWordsHit + off;
+        while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1u;
+            const int w = sw * 32 + b;
+            if (w < t1.nWords && at < t1.cap) nxt[at] = w;
+            ++at;
+        }
+        __syncthreads();
+        if (tid == 0) nWordsHit = min(nWordsHit + tot, t1.cap);
+        __syncthreads();
+    }
+    const int nHit = nWordsHit;
+    for (int base = 0; base < nHit; base += blockDim.x) {
+        const int i = base + tid;
+        const int w = i < nHit ? nxt[i] : -1;
+        const unsigned word = (w >= 0 && w < t1.nWords) ? t1.bits[w] : 0u;
         int tot;
         const int off = block_excl_scan(__popc(word), &tot);
         if (nCur + tot > t1.cap) { if (tid == 0) flag = 1; __syncthreads(); break; }
@@ -948,13 +902,6 @@ __global__ void k_energy(const double2* __restrict__ ap, const double2* __restri
 }
 
 // ---- launch helpers --------------------------------------------------------------------------
-static ForceArgs force_args(svm_model* m, int buf) {
-    ForceArgs A;
-    A.pos = m->pos[buf]; A.vsph = m->vsph; A.vcell = m->vcell; A.vlast = m->vlast; A.vnext = m->vnext;
-    A.cellPos = m->cellPos; A.cellSph = m->cellSph; A.ap = m->ap; A.pref = m->pref; A.Kr = m->Kr; A.R = m->R;
-    A.vec = m->precision == SVM_PRECISION_FP64_VECTOR ? 1 : 0;
-    return A;
-}
 static ApplyArgs apply_args(svm_model* m, int bump) {
     ApplyArgs A;
     A.pos32 = m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr;
@@ -1056,12 +1003,8 @@ static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, 
         rc = batch_tuned_force_bd(m, T, dt, mu, noiseMode, noise, seed, nxt);
     else if (m->precision == SVM_PRECISION_MIXED)
         rc = mixed_launch_force_bd(m, T, dt, mu, noiseMode, noise, seed, nxt);
-    else if (noiseMode == SVM_NOISE_BUFFER)
-        k_force_bd<SVM_NOISE_BUFFER><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
-            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     else
-        k_force_bd<SVM_NOISE_PHILOX><<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
-            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+        rc = launch_force_bd_fp64(m, np, fp, noiseMode, noise, seed, nxt);
     }
     if (rc || (rc = check_launch())) return rc;
     m->cur = nxt;
@@ -1377,8 +1320,7 @@ int svm_model_compute_forces(svm_model* m) {
     if (rc) return rc;
     svm::PhaseTimer pt(m, SVM_PHASE_FORCE);
     if (m->precision == SVM_PRECISION_MIXED) return svm::mixed_launch_force(m);
-    k_force<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(svm::force_args(m, m->cur), m->nVertices, m->force);
-    return svm::check_launch();
+    return svm::launch_force_fp64(m);
 }
 
 int svm_model_compute_energy(svm_model* m, double* e) {
