@@ -1,9 +1,9 @@
 // The FP64 force kernels of the plain form: computeForce (sphericalVertexModel.cpp:356-420) alone
 // and fused with the Brownian displacement and the move (brownianDynamics.cpp:37-44,
-// sphericalDomain.h:203-209).  This translation unit is the one compiled with FMA contraction:
-// the force's own arithmetic differs from the CPU's by rounding only (as CUDA's acos already
-// does), while the displacement and the move spell out every product and sum with __dmul_rn /
-// __dadd_rn, so the position update keeps the CPU's sequence of roundings.
+// sphericalDomain.h:203-209).  Kept in its own translation unit so that its contraction setting
+// can differ from the geometry's; it is built without FMA contraction like the rest (the force's
+// rounding then differs from the CPU's only through acos), and the displacement and the move spell
+// out every product and sum with __dmul_rn / __dadd_rn.
 #include "svm_force.cuh"
 
 namespace svm {
