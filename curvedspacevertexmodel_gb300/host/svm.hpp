@@ -5,7 +5,9 @@
 // lives on the GPU; there is no CPU branch (setCPUOperation(true) throws).  Failures of the C ABI
 // are raised as std::runtime_error, as the reference's HANDLE_ERROR raises (inc/std_include.h:123-134).
 #pragma once
+#include <algorithm>
 #include <cmath>
+#include <iostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -30,6 +32,12 @@ class noiseSource {
     void setReproducible(bool rep) { Reproducible = rep; }
     bool Reproducible;
     int RNGSeed = -1;
+};
+
+// a created model and its sizes (used by derived models that build their own handle)
+struct ModelHandle {
+    svm_model* h;
+    int nCells, nVertices, ringCapacity;
 };
 
 // sphericalVertexModel (src/model/sphericalVertexModel.h:10-123); n counts cells.
@@ -70,6 +78,9 @@ class sphericalVertexModel {
     void setScalarModelParameter(scalar kr) { Kr = kr; check(svm_model_set_scalar_model_parameter(h(), kr), "setScalarModelParameter"); }
     void setT1Threshold(scalar t) { t1Threshold = t; check(svm_model_set_t1_threshold(h(), t), "setT1Threshold"); }
     void setRestrictedMotion(bool r) { restrictedMotion = r; check(svm_model_set_restricted_motion(h(), r), "restrictedMotion"); }
+    // SVM_PRECISION_FP64 (the plain form), SVM_PRECISION_MIXED (FP32 bulk, FP64 areas/energy/
+    // renormalisation) or SVM_PRECISION_FP64_VECTOR (FP64 with the vector-form gradient)
+    void setPrecision(int precision) { check(svm_model_set_precision(h(), precision), "setPrecision"); }
     int getNumberOfParticles() const { return nVertices; }
 
     // the path
@@ -92,9 +103,134 @@ class sphericalVertexModel {
     scalar radius = 1.0, Kr = 1.0, t1Threshold = 0.1;
     bool restrictedMotion = false;
 
+  protected:
+    // adopts an already created model (batches)
+    explicit sphericalVertexModel(ModelHandle mh)
+        : nCells(mh.nCells), nVertices(mh.nVertices), ringCapacity(mh.ringCapacity), m(mh.h) {}
+
   private:
     struct Del { void operator()(svm_model* p) const { svm_model_destroy(p); } };
     std::unique_ptr<svm_model, Del> m;
+};
+
+// Independent spheres of uneven size in one model (svm_batch_* in svm.h; no counterpart in the
+// reference, which runs one sphere per process).  Replica r has nCellsPerReplica[r] cells from
+// the seeded recipe with seeds[r] and radius sqrt(N_r / 4 pi); the batch runs the mixed form, and a
+// brownianDynamics updater drives it with the per-replica temperatures of setTemperatures.
+namespace detail {
+// concatenated topology of a batch, built before the model base class is constructed
+struct BatchTopo {
+    std::vector<double> vp;
+    std::vector<int> rings, vc, vn;
+    std::vector<unsigned> counts;
+    int nv = 0, cap = 0;
+};
+struct BatchTopoHolder {
+    BatchTopo topo;
+};
+}  // namespace detail
+
+class sphericalVertexModelBatch : private detail::BatchTopoHolder, public sphericalVertexModel {
+  public:
+    sphericalVertexModelBatch(const std::vector<int>& nCellsPerReplica, const std::vector<int>& seeds, scalar a0 = 1.0,
+                              scalar p0 = 3.8, int cap = 16)
+        : sphericalVertexModel(create(nCellsPerReplica, seeds, cap, topo)) {
+        nReplicas = (int)nCellsPerReplica.size();
+        check(svm_model_set_topology(h(), topo.vp.data(), topo.rings.data(), topo.cap, topo.counts.data(), topo.vc.data(),
+                                     topo.vn.data()),
+              "svm_model_set_topology");
+        topo = detail::BatchTopo{};
+        setT1Threshold(0.1);
+        setPreferredParameters(a0, p0);
+        setScalarModelParameter(1.0);
+        computeGeometry();
+    }
+    void setTemperatures(const std::vector<double>& T) { check(svm_batch_set_temperatures(h(), T.data()), "setTemperatures"); }
+    std::vector<double> replicaEnergies() {
+        std::vector<double> e(nReplicas);
+        check(svm_batch_energies(h(), e.data()), "replicaEnergies");
+        return e;
+    }
+    // kernelTuner-style block-size tuning of the batch kernels (lo <= 0: off)
+    void autotune(int lo = 64, int hi = 1024, int step = 64, int nSamples = 3, int period = 1000) {
+        check(svm_batch_autotune(h(), lo, hi, step, nSamples, period), "autotune");
+    }
+    int nReplicas = 0;
+
+  private:
+    using Topo = detail::BatchTopo;
+    static ModelHandle create(const std::vector<int>& n, const std::vector<int>& seeds, int cap, Topo& T) {
+        if (n.size() != seeds.size() || n.empty()) throw std::runtime_error("one seed per replica");
+        struct One { std::vector<double> vp; std::vector<int> rings, vc, vn; std::vector<unsigned> counts; int nv, w; };
+        std::vector<One> reps;
+        std::vector<int> nvs;
+        std::vector<double> radius;
+        int width = cap;
+        for (size_t r = 0; r < n.size(); ++r) {
+            std::vector<double> centres(3 * (size_t)n[r]);
+            check(svm_random_cell_centres(seeds[r], n[r], centres.data()), "svm_random_cell_centres");
+            svm_topology* t = nullptr;
+            check(svm_topology_from_points(centres.data(), n[r], &t), "svm_topology_from_points");
+            int nc = 0, nv = 0, mr = 0;
+            svm_topology_sizes(t, &nc, &nv, &mr);
+            One o{std::vector<double>(3 * (size_t)nv), std::vector<int>((size_t)nc * mr), std::vector<int>(3 * (size_t)nv),
+                  std::vector<int>(3 * (size_t)nv), std::vector<unsigned>(nc), nv, mr};
+            const int rc = svm_topology_get(t, o.vp.data(), o.rings.data(), mr, o.counts.data(), o.vc.data(), o.vn.data());
+            svm_topology_free(t);
+            check(rc, "svm_topology_get");
+            width = std::max(width, mr + 1);
+            nvs.push_back(nv);
+            radius.push_back(std::sqrt(n[r] / (4.0 * M_PI)));
+            reps.push_back(std::move(o));
+        }
+        int cOff = 0, vOff = 0;
+        T.cap = width;
+        for (size_t r = 0; r < reps.size(); ++r) {
+            const One& o = reps[r];
+            for (double x : o.vp) T.vp.push_back(x);
+            for (int c = 0; c < n[r]; ++c) {
+                for (int k = 0; k < width; ++k)
+                    T.rings.push_back(k < o.w && o.rings[(size_t)c * o.w + k] >= 0 ? o.rings[(size_t)c * o.w + k] + vOff : -1);
+                T.counts.push_back(o.counts[c]);
+            }
+            for (int x : o.vc) T.vc.push_back(x + cOff);
+            for (int x : o.vn) T.vn.push_back(x + vOff);
+            cOff += n[r];
+            vOff += o.nv;
+        }
+        T.nv = vOff;
+        svm_model* h = nullptr;
+        check(svm_batch_create((int)n.size(), n.data(), nvs.data(), width, radius.data(), nullptr, &h), "svm_batch_create");
+        return ModelHandle{h, cOff, vOff, width};
+    }
+};
+
+// kernelTuner (src/utilities/kernelTuner.{h,cpp}): bracket a launch with begin()/end() and launch
+// with getParameter(); CUDA events on `stream` (nullptr: the legacy default stream).
+class kernelTuner {
+  public:
+    kernelTuner(int start, int end, int step, int nSamples, int period, void* stream = nullptr) {
+        check(svm_tuner_create(start, end, step, nSamples, period, stream, &t), "kernelTuner");
+    }
+    ~kernelTuner() { svm_tuner_destroy(t); }
+    kernelTuner(const kernelTuner&) = delete;
+    kernelTuner& operator=(const kernelTuner&) = delete;
+    void begin() { check(svm_tuner_begin(t), "kernelTuner::begin"); }
+    void end() { check(svm_tuner_end(t), "kernelTuner::end"); }
+    int getParameter() { int v = 0; check(svm_tuner_parameter(t, &v), "kernelTuner::getParameter"); return v; }
+    bool samplingComplete() { int d = 0; check(svm_tuner_sampling_complete(t, &d), "samplingComplete"); return d != 0; }
+    void printTimingData() {
+        int n = 0;
+        svm_tuner_timing_data(t, nullptr, nullptr, 0, &n);
+        std::vector<int> c(n);
+        std::vector<float> med(n);
+        svm_tuner_timing_data(t, c.data(), med.data(), n, &n);
+        std::cout << "parameter used: " << getParameter() << std::endl;
+        for (int i = 1; i < n; ++i) std::cout << "tuner value " << c[i] << " median time " << med[i] << std::endl;
+    }
+
+  private:
+    svm_tuner* t = nullptr;
 };
 
 class updater {
@@ -133,7 +269,10 @@ class energyMinimizerFIRE : public updater {
         p = {dt, alphaStart, dtMax, dtInc, dtDec, alphaDec, (double)nMin, forceCutoff, alphaMin};
         reset();
     }
-    void setMaximumIterations(int n) { maxIterations = n; reset(); }
+    void setMaximumIterations(int n) {
+        maxIterations = n;
+        if (f) check(svm_fire_set_max_iterations(f, n), "setMaximumIterations");
+    }
     void performUpdate() override { minimize(); }
     void minimize() {
         ensure();

@@ -5,7 +5,8 @@
 Builds a model of N cells from the seeded recipe, runs `stab` stabilisation steps (T = 0, P0 = 1,
 as the reference driver does) and then `steps` Brownian steps at T = 0.01, P0 = 3.8, dt = 0.01
 (T1 threshold 0.04), one launch per kernel per step (no graph), and prints the energy per cell.
-With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*).
+With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*); with --replicas R
+a batch of R replicas runs instead (stabilisation, then `steps` steps at per-replica P0 and T).
 """
 from __future__ import annotations
 
@@ -22,8 +23,31 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--seed", type=int, default=1137)
     ap.add_argument("--mixed", action="store_true", help="run the timed steps in the mixed-precision form")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="instead: a batch of this many replicas, N log-uniform in [100, 5000] (seeded), "
+                         "P0 U[3.6, 3.95], T logU[1e-4, 1e-1]")
     args = ap.parse_args()
     t0 = time.time()
+    if args.replicas:
+        import numpy as np
+        rng = np.random.default_rng(args.seed)
+        sizes = np.exp(rng.uniform(np.log(100), np.log(5000), args.replicas)).astype(int)
+        b = svm.sphericalVertexModelBatch(sizes, args.seed + np.arange(args.replicas), p0=1.0)
+        b.setT1Threshold(0.04)
+        bd = svm.brownianDynamics()
+        bd.setModel(b)
+        b.setTemperatures(np.zeros(args.replicas))
+        for _ in range(args.stab):
+            bd.integrateEquationOfMotion()
+        b.setPreferredParameters(1.0, rng.uniform(3.6, 3.95, args.replicas))
+        b.setTemperatures(np.exp(rng.uniform(np.log(1e-4), np.log(1e-1), args.replicas)))
+        for _ in range(args.steps):
+            bd.integrateEquationOfMotion()
+        b.computeGeometry()
+        e = b.replicaEnergies() / sizes
+        print(f"replicas {args.replicas} cells {b.nCells} vertices {b.nVertices} median energy/cell {np.median(e):.6g} "
+              f"status {b.deviceStatus()} wall {time.time() - t0:.1f} s")
+        return
     noise = svm.noiseSource()
     noise.setReproducibleSeed(args.seed)
     m = svm.sphericalVertexModel(args.cells, noise, 1.0, 3.8)
