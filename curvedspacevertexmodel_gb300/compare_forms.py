@@ -5,7 +5,8 @@ same FP32-representable state and are driven by the same standard normals (host-
 injected each step), so they differ only by arithmetic.  Reported at checkpoints: energy per cell,
 the relative energy difference, area and perimeter differences (cells matched by index), the
 fraction of vertices whose neighbours agree, the T1 flips of the last interval in both forms and
-how many of them coincide, and each form's step time.
+how many of them coincide (the same edge flipped in the same 200-step window), and each form's
+step time (host-synchronised, including the noise upload).
 
     python -m curvedspacevertexmodel_gb300.compare_forms --steps 10000 --every 1000
 """
@@ -61,6 +62,7 @@ def main():
     a.takeFlips()
     b.takeFlips()
     ta = tb = 0.0
+    nfa = nfb = ncommon = 0
     for step in range(1, args.steps + 1):
         xi = rng.standard_normal((a.nVertices, 3))
         for bd, m in ((bda, a), (bdb, b)):
@@ -73,9 +75,12 @@ def main():
                 ta += time.perf_counter() - t0
             else:
                 tb += time.perf_counter() - t0
-        if step % args.every == 0:
+        if step % 200 == 0 or step % args.every == 0:  # the flip logs hold 65,536 flips
             fa, fb = a.takeFlips(), b.takeFlips()
-            common = len(set(map(tuple, fa)) & set(map(tuple, fb)))
+            nfa += len(fa)
+            nfb += len(fb)
+            ncommon += len(set(map(tuple, fa)) & set(map(tuple, fb)))
+        if step % args.every == 0:
             a.computeGeometry()
             b.computeGeometry()
             ea, eb = a.computeEnergy() / args.cells, b.computeEnergy() / args.cells
@@ -88,9 +93,10 @@ def main():
                                              float(np.max(np.abs(apa[:, 0] - apb[:, 0])))],
                 "perimeter_abs_diff_median_max": [float(np.median(np.abs(apa[:, 1] - apb[:, 1]))),
                                                   float(np.max(np.abs(apa[:, 1] - apb[:, 1])))],
-                "same_neighbour_fraction": float(same_nb), "flips_fp64": len(fa), "flips_mixed": len(fb),
-                "flips_common": common, "ms_per_step_fp64": 1e3 * ta / step, "ms_per_step_mixed": 1e3 * tb / step,
+                "same_neighbour_fraction": float(same_nb), "flips_fp64": nfa, "flips_mixed": nfb,
+                "flips_common": ncommon, "ms_per_step_fp64": 1e3 * ta / step, "ms_per_step_mixed": 1e3 * tb / step,
                 "status": [a.deviceStatus(), b.deviceStatus()]}), flush=True)
+            nfa = nfb = ncommon = 0
 
 
 def _noise(seed):

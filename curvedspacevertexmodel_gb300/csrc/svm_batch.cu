@@ -194,15 +194,12 @@ int svm_batch_create(int nReplicas, const int* nCells, const int* nVertices, int
     m->hRepCellOff = cOff;
     m->hRepVertOff = vOff;
     if ((rc = svm_model_set_precision(m, SVM_PRECISION_MIXED))) { svm_model_destroy(m); return rc; }
-    int* dv = nullptr;
     bool ok = cudaMemcpy(m->repCellOff, cOff.data(), sizeof(int) * (nReplicas + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMalloc(&dv, sizeof(int) * (nReplicas + 1)) == cudaSuccess &&
-              cudaMemcpy(dv, vOff.data(), sizeof(int) * (nReplicas + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+              cudaMemcpy(m->repVertOff, vOff.data(), sizeof(int) * (nReplicas + 1), cudaMemcpyHostToDevice) == cudaSuccess;
     if (ok) {
-        k_set_rep<<<nReplicas, kRB, 0, m->stream>>>(m->pos32[0], m->pos32[1], dv);
+        k_set_rep<<<nReplicas, kRB, 0, m->stream>>>(m->pos32[0], m->pos32[1], m->repVertOff);
         ok = cudaStreamSynchronize(m->stream) == cudaSuccess;
     }
-    if (dv) cudaFree(dv);
     if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
     *out = m;
     return SVM_OK;

@@ -113,9 +113,16 @@ __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
 // computed once per neighbour of p: cross(pl, p) = -(p x pl) exactly, the negations cancel exactly
 // in the dot product and the norms, and det(pl, p, px) = pl . (p x px) in the same operation
 // order, so the result is bitwise included_angle(pl, p, px).
+//
+// With `clamp` (the mixed form) the cosine is clamped to [-1, 1]: for a nearly straight corner its
+// rounding can leave the domain, where acos is NaN (the reference does not clamp, and the FP64
+// form keeps that behaviour).
+template <bool clamp = false>
 __device__ __forceinline__ double included_angle_pre(D3 Cx, D3 Cl, double nx, double nl, D3 pl) {
     const double det = dot3(pl, Cx);
-    double a = acos(dot3(Cx, Cl) / (nx * nl));
+    double c = dot3(Cx, Cl) / (nx * nl);
+    if (clamp) c = fmin(1.0, fmax(-1.0, c));
+    double a = acos(c);
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -125,6 +132,16 @@ template <class T>
 __device__ __forceinline__ T pick3(const T* a, int j) { return j == 0 ? a[0] : (j == 1 ? a[1] : a[2]); }
 // slot of vertex u among the three neighbour slots nb (-1 if absent)
 __device__ __forceinline__ int nbr_slot(int4 nb, int u) { return u == nb.x ? 0 : (u == nb.y ? 1 : (u == nb.z ? 2 : -1)); }
+// included_angle with the cosine clamped to [-1, 1] (the mixed form)
+__device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
+    D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
+    double det = det3(p1, p2, p3);
+    double c = -dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1)));
+    double a = acos(fmin(1.0, fmax(-1.0, c)));
+    if (det > 0) a = -a;
+    if (a < 0) a += 2. * kPI;
+    return a;
+}
 // sphericalTriangleArea (sphericalDomain.h:135-166)
 __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
     D3 p1 = scl3(1.0 / sqrt(dot3(q1, q1)), q1), p2 = scl3(1.0 / sqrt(dot3(q2, q2)), q2),
@@ -205,6 +222,7 @@ struct UndoEntry {
     int4 vc1, vc2;                 // old vertex->cell slots of v1, v2
     int4 vn[4];                    // old vertex->vertex slots of v1, v2, b, c
     int counts[4];                 // old ring sizes
+    int logIdx;                    // the flip's entry in the flip log
 };
 
 struct T1Scratch {
@@ -233,6 +251,8 @@ struct T1Scratch {
     int cap = 0, undoCap = 0;
 };
 constexpr int kFootprint = 14;     // 8 vertex slots + 6 cell slots (duplicates allowed)
+constexpr int kListPad = 1024;     // list slack of a single-sphere parallel pass
+constexpr int kListPadBatch = 64;  // list slack per replica of a batch's parallel pass
 constexpr int kResFree = 0x7f7f7f7f;
 
 }  // namespace svm
@@ -270,6 +290,7 @@ struct svm_model {
     double* repR = nullptr;            // device [nRep]
     float* repNp = nullptr;            // device [nRep], sqrt(2 dt mu T_r) of the batch's last step
     int* repCellOff = nullptr;         // device [nRep + 1]
+    int* repVertOff = nullptr;         // device [nRep + 1]
     int* repFlag = nullptr;            // device [nRep], area-check fallback flags
     double* repScal = nullptr;         // device [3 nRep]: total area, excess, energy
     std::vector<double> repT;          // host, per-replica temperatures of a batch

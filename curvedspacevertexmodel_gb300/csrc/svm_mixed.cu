@@ -154,11 +154,11 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
         const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
         double2 cr;
         if (jl >= 0 && jx >= 0) {
-            cr = make_double2((double)pick3(arc, jl), included_angle_pre(pick3(C, jx), pick3(C, jl), pick3(nC, jx),
-                                                                         pick3(nC, jl), pick3(U, jl)));
+            cr = make_double2((double)pick3(arc, jl), included_angle_pre<true>(pick3(C, jx), pick3(C, jl),
+                                                                               pick3(nC, jx), pick3(nC, jl), pick3(U, jl)));
         } else {  // inconsistent lists: evaluate directly
             const int L = comp(lasts, s), X = comp(nexts, s);
-            cr = make_double2((double)arc32(pos[L], p, R), included_angle(ld3(pos, L), pd, ld3(pos, X)));
+            cr = make_double2((double)arc32(pos[L], p, R), included_angle_clamped(ld3(pos, L), pd, ld3(pos, X)));
         }
         corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
     }

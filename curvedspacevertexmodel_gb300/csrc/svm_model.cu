@@ -456,7 +456,7 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
         const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
         if (A.pos32) {
             A.corner[(long)cell * A.Wc + k] =
-                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle(pl, p, px));
+                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped(pl, p, px));
         } else {
             A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
             A.vsph[u] = sph_coords(p);
@@ -505,7 +505,8 @@ __global__ void __launch_bounds__(kApplyThreads) k_t1_apply(ApplyArgs A, T1Scrat
         }
         return;
     }
-    if (tid == 0) { nbuf = 0; head = 0; nheap = 0; extractWord = 0; nTouched = 0; t1.stats[6] = *t1.flipCount; }
+    // touched cells are appended after those of the parallel pass's segments that succeeded
+    if (tid == 0) { nbuf = 0; head = 0; nheap = 0; extractWord = 0; nTouched = t1.ctr[5]; t1.stats[6] = *t1.flipCount; }
     __syncthreads();
     int lastProcessed = -1;
     while (true) {
@@ -631,7 +632,8 @@ __device__ __forceinline__ void t1_footprint(const ApplyArgs& A, int p, int* f) 
     f[8] = c1.x; f[9] = c1.y; f[10] = c1.z; f[11] = c2.x; f[12] = c2.y; f[13] = c2.z;
 }
 
-constexpr int kParThreads = 1024;
+constexpr int kParThreads = 1024;       // one segment: the whole sphere
+constexpr int kParThreadsBatch = 256;   // one segment per replica
 
 // Block-wide exclusive scan of one int per thread; returns the block total in *total.
 __device__ int block_excl_scan(int v, int* total) {
@@ -669,27 +671,44 @@ __device__ int block_excl_scan(int v, int* total) {
 // detected through the per-vertex/per-cell record of the highest position that ran, and then
 // every flip of the pass is undone and the bitmap restored for k_t1_apply, which then applies
 // the flips one by one.  On success *t1.count is cleared so k_t1_apply returns at once.
-__global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scratch t1) {
-    __shared__ int nCur, nTouched, flip0, flag;
-    const int tid = threadIdx.x;
-    if (tid == 0) t1.ctr[5] = 0;  // touched cells of this pass (read by k_t1_patch)
-    if (*t1.count == 0) return;
-    int* cur = t1.listA;
-    int* nxt = t1.listB;
-    if (tid == 0) {
-        nCur = 0; nTouched = 0; flip0 = *t1.flipCount; flag = 0;
-        t1.ctr[1] = 0; t1.ctr[2] = 0; t1.ctr[3] = 0; t1.ctr[4] = 0;
-    }
+// One block per segment of the position space: the whole sphere, or one replica of a batch (whose
+// flagged edges share no vertex or cell with another replica's, and whose positions are a
+// contiguous range).  A block's lists, footprints, commit list and undo log are its own slices of
+// the scratch arrays; the touched-cell list and the flip log are shared (atomic appends).  A block
+// whose pass is not the sequential order undoes its own flips, marks their log entries invalid
+// (pass -1) and restores its segment's flags, which k_t1_apply then replays; the counter of
+// flagged positions drops by the positions of every block that succeeded.  The last block to
+// finish (ticket) folds the round count into the statistics and clears summary bits whose bitmap
+// words are empty.
+__global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scratch t1, const int* __restrict__ segOff,
+                                                             int listPad, int undoPer) {
+    __shared__ int nCur, nTouchedB, flag, sNext, sUndo, sRollback, sExec, sFlips, nWordsHit;
+    const int tid = threadIdx.x, seg = blockIdx.x;
+    // one segment and nothing flagged: nothing to do.  (With several segments every block runs:
+    // the last one to finish does the pass's cleanup.)
+    if (gridDim.x == 1 && *t1.count == 0) return;
+    const int qLo = segOff ? 3 * segOff[seg] : 0;
+    const int qHi = segOff ? 3 * segOff[seg + 1] : 3 * A.nV;
+    const int base = qLo / 2 + listPad * seg;
+    const int capB = (qHi - qLo) / 2 + listPad;
+    int* cur = t1.listA + base;
+    int* nxt = t1.listB + base;
+    int* orig = t1.listOrig + base;
+    int* fpB = t1.fp + (long)base * kFootprint;
+    int* comB = t1.comList + (long)base * kFootprint;
+    UndoEntry* undoB = t1.undo + (long)seg * undoPer;
+    int* undoRingsB = t1.undoRings + (long)seg * undoPer * 4 * A.Wc;
+    if (tid == 0) { nCur = 0; nTouchedB = 0; flag = 0; sNext = 0; sUndo = 0; sRollback = 0; sExec = 0; sFlips = 0; nWordsHit = 0; }
     __syncthreads();
-    // 1. the flagged positions, ascending (bits stay set: a set bit means "pending").  First the
-    //    bitmap words whose summary bit is set (a superset of the non-empty words), ascending,
-    //    into `nxt`; then the set bits of those words.
-    __shared__ int nWordsHit;
-    if (tid == 0) nWordsHit = 0;
-    __syncthreads();
-    for (int base = 0; base < t1.nSummary; base += blockDim.x) {
-        const int sw = base + tid;
-        const unsigned sword = sw < t1.nSummary ? t1.summary[sw] : 0u;
+    // 1. the segment's flagged positions, ascending: the bitmap words whose summary bit is set
+    //    (a superset of the non-empty words) into `nxt`, then their set bits inside [qLo, qHi)
+    const int wLo = qLo >> 5, wHi = (qHi + 31) >> 5;  // words [wLo, wHi)
+    for (int base2 = wLo >> 5; base2 < ((wHi + 31) >> 5); base2 += blockDim.x) {
+        const int sw = base2 + tid;
+        unsigned sword = sw < ((wHi + 31) >> 5) && sw < t1.nSummary ? t1.summary[sw] : 0u;
+        // keep the summary bits of words inside [wLo, wHi)
+        if (sw == (wLo >> 5)) sword &= ~0u << (wLo & 31);
+        if (sw == ((wHi - 1) >> 5) && (wHi & 31)) sword &= (1u << (wHi & 31)) - 1u;
         int tot;
         const int off = block_excl_scan(__popc(sword), &tot);
         unsigned x = sword;
@@ -698,160 +717,204 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
             const int b = __ffs(x) - 1;
             x &= x - 1u;
             const int w = sw * 32 + b;
-            if (w < t1.nWords && at < t1.cap) nxt[at] = w;
+            if (w < t1.nWords && at < capB) nxt[at] = w;
             ++at;
         }
         __syncthreads();
-        if (tid == 0) nWordsHit = min(nWordsHit + tot, t1.cap);
+        if (tid == 0) nWordsHit = min(nWordsHit + tot, capB);
         __syncthreads();
     }
     const int nHit = nWordsHit;
-    for (int base = 0; base < nHit; base += blockDim.x) {
-        const int i = base + tid;
+    for (int b0 = 0; b0 < nHit; b0 += blockDim.x) {
+        const int i = b0 + tid;
         const int w = i < nHit ? nxt[i] : -1;
-        const unsigned word = (w >= 0 && w < t1.nWords) ? t1.bits[w] : 0u;
+        unsigned word = (w >= 0 && w < t1.nWords) ? t1.bits[w] : 0u;
+        if (w == (qLo >> 5)) word &= ~0u << (qLo & 31);
+        if (w >= 0 && w == ((qHi - 1) >> 5) && (qHi & 31)) word &= (1u << (qHi & 31)) - 1u;
         int tot;
         const int off = block_excl_scan(__popc(word), &tot);
-        if (nCur + tot > t1.cap) { if (tid == 0) flag = 1; __syncthreads(); break; }
+        if (nCur + tot > capB) { if (tid == 0) flag = 1; __syncthreads(); break; }
         unsigned x = word;
         int at = nCur + off;
         while (x) {
             const int b = __ffs(x) - 1;
             x &= x - 1u;
             cur[at] = w * 32 + b;
-            t1.listOrig[at] = w * 32 + b;
+            orig[at] = w * 32 + b;
             ++at;
         }
         __syncthreads();
         if (tid == 0) nCur += tot;
         __syncthreads();
     }
-    if (flag) return;  // more candidates than the pass holds: k_t1_apply takes them all
     const int nOrig = nCur;
     int rounds = 0;
+    bool rollback = flag != 0;  // more candidates than the slice holds: k_t1_apply takes them all
     // 2. rounds
-    while (nCur > 0) {
+    while (!rollback && nCur > 0) {
         ++rounds;
         // reserve
         for (int i = tid; i < nCur; i += blockDim.x) {
             const int p = cur[i];
-            int* f = t1.fp + (long)i * kFootprint;
+            int* f = fpB + (long)i * kFootprint;
             t1_footprint(A, p, f);
             bool late = false;
             for (int k = 0; k < 8; ++k) { late |= t1.comV[f[k]] > p; atomicMin(t1.resV + f[k], p); }
             for (int k = 8; k < kFootprint; ++k) { late |= t1.comC[f[k]] > p; atomicMin(t1.resC + f[k], p); }
-            if (late) atomicExch(t1.ctr + 3, 1);
+            if (late) atomicExch(&sRollback, 1);
         }
         __syncthreads();
-        if (*(volatile int*)(t1.ctr + 3)) break;
+        if (sRollback) {
+            // release this round's reservations before leaving
+            for (int i = tid; i < nCur; i += blockDim.x) {
+                const int* f = fpB + (long)i * kFootprint;
+                for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
+                for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
+            }
+            rollback = true;
+            break;
+        }
         // run the positions that hold their whole footprint
         for (int i = tid; i < nCur; i += blockDim.x) {
             const int p = cur[i];
-            const int* f = t1.fp + (long)i * kFootprint;
+            const int* f = fpB + (long)i * kFootprint;
             bool ready = true;
             for (int k = 0; k < 8; ++k) ready &= t1.resV[f[k]] == p;
             for (int k = 8; k < kFootprint; ++k) ready &= t1.resC[f[k]] == p;
             if (!ready) {
-                const int ni = atomicAdd(t1.ctr + 1, 1);
-                if (ni < t1.cap) nxt[ni] = p;
-                else atomicExch(t1.ctr + 3, 1);
+                const int ni = atomicAdd(&sNext, 1);
+                if (ni < capB) nxt[ni] = p;
+                else atomicExch(&sRollback, 1);
                 continue;
             }
-            const int ci = atomicAdd(t1.ctr + 4, 1);
-            if (ci >= t1.cap) { atomicExch(t1.ctr + 3, 1); continue; }
-            for (int k = 0; k < kFootprint; ++k) t1.comList[(long)ci * kFootprint + k] = f[k];
+            const int ci = atomicAdd(&sExec, 1);
+            if (ci >= capB) { atomicExch(&sRollback, 1); continue; }
+            for (int k = 0; k < kFootprint; ++k) comB[(long)ci * kFootprint + k] = f[k];
             for (int k = 0; k < 8; ++k) atomicMax(t1.comV + f[k], p);
             for (int k = 8; k < kFootprint; ++k) atomicMax(t1.comC + f[k], p);
             atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
             if (!t1_candidate(A, p)) continue;
-            const int ui = atomicAdd(t1.ctr + 2, 1);
-            if (ui >= t1.undoCap) { atomicExch(t1.ctr + 3, 1); continue; }
+            const int ui = atomicAdd(&sUndo, 1);
+            if (ui >= undoPer) { atomicExch(&sRollback, 1); continue; }
             const int v1 = p / 3, v2 = compRef(A.vnbr, v1, p - 3 * v1);
             int4 cs, vs;
-            if (!t1_flip(A, v1, v2, cs, vs, t1.undo + ui, t1.undoRings + (long)ui * 4 * A.Wc)) {
-                t1.undo[ui].v1 = -1;  // nothing was written
+            UndoEntry* u = undoB + ui;
+            if (!t1_flip(A, v1, v2, cs, vs, u, undoRingsB + (long)ui * 4 * A.Wc)) {
+                u->v1 = -1;  // nothing was written
                 continue;
             }
+            atomicAdd(&sFlips, 1);
             const int fc = atomicAdd(t1.flipCount, 1);
+            u->logIdx = fc;
             if (fc < t1.flipLogCap) {
                 int* e = t1.flipLog + 4 * fc;
                 e[0] = *t1.pass; e[1] = p; e[2] = v1; e[3] = v2;
             }
-            const int tc = atomicAdd(&nTouched, 4);
+            const int tc = atomicAdd(t1.ctr + 5, 4);
             if (tc + 4 <= t1.touchedCap) {
                 t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
+                atomicAdd(&nTouchedB, 4);
             } else {
-                atomicExch(t1.ctr + 3, 1);
+                atomicExch(&sRollback, 1);
             }
+            // re-test the 18 slots of the six vertices whose slots or positions the flip changed:
+            // all tests first (independent loads that overlap), then the flagging
             const int aff[6] = {v1, v2, vs.x, vs.y, vs.z, vs.w};
+            bool again[18];
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int sl = 0; sl < 3; ++sl) {
+                    const int r = 3 * aff[a] + sl;
+                    again[3 * a + sl] = r > p && r < qHi && t1_candidate(A, r);
+                }
             for (int a = 0; a < 6; ++a)
                 for (int sl = 0; sl < 3; ++sl) {
                     const int r = 3 * aff[a] + sl;
-                    if (r <= p || !t1_candidate(A, r)) continue;
+                    if (!again[3 * a + sl]) continue;
                     const unsigned bit = 1u << (r & 31);
                     if (!(atomicOr(t1.bits + (r >> 5), bit) & bit)) {
                         atomicOr(t1.summary + (r >> 10), 1u << ((r >> 5) & 31));
-                        const int ni = atomicAdd(t1.ctr + 1, 1);
-                        if (ni < t1.cap) nxt[ni] = r;
-                        else atomicExch(t1.ctr + 3, 1);
+                        const int ni = atomicAdd(&sNext, 1);
+                        if (ni < capB) nxt[ni] = r;
+                        else atomicExch(&sRollback, 1);
                     }
                 }
         }
         __syncthreads();
         // release this round's reservations
         for (int i = tid; i < nCur; i += blockDim.x) {
-            const int* f = t1.fp + (long)i * kFootprint;
+            const int* f = fpB + (long)i * kFootprint;
             for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
             for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
         }
         __syncthreads();
-        if (tid == 0) { nCur = min(*(volatile int*)(t1.ctr + 1), t1.cap); t1.ctr[1] = 0; }
+        if (tid == 0) { nCur = min(sNext, capB); sNext = 0; }
         int* t = cur; cur = nxt; nxt = t;
         __syncthreads();
-        if (*(volatile int*)(t1.ctr + 3)) break;
+        if (sRollback) rollback = true;
     }
     __syncthreads();
-    const bool rollback = *(volatile int*)(t1.ctr + 3) != 0;
     if (rollback) {
-        // release reservations still held (a break after the reserve phase)
-        for (int i = tid; i < nCur; i += blockDim.x) {
-            const int* f = t1.fp + (long)i * kFootprint;
-            for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
-            for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
-        }
         if (tid == 0) {
-            const int nu = min(*(volatile int*)(t1.ctr + 2), t1.undoCap);
-            for (int u = nu - 1; u >= 0; --u)
-                if (t1.undo[u].v1 >= 0) t1_undo(A, t1.undo[u], t1.undoRings + (long)u * 4 * A.Wc);
-            *t1.flipCount = flip0;
+            // undo this segment's flips, newest first, and invalidate their log entries
+            const int nu = min(sUndo, undoPer);
+            for (int i = nu - 1; i >= 0; --i) {
+                const UndoEntry& u = undoB[i];
+                if (u.v1 < 0) continue;
+                t1_undo(A, u, undoRingsB + (long)i * 4 * A.Wc);
+                if (u.logIdx >= 0 && u.logIdx < t1.flipLogCap) t1.flipLog[4 * u.logIdx] = -1;
+            }
         }
         __syncthreads();
-        for (int w = tid; w < t1.nWords; w += blockDim.x) t1.bits[w] = 0u;
-        for (int w = tid; w < t1.nSummary; w += blockDim.x) t1.summary[w] = 0u;
+        // the segment's flags back to the ones the test set: clear, then set the originals
+        for (int w = wLo + tid; w < wHi; w += blockDim.x) {
+            unsigned keep = 0u;  // bits of other segments in a shared boundary word
+            if (w == (qLo >> 5)) keep |= ~(~0u << (qLo & 31));
+            if (w == ((qHi - 1) >> 5) && (qHi & 31)) keep |= ~((1u << (qHi & 31)) - 1u);
+            atomicAnd(t1.bits + w, keep);
+        }
         __syncthreads();
         for (int i = tid; i < nOrig; i += blockDim.x) {
-            const int q = t1.listOrig[i];
+            const int q = orig[i];
             atomicOr(t1.bits + (q >> 5), 1u << (q & 31));
             atomicOr(t1.summary + (q >> 10), 1u << ((q >> 5) & 31));
         }
-    } else {
-        if (tid == 0) t1.ctr[5] = min(nTouched, t1.touchedCap);  // for k_t1_patch
-        // the bitmap is empty again; clear the summary words
-        for (int w = tid; w < t1.nSummary; w += blockDim.x) t1.summary[w] = 0u;
     }
     __syncthreads();
-    const int ne = min(*(volatile int*)(t1.ctr + 4), t1.cap);
+    const int ne = min(sExec, capB);
     for (int i = tid; i < ne; i += blockDim.x) {
-        const int* f = t1.comList + (long)i * kFootprint;
+        const int* f = comB + (long)i * kFootprint;
         for (int k = 0; k < 8; ++k) t1.comV[f[k]] = -1;
         for (int k = 8; k < kFootprint; ++k) t1.comC[f[k]] = -1;
     }
+    __shared__ bool amLast;
     if (tid == 0) {
-        t1.stats[1] += nOrig;
-        t1.stats[2] += ne;
-        t1.stats[4] += rounds;
-        if (rollback) t1.stats[5] += 1;
-        else { t1.stats[3] += *t1.flipCount - flip0; *t1.count = 0; }
+        atomicAdd(t1.stats + 1, nOrig);
+        atomicAdd(t1.stats + 2, ne);
+        atomicMax(t1.ctr + 6, rounds);
+        if (rollback) atomicAdd(t1.stats + 5, 1);
+        else {
+            atomicAdd(t1.stats + 3, sFlips);
+            atomicSub(t1.count, nOrig);
+        }
+        __threadfence();
+        amLast = atomicAdd(t1.ctr + 7, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!amLast) return;
+    if (tid == 0) t1.stats[4] += *(volatile int*)(t1.ctr + 6);
+    // summary bits of words that are now empty
+    for (int sw = tid; sw < t1.nSummary; sw += blockDim.x) {
+        unsigned sword = *(volatile unsigned*)(t1.summary + sw);
+        unsigned keep = sword;
+        while (sword) {
+            const int b = __ffs(sword) - 1;
+            sword &= sword - 1u;
+            const int w = sw * 32 + b;
+            if (w >= t1.nWords || *(volatile unsigned*)(t1.bits + w) == 0u) keep &= ~(1u << b);
+        }
+        t1.summary[sw] = keep;
     }
 }
 
@@ -982,7 +1045,13 @@ int launch_geometry(svm_model* m) {
 
 int launch_t1_apply(svm_model* m, int bump) {
     PhaseTimer pt(m, SVM_PHASE_T1APPLY, 3);
-    k_t1_parallel<<<1, kParThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
+    // touched-cell count (ctr[5]), per-pass round maximum (ctr[6]) and block ticket (ctr[7])
+    if (cudaMemsetAsync(m->t1.ctr + 5, 0, 3 * sizeof(int), m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    const bool batch = m->nRep > 1;
+    const int nSeg = batch ? m->nRep : 1;
+    k_t1_parallel<<<nSeg, batch ? kParThreadsBatch : kParThreads, 0, m->stream>>>(
+        apply_args(m, bump), m->t1, batch ? m->repVertOff : nullptr, batch ? kListPadBatch : kListPad,
+        m->t1.undoCap / nSeg);
     k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
     k_t1_patch<<<2 * 152, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
     return check_launch();
@@ -1148,8 +1217,8 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     m->t1.nSummary = (m->t1.nWords + 31) / 32;
     m->t1.flipLogCap = 1 << 16;
     m->t1.touchedCap = 4 * 65536;
-    m->t1.cap = (int)(3 * nV / 2 + 1024);
-    m->t1.undoCap = 65536;
+    m->t1.cap = (int)(3 * nV / 2 + (nRep > 1 ? svm::kListPadBatch * (size_t)nRep : svm::kListPad));
+    m->t1.undoCap = std::max(65536, 256 * nRep);
     alloc((void**)&m->t1.bits, (size_t)m->t1.nSummary * 32 * sizeof(unsigned));
     alloc((void**)&m->t1.summary, (size_t)m->t1.nSummary * sizeof(unsigned));
     alloc((void**)&m->t1.count, sizeof(int));
@@ -1173,6 +1242,7 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->repR, nRep * sizeof(double));
     alloc((void**)&m->repNp, nRep * sizeof(float));
     alloc((void**)&m->repCellOff, (nRep + 1) * sizeof(int));
+    alloc((void**)&m->repVertOff, (nRep + 1) * sizeof(int));
     alloc((void**)&m->repFlag, nRep * sizeof(int));
     alloc((void**)&m->repScal, 3 * nRep * sizeof(double));
     if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
@@ -1202,6 +1272,7 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
                     m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->dap32, m->repR, m->repNp, m->repCellOff,
+                    m->repVertOff,
                     m->repFlag, m->repScal};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
@@ -1267,6 +1338,8 @@ int svm_model_set_topology(svm_model* m, const double* vp, const int* rings, int
     SVM_CUDA(cudaMemcpyAsync(m->ringCount, cnt.data(), sizeof(int) * nC, cudaMemcpyHostToDevice, m->stream));
     SVM_CUDA(cudaMemcpyAsync(m->vcell, vcell.data(), sizeof(int4) * nV, cudaMemcpyHostToDevice, m->stream));
     SVM_CUDA(cudaMemcpyAsync(m->vnbr, vnbr.data(), sizeof(int4) * nV, cudaMemcpyHostToDevice, m->stream));
+    // a new state: status bits of the old one no longer apply, and this upload's checks set their own
+    SVM_CUDA(cudaMemsetAsync(m->status, 0, sizeof(int), m->stream));
     k_ring_index<<<svm::blocksFor(nC), svm::kBlock, 0, m->stream>>>(m->ring, m->ringCount, Wc, nC, m->vcell, m->vlast,
                                                                     m->vnext, m->vrpos, m->status);
     if (svm::check_launch()) return SVM_ERR_CUDA;
@@ -1474,11 +1547,14 @@ int svm_model_take_flips(svm_model* m, int* pairs, int cap, int* count) {
     if (pairs && k > 0) {
         std::vector<int4> e(k);
         SVM_CUDA(cudaMemcpy(e.data(), m->t1.flipLog, sizeof(int4) * k, cudaMemcpyDeviceToHost));
+        // entries of a rolled-back parallel pass carry pass -1 (the flips were undone and replayed)
+        e.erase(std::remove_if(e.begin(), e.end(), [](const int4& a) { return a.x < 0; }), e.end());
         // the CPU order: pass by pass, ascending edge position within a pass
         std::stable_sort(e.begin(), e.end(), [](const int4& a, const int4& b) {
             return a.x != b.x ? a.x < b.x : a.y < b.y;
         });
-        for (int i = 0; i < std::min(k, cap); ++i) { pairs[2 * i] = e[i].z; pairs[2 * i + 1] = e[i].w; }
+        *count = (int)e.size() + (n - k);
+        for (int i = 0; i < std::min((int)e.size(), cap); ++i) { pairs[2 * i] = e[i].z; pairs[2 * i + 1] = e[i].w; }
     }
     SVM_CUDA(cudaMemset(m->t1.flipCount, 0, sizeof(int)));
     return SVM_OK;

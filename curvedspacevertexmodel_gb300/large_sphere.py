@@ -76,7 +76,7 @@ def main():
     e0 = ws.energy(m)
     it, secs, fmax = fire(m, 1e-8, args.fire_cap)
     out["fire_plain"] = {"iterations": it, "seconds": secs, "max_force": fmax, "energy_per_cell": ws.energy(m) / args.cells,
-                         "ms_per_iteration": 1e3 * secs / max(1, it)}
+                         "ms_per_iteration": 1e3 * secs / max(1, it), "device_status": m.deviceStatus()}
     m.loadState(start)
     net = ws.load(os.path.join(os.path.dirname(__file__), "data", "warm_start_n20k.npz"))
     m.synchronize()
@@ -93,7 +93,7 @@ def main():
     m.synchronize()
     out["fire_warm"] = {"iterations": it_w, "seconds": time.perf_counter() - t0, "max_force": fmax_w,
                         "energy_start": e0, "energy_after_warm_start": e_w, "fallback": fallback,
-                        "energy_per_cell": ws.energy(m) / args.cells}
+                        "energy_per_cell": ws.energy(m) / args.cells, "device_status": m.deviceStatus()}
     print(json.dumps(out), flush=True)
 
 
