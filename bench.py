@@ -15,8 +15,9 @@ start relaxes normally.  Timing starts after the stabilisation and an untimed eq
 
 ours: `value` is device-resident throughput over K steps, each timed with CUDA events on the
 model's stream after an L2 flush (the model state, ~40 MB, would otherwise stay in the 129 MB L2);
-`e2e` is the same step through the C ABI with host buffers: H2D of the positions from pinned host
-memory, the step, D2H of the positions and the energy.  Per-phase CUDA events taken during the
+`e2e` is the same step through the C ABI with host buffers (svm_brownian_step_io, one call per
+step): H2D of the positions from pinned host memory, the step, D2H of the positions and the
+energy, one synchronisation.  Per-phase CUDA events taken during the
 timed steps give the dominant kernel's launch duration for `roofline`.  `cpu_baseline` times the
 CPU oracle (restatement of the reference CPU path, one core as the reference's vertex-model loops
 are serial) on a bounded sample of the same workload from the same equilibrated state.
@@ -265,11 +266,8 @@ def run_ours(args):
         pg.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        _lib.call("svm_model_set_positions", model.handle, host_pos)
-        _lib.call("svm_brownian_step", model.handle, PARAMS["T"], PARAMS["dt"], PARAMS["mu"], _lib.SVM_NOISE_PHILOX,
-                  None, BD_SEED + rank)
-        _lib.call("svm_model_get_positions", model.handle, host_out)
-        _lib.call("svm_model_compute_energy", model.handle, C.byref(energy))
+        _lib.call("svm_brownian_step_io", model.handle, PARAMS["T"], PARAMS["dt"], PARAMS["mu"], BD_SEED + rank,
+                  host_pos, host_out, C.byref(energy))
         host_pos, host_out = host_out, host_pos
     e2e_s, e2e_value = job_throughput(pg, time.perf_counter() - t0, nv, args.steps, world)
 

@@ -100,6 +100,7 @@ SIGNATURES = {
     "svm_energy_noalloc": (i32, [vp, vp, f64, i32, vp, vp]),
     "svm_brownian_step": (i32, [vp, f64, f64, f64, i32, vp, u64]),
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
+    "svm_brownian_step_io": (i32, [vp, f64, f64, f64, u64, dp, dp, C.POINTER(f64)]),
     "svm_brownian_run": (i32, [vp, f64, f64, f64, u64, i32]),
     "svm_fire_create": (i32, [vp, f64, f64, f64, f64, f64, f64, i32, f64, f64, i32, pvp]),
     "svm_fire_destroy": (i32, [vp]),

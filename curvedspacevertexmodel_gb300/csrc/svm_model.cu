@@ -1613,6 +1613,47 @@ int svm_brownian_step(svm_model* m, double T, double dt, double mu, int mode, co
     return svm::bd_step(m, T, dt, mu, mode, noise, seed);
 }
 
+// One Brownian step with host input and output in a single stream sequence and one
+// synchronisation: positions H2D (optional), the step (Philox noise), the energy of the geometry
+// the step's forces used (what computeEnergy returns after a timestep, sphericalVertexModel.cpp:
+// 150-160) and the new positions D2H (optional).
+int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
+                         double* posOut, double* energyOut) {
+    if (!m) return SVM_ERR_ARG;
+    const bool mixedForm = m->precision == SVM_PRECISION_MIXED;
+    if (posIn) {
+        SVM_CUDA(cudaMemcpyAsync(m->dispBuf, posIn, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));
+        if (mixedForm) {
+            if (svm::mixed_upload_positions(m, m->dispBuf)) return SVM_ERR_CUDA;
+        } else {
+            k_aos_to_d4<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->dispBuf, m->pos[m->cur], m->nVertices);
+            if (svm::check_launch()) return SVM_ERR_CUDA;
+        }
+        m->cornersValid = false;
+    }
+    int rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+    if (rc) return rc;
+    if (energyOut) {
+        k_energy<<<svm::blocksFor(m->nCells), svm::kBlock, 0, m->stream>>>(m->ap, m->pref, m->Kr, m->nCells,
+                                                                             m->partials + m->maxPartialBlocks,
+                                                                             m->ticket + 1, m->scalars + 2);
+        if (svm::check_launch()) return SVM_ERR_CUDA;
+        SVM_CUDA(cudaMemcpyAsync(energyOut, m->scalars + 2, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    }
+    if (posOut) {
+        if (mixedForm) {
+            if (svm::mixed_download(m, m->pos32[m->cur], m->nVertices, m->dispBuf)) return SVM_ERR_CUDA;
+        } else {
+            k_d4_to_aos<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->dispBuf,
+                                                                                    m->nVertices);
+            if (svm::check_launch()) return SVM_ERR_CUDA;
+        }
+        SVM_CUDA(cudaMemcpyAsync(posOut, m->dispBuf, sizeof(double) * 3 * m->nVertices, cudaMemcpyDeviceToHost, m->stream));
+    }
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
 int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, const double* noise) {
     if (!m || !noise) return SVM_ERR_ARG;
     SVM_CUDA(cudaMemcpyAsync(m->noiseBuf, noise, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));

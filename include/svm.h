@@ -204,6 +204,13 @@ int svm_brownian_step(svm_model* m, double T, double dt, double mu, int noiseMod
                       uint64_t seed);
 /* Same with host-supplied standard normals (copied on the model's stream). */
 int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, const double* noise);
+/* One timestep with Philox noise and host buffers, in one stream sequence with one
+ * synchronisation: positions[3 nV] uploaded from posIn (NULL: keep the device state), the step,
+ * *energyOut = the energy of the geometry the step's forces used (what svm_model_compute_energy
+ * returns after a step; computeEnergy, sphericalVertexModel.cpp:150-160), and the new positions
+ * copied to posOut (NULL: none).  Pinned host buffers make the copies asynchronous DMA. */
+int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
+                         double* posOut, double* energyOut);
 /* nSteps timesteps with Philox noise, launched as a captured CUDA graph. */
 int svm_brownian_run(svm_model* m, double T, double dt, double mu, uint64_t seed, int nSteps);
 

@@ -367,3 +367,22 @@ def test_fire_outliving_its_model(svm, gold):
     with pytest.raises(svm.SVMError):
         fire.minimize()
     del fire
+
+
+def test_host_io_step_equals_the_call_sequence(svm, gold):
+    """svm_brownian_step_io (positions in, step, energy and positions out, one synchronisation)
+    gives bit for bit what set_positions + brownian_step + compute_energy + get_positions give."""
+    import ctypes as C
+    from curvedspacevertexmodel_gb300 import _lib
+    a, b = gpu_model(svm, gold), gpu_model(svm, gold)
+    pos = a.returnPositions()
+    pos[0] *= 1.0 + 1e-9
+    out = np.empty(3 * a.nVertices)
+    e_io = C.c_double()
+    _lib.call("svm_brownian_step_io", a.handle, 0.01, 0.01, 1.0, 99, np.ascontiguousarray(pos).reshape(-1), out,
+              C.byref(e_io))
+    b.setPositions(pos)
+    _lib.call("svm_brownian_step", b.handle, 0.01, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, 99)
+    e_seq = b.computeEnergy()
+    assert np.array_equal(out.reshape(-1, 3), b.returnPositions())
+    assert e_io.value == e_seq
