@@ -22,6 +22,7 @@
 // block order, so gradients are deterministic.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <random>
 #include <vector>
@@ -324,13 +325,15 @@ static int mlp_grad(svm_mlp* M, const float* X, const float* Y, const int* order
     const int blocks = (count + kTB - 1) / kTB;
     int rc = mlp_reserve(M, blocks);
     if (rc) return rc;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_train_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()) !=
-            cudaSuccess)
-            return SVM_ERR_CUDA;
-        attr = true;
-    }
+    // the training kernel's shared memory exceeds the default 48 KB: opt in (per device)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SVM_ERR_CUDA;
+    static std::once_flag once[64];
+    static cudaError_t attrErr[64];
+    std::call_once(once[dev], [&] {
+        attrErr[dev] = cudaFuncSetAttribute(k_train_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem());
+    });
+    if (attrErr[dev] != cudaSuccess) return SVM_ERR_CUDA;
     k_train_block<<<blocks, kTB, train_smem(), M->stream>>>(M->wb, X, Y, order, first, count, invBatch, M->partials,
                                                           M->lossPartials);
     k_reduce_grad<<<(kParams + 255) / 256, 256, 0, M->stream>>>(M->partials, blocks, M->g, M->lossPartials, M->loss);
