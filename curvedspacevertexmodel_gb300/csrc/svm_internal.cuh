@@ -24,6 +24,8 @@
 namespace svm {
 
 constexpr double kPI = 3.141592653589793115997963468544185161590576171875;
+// pi - kPI (the next term of pi's double-double expansion)
+constexpr double kPILo = 1.2246467991473532e-16;
 
 struct D3 { double x, y, z; };
 

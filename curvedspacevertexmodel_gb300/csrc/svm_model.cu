@@ -14,6 +14,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 #include "svm_internal.cuh"
 #include "svm_force.cuh"
 #include "svm_hull.h"
@@ -184,6 +185,11 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
             k = (k + 1 == n) ? 0 : k + 1;
         }
         area = __dsub_rn(ang, __dmul_rn((double)(n - 2), kPI));
+        // The mixed form also subtracts (n - 2) times the part of pi below the double kPI: the
+        // reference's excess is biased by +(n - 2)(pi - kPI) per cell, which over a sphere sums to
+        // ~4N (pi - kPI) R^2 (4e-7 at N = 100k, 4e-5 at N = 1M) and trips its absolute 1e-6 area
+        // check by itself at large N.  The FP64 form keeps the reference's arithmetic.
+        if (std::is_same<PT, float4>::value) area = __dsub_rn(area, __dmul_rn((double)(n - 2), kPILo));
         const int extra = (int)floor(area / (1.0 * kPI));
         if (extra > 0) area = __dsub_rn(area, __dmul_rn((double)extra, kPI));
         area = __dmul_rn(__dmul_rn(area, R), R);

@@ -3,7 +3,8 @@
     python -m curvedspacevertexmodel_gb300.profile_case --cells 1000000 --stab 2 --steps 1
 
 Builds a model of N cells from the seeded recipe, runs `stab` stabilisation steps (T = 0, P0 = 1,
-as the reference driver does) and then `steps` Brownian steps at T = 0.01, P0 = 3.8, dt = 0.01
+as the reference driver does), `equil` graph-replayed steps at the run parameters, and then
+`steps` Brownian steps at T = 0.01, P0 = 3.8, dt = 0.01
 (T1 threshold 0.04), one launch per kernel per step (no graph), and prints the energy per cell.
 With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*); with --replicas R
 a batch of R replicas runs instead (stabilisation, then `steps` steps at per-replica P0 and T).
@@ -21,6 +22,8 @@ def main():
     ap.add_argument("--cells", type=int, default=1_000_000)
     ap.add_argument("--stab", type=int, default=2)
     ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--equil", type=int, default=0,
+                    help="graph-replayed steps at the run parameters (FP64) before the profiled steps")
     ap.add_argument("--seed", type=int, default=1137)
     ap.add_argument("--mixed", action="store_true", help="run the timed steps in the mixed-precision form")
     ap.add_argument("--replicas", type=int, default=0,
@@ -61,6 +64,8 @@ def main():
         bd.integrateEquationOfMotion()
     bd.setT(0.01)
     m.setPreferredParameters(1.0, 3.8)
+    if args.equil:
+        bd.run(args.equil)
     if args.mixed:
         m.precision = "mixed"
     for _ in range(args.steps):

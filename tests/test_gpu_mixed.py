@@ -36,6 +36,10 @@ def svm(svm_lib):
     return svm_lib
 
 
+def counts_of(m):
+    return m.rings()[1].astype(np.float64)
+
+
 @pytest.fixture(scope="module")
 def state20k(svm):
     m, bd = stabilised(svm, 20000)
@@ -55,8 +59,10 @@ def test_same_state_evaluation_matches_fp64(svm, state20k):
     m.computeForces()
     ap32, f32, e32, cp32 = m.areaPerimeter(), m.returnForces(), m.computeEnergy(), m.cellPositions()
     m.precision = "fp64"
-    # areas: FP64 included angles of the same positions, summed in the same order
-    assert rel_err(ap32[:, 0], ap64[:, 0]) < 1e-13
+    # areas: FP64 included angles of the same positions, summed in the same order; the mixed form
+    # also removes the reference's (n - 2)(pi - kPI) R^2 rounding bias per cell (~1e-12 here)
+    bias = (counts_of(m) - 2) * 1.2246467991473532e-16 * m.radius ** 2
+    assert np.max(np.abs(ap64[:, 0] - ap32[:, 0] - bias)) < 1e-13 * np.max(ap64[:, 0])
     per = np.abs(ap32[:, 1] - ap64[:, 1]) / ap64[:, 1]
     assert per.max() < RTOL_PERIMETER
     assert abs(e32 - e64) / e64 < 1e-5
