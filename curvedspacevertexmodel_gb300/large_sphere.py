@@ -68,9 +68,13 @@ def main():
     dt = time.perf_counter() - t0
     t1 = m.t1Stats()
     out["brownian"] = {"ms_per_step": 1e3 * dt / args.steps, "vertex_steps_per_s": m.nVertices * args.steps / dt,
-                       "t1_flips_per_step": t1["flips"] / args.steps, "device_status": m.deviceStatus()}
+                       "t1_flips_per_step": t1["flips"] / args.steps, "device_status": m.deviceStatus(),
+                       "area_fallback_taken_last_step": bool(m.areaCheck()[2])}
     m.computeGeometry()
     out["brownian"]["energy_per_cell"] = m.computeEnergy() / args.cells
+    if args.fire_cap <= 0:
+        print(json.dumps(out), flush=True)
+        return
     m.precision = "fp64_vector"
     start = m.saveState()
     e0 = ws.energy(m)

@@ -61,8 +61,11 @@ def test_same_state_evaluation_matches_fp64(svm, state20k):
     m.precision = "fp64"
     # areas: FP64 included angles of the same positions, summed in the same order; the mixed form
     # also removes the reference's (n - 2)(pi - kPI) R^2 rounding bias per cell (~1e-12 here)
+    # (the few-ulp-of-an-angle differences left come from the mixed form's clamped cosine path)
     bias = (counts_of(m) - 2) * 1.2246467991473532e-16 * m.radius ** 2
-    assert np.max(np.abs(ap64[:, 0] - ap32[:, 0] - bias)) < 1e-13 * np.max(ap64[:, 0])
+    resid = np.abs(ap64[:, 0] - ap32[:, 0] - bias)
+    ulp_angle = 4.4e-16  # of an angle ~2 rad
+    assert np.median(resid) < 1e-15 and resid.max() < 4 * ulp_angle * m.radius ** 2
     per = np.abs(ap32[:, 1] - ap64[:, 1]) / ap64[:, 1]
     assert per.max() < RTOL_PERIMETER
     assert abs(e32 - e64) / e64 < 1e-5
