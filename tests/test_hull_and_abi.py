@@ -133,3 +133,30 @@ def test_oracle_topology_matches_product(svm, oracle_mod):
     assert np.array_equal(t["counts"], topo.ringCounts)
     assert np.array_equal(t["vcells"], topo.vertexCells)
     assert np.array_equal(t["vnbrs"], topo.vertexNeighbors)
+
+
+def test_abi_rejects_bad_arguments_without_a_device(svm):
+    """Argument checks come before any device work: invalid sizes, null handles and pointers
+    return SVM_ERR_ARG (no exception crosses the ABI, nothing touches a GPU)."""
+    import ctypes as C
+    L = svm.lib()
+    h = C.c_void_p()
+    ERR_ARG = 1
+    assert L.svm_model_create(3, 2, 16, 1.0, None, C.byref(h)) == ERR_ARG          # N < 4
+    assert L.svm_model_create(100, 197, 16, 1.0, None, C.byref(h)) == ERR_ARG      # Nv != 2N - 4
+    assert L.svm_model_create(100, 196, 2, 1.0, None, C.byref(h)) == ERR_ARG       # ring capacity
+    assert L.svm_model_create(100, 196, 16, -1.0, None, C.byref(h)) == ERR_ARG     # radius
+    n = np.array([100, 3], dtype=np.int32)
+    nv = np.array([196, 2], dtype=np.int32)
+    r = np.array([1.0, 1.0])
+    assert L.svm_batch_create(2, n, nv, 16, r, None, C.byref(h)) == ERR_ARG         # a replica with N < 4
+    assert L.svm_batch_create(0, n, nv, 16, r, None, C.byref(h)) == ERR_ARG
+    for fn in ("svm_model_compute_geometry", "svm_model_compute_forces", "svm_model_enforce_topology",
+               "svm_model_destroy", "svm_fire_destroy", "svm_mlp_destroy", "svm_tuner_destroy"):
+        assert getattr(L, fn)(None) == ERR_ARG, fn
+    assert L.svm_model_set_precision(None, 1) == ERR_ARG
+    assert L.svm_brownian_step_io(None, 0.0, 0.01, 1.0, 1, None, None, None) == ERR_ARG
+    assert L.svm_energy_noalloc(None, None, 1.0, 10, None, None) == ERR_ARG
+    cnt = C.c_int()
+    assert L.svm_mlp_parameter_count(C.byref(cnt)) == 0 and cnt.value == 24 * 64 + 64 + 64 * 64 + 64 + 2 * 64 + 2
+    assert L.svm_status_string(ERR_ARG) and L.svm_status_string(999)
