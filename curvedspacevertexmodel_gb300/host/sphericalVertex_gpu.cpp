@@ -1,16 +1,51 @@
 // The reference's Brownian driver (sphericalVertex.cpp:86-138) written against svm.hpp:
 // build a model from a seed, equilibrate at T = 0 with p0 = 1, then run at (T, p0), printing the
 // energy and the timing.  Usage: sphericalVertex_gpu [N cells] [iterations] [T] [p0] [dt] [seed]
+//
+// With "batch" as the first argument it runs replicas of sizes N, 2N, 3N (seeds seed, seed+1,
+// seed+2; temperatures T, 2T, 3T) as one sphericalVertexModelBatch and prints each replica's
+// energy:  sphericalVertex_gpu batch [N] [iterations] [T] [p0] [dt] [seed]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
+#include <string>
+#include <vector>
 
 #include "svm.hpp"
 
 using namespace svmgpu;
 
+static int run_batch(int argc, char** argv) {
+    const int N = argc > 2 ? std::atoi(argv[2]) : 200;
+    const int iterations = argc > 3 ? std::atoi(argv[3]) : 100;
+    const double T = argc > 4 ? std::atof(argv[4]) : 0.01;
+    const double p0 = argc > 5 ? std::atof(argv[5]) : 3.8;
+    const double dt = argc > 6 ? std::atof(argv[6]) : 0.01;
+    const int seed = argc > 7 ? std::atoi(argv[7]) : 1137;
+    try {
+        auto batch = std::make_shared<sphericalVertexModelBatch>(std::vector<int>{N, 2 * N, 3 * N},
+                                                                 std::vector<int>{seed, seed + 1, seed + 2}, 1.0, p0);
+        batch->setT1Threshold(0.04);
+        auto BD = std::make_shared<brownianDynamics>(true);
+        BD->noise.setReproducibleSeed(seed + 7);
+        BD->setModel(batch);
+        BD->setDeltaT(dt);
+        batch->setTemperatures({T, 2 * T, 3 * T});
+        for (int i = 0; i < iterations; ++i) BD->performUpdate();
+        batch->computeGeometry();
+        const std::vector<double> e = batch->replicaEnergies();
+        std::printf("{\"replicas\": %d, \"vertices\": %d, \"energies\": [%.17g, %.17g, %.17g]}\n", batch->nReplicas,
+                    batch->getNumberOfParticles(), e[0], e[1], e[2]);
+    } catch (const std::exception& ex) {
+        std::fprintf(stderr, "error: %s\n", ex.what());
+        return 1;
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc > 1 && std::string(argv[1]) == "batch") return run_batch(argc, argv);
     const int N = argc > 1 ? std::atoi(argv[1]) : 200;
     const int iterations = argc > 2 ? std::atoi(argv[2]) : 100;
     const double T = argc > 3 ? std::atof(argv[3]) : 0.01;

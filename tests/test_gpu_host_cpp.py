@@ -43,3 +43,24 @@ def test_cpp_driver_matches_python_classes(svm):
     m.computeGeometry()
     assert cpp["vertices"] == m.nVertices
     assert cpp["energy"] == m.computeEnergy()
+
+
+def test_cpp_batch_matches_python_batch(svm):
+    exe = os.path.join(os.path.dirname(svm.__file__), "sphericalVertex_gpu")
+    N, steps, T, p0, dt, seed = 150, 40, 0.01, 3.7, 0.01, 21
+    out = subprocess.run([exe, "batch", str(N), str(steps), str(T), str(p0), str(dt), str(seed)], capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    cpp = json.loads(out.stdout.strip().splitlines()[-1])
+    b = svm.sphericalVertexModelBatch([N, 2 * N, 3 * N], [seed, seed + 1, seed + 2], p0=p0)
+    b.setT1Threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(b)
+    bd.noise.setReproducibleSeed(seed + 7)
+    bd.setDeltaT(dt)
+    b.setTemperatures([T, 2 * T, 3 * T])
+    for _ in range(steps):
+        bd.integrateEquationOfMotion()
+    b.computeGeometry()
+    assert cpp["vertices"] == b.nVertices
+    assert cpp["energies"] == list(b.replicaEnergies())
