@@ -105,16 +105,23 @@ __global__ void k_fire_consume(FireState* S) {
     if (!S->done) S->pending = 0;
 }
 
-__global__ void k_fire_force(ForceArgs A, FireState* __restrict__ Sp, int nV, double4_32a* __restrict__ force,
-                             double4_32a* __restrict__ vel, double* __restrict__ partials, unsigned* __restrict__ ticket) {
+// Blocks of 3 kSlotVerts threads: three per vertex for the force (one per cell slot), then the
+// first kSlotVerts threads finish their vertex.
+__global__ void __launch_bounds__(3 * kSlotVerts) k_fire_force(ForceArgs A, FireState* __restrict__ Sp, int nV,
+                                                               double4_32a* __restrict__ force,
+                                                               double4_32a* __restrict__ vel,
+                                                               double* __restrict__ partials,
+                                                               unsigned* __restrict__ ticket) {
     __shared__ double sh[32];
     __shared__ bool amLast;
+    __shared__ SlotShared slots;
     if (Sp->done) return;
     const double dt = Sp->dt;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const D3 fv = block_slot_force(A, nV, slots);
+    const int i = blockIdx.x * kSlotVerts + threadIdx.x;
     double P = 0.0, FF = 0.0, VV = 0.0;
-    if (i < nV) {
-        const D3 f = vertex_force(A, i);
+    if (threadIdx.x < kSlotVerts && i < nV) {
+        const D3 f = fv;
         st3(force, i, f);
         const double hv = (0.5 / 1.0) * dt;
         D3 v = ld3(vel, i);
@@ -201,7 +208,8 @@ int fire_iteration(svm_fire* F) {
     rc = launch_geometry(m);
     if (rc) return rc;
     PhaseTimer pt(m, SVM_PHASE_FORCE);
-    k_fire_force<<<nb, kB, 0, m->stream>>>(fargs(m), F->d, m->nVertices, m->force, m->vel, F->partials, F->ticket);
+    k_fire_force<<<(m->nVertices + kSlotVerts - 1) / kSlotVerts, 3 * kSlotVerts, 0, m->stream>>>(
+        fargs(m), F->d, m->nVertices, m->force, m->vel, F->partials, F->ticket);
     return check_launch();
 }
 
@@ -224,7 +232,7 @@ int svm_fire_create(svm_model* m, double dt, double alphaStart, double dtMax, do
     S.dt = dt; S.dtMin = dt * .01; S.alphaStart = alphaStart; S.alpha = alphaStart; S.dtMax = dtMax;
     S.dtInc = dtInc; S.dtDec = dtDec; S.alphaDec = alphaDec; S.nMin = nMin; S.cutoff = forceCutoff;
     S.alphaMin = alphaMin; S.maxIterations = maxIterations; S.rmsOverN = 100.; S.maxForce = 100.;
-    F->nBlocks = (m->nVertices + kB - 1) / kB;
+    F->nBlocks = (m->nVertices + kSlotVerts - 1) / kSlotVerts;  // blocks of k_fire_force
     bool ok = cudaMalloc(&F->d, sizeof(FireState)) == cudaSuccess &&
               cudaMalloc(&F->partials, sizeof(double) * 4 * (F->nBlocks + 1)) == cudaSuccess &&
               cudaMalloc(&F->ticket, sizeof(unsigned)) == cudaSuccess;

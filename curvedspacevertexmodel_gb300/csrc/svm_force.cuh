@@ -108,6 +108,71 @@ __device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
     return f;
 }
 
+// The contribution of cell slot s to the force on vertex v: one term of vertex_force's (or
+// vertex_force_vec's) sum, with the same operations, so that summing the three terms in slot order
+// and skipping a NaN term, as those functions do, gives the same force bit for bit.  Lets three
+// threads share a vertex (more warps in flight when the vertex count is small).
+__device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s) {
+    const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
+    const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
+    if (A.vec) {
+        const D3 P = ld3(A.pos, v);
+        const double inv = 1.0 / sqrt(dot3(P, P));
+        const D3 a = scl3(inv, P);
+        const D3 dc = sub3(ld3(A.cellPos, c), P);
+        const D3 dl = sub3(ld3(A.pos, L), P), dx = sub3(ld3(A.pos, X), P);
+        const double2 apc = A.ap[c], pr = A.pref[c];
+        const double pp = 2.0 * (apc.y - pr.y), aa = 2.0 * A.Kr * (apc.x - pr.x);
+        const D3 bl = scl3(inv, dl), bc = scl3(inv, dc), bx = scl3(inv, dx);
+        return add3(scl3(-pp, add3(grad_geo_vec(a, dl), grad_geo_vec(a, dx))),
+                    scl3(-aa, add3(grad_tri_vec(a, bl, bc, A.R), grad_tri_vec(a, bc, bx, A.R))));
+    }
+    const D3 p = ld3(A.pos, v);
+    const double4_32a sv = A.vsph[v];
+    const D3 cp = ld3(A.cellPos, c);
+    const double4_32a sc = A.cellSph[c];
+    const double2 apc = A.ap[c], pr = A.pref[c];
+    const double dA = apc.x - pr.x, dP = apc.y - pr.y;
+    const D3 pl = ld3(A.pos, L), px = ld3(A.pos, X);
+    const double4_32a sl = A.vsph[L], sx = A.vsph[X];
+    const double pp = 2.0 * dP;
+    const double aa = 2.0 * A.Kr * dA;
+    D3 fs{0.0, 0.0, 0.0}, t;
+    t = from_basis(sv, grad_geodesic(sv, sl));
+    fs = sub3(fs, scl3(pp, t));
+    t = from_basis(sv, grad_geodesic(sv, sx));
+    fs = sub3(fs, scl3(pp, t));
+    t = from_basis(sv, grad_triangle(sv, sl, sc, p, pl, cp, A.R));
+    fs = sub3(fs, scl3(aa, t));
+    t = from_basis(sv, grad_triangle(sv, sc, sx, p, cp, px, A.R));
+    fs = sub3(fs, scl3(aa, t));
+    return fs;
+}
+
+// Block-level force of kSlotVerts vertices by 3 kSlotVerts threads (thread 3 i + s computes slot s
+// of vertex i of the block); threads i < kSlotVerts receive vertex i's force in slot order.
+constexpr int kSlotVerts = 64;
+struct SlotShared { double x[3 * kSlotVerts], y[3 * kSlotVerts], z[3 * kSlotVerts]; };
+__device__ __forceinline__ D3 block_slot_force(const ForceArgs& A, int nV, SlotShared& sh) {
+    const int t = threadIdx.x, base = blockIdx.x * kSlotVerts;
+    const int vi = t / 3, s = t - 3 * (t / 3);
+    const int v = base + vi;
+    if (v < nV) {
+        const D3 fs = slot_force(A, v, s);
+        sh.x[t] = fs.x; sh.y[t] = fs.y; sh.z[t] = fs.z;
+    }
+    __syncthreads();
+    D3 f{0.0, 0.0, 0.0};
+    if (t < kSlotVerts && base + t < nV) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const D3 fs{sh.x[3 * t + q], sh.y[3 * t + q], sh.z[3 * t + q]};
+            if (!isnan(fs.x)) f = add3(f, fs);
+        }
+    }
+    return f;
+}
+
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11): ten rounds of two 32x32->64 multiplies with a Weyl-sequence key schedule.
 __device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {

@@ -13,22 +13,26 @@ int check_launch();
 namespace {
 using namespace svm;
 
-constexpr int kFB = 256;
-
-__global__ void k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    st3(force, v, vertex_force(A, v));
+// Blocks of 3 kSlotVerts threads, three per vertex (one per cell slot), kSlotVerts vertices each.
+__global__ void __launch_bounds__(3 * kSlotVerts) k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
+    __shared__ SlotShared sh;
+    const D3 f = block_slot_force(A, nV, sh);
+    const int v = blockIdx.x * kSlotVerts + threadIdx.x;
+    if (threadIdx.x >= kSlotVerts || v >= nV) return;
+    st3(force, v, f);
 }
 
 // Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
 template <int kNoise>
-__global__ void k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force, double4_32a* __restrict__ posNext,
-                           const double* __restrict__ noise, uint64_t seed,
-                           const unsigned long long* __restrict__ stepCounter, double np, double fp) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    const D3 f = vertex_force(A, v);
+__global__ void __launch_bounds__(3 * kSlotVerts) k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force,
+                                                             double4_32a* __restrict__ posNext,
+                                                             const double* __restrict__ noise, uint64_t seed,
+                                                             const unsigned long long* __restrict__ stepCounter,
+                                                             double np, double fp) {
+    __shared__ SlotShared sh;
+    const D3 f = block_slot_force(A, nV, sh);
+    const int v = blockIdx.x * kSlotVerts + threadIdx.x;
+    if (threadIdx.x >= kSlotVerts || v >= nV) return;
     st3(force, v, f);
     D3 xi;
     if (kNoise == SVM_NOISE_BUFFER) xi = D3{noise[3 * v], noise[3 * v + 1], noise[3 * v + 2]};
@@ -42,19 +46,20 @@ __global__ void k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force,
 namespace svm {
 
 int launch_force_fp64(svm_model* m) {
-    k_force<<<(m->nVertices + kFB - 1) / kFB, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force);
+    const int nb = (m->nVertices + kSlotVerts - 1) / kSlotVerts;
+    k_force<<<nb, 3 * kSlotVerts, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force);
     return check_launch();
 }
 
 int launch_force_bd_fp64(svm_model* m, double np, double fp, int noiseMode, const double* noise, uint64_t seed,
                          int nxt) {
-    const int nb = (m->nVertices + kFB - 1) / kFB;
+    const int nb = (m->nVertices + kSlotVerts - 1) / kSlotVerts;
     if (noiseMode == SVM_NOISE_BUFFER)
-        k_force_bd<SVM_NOISE_BUFFER><<<nb, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force,
-                                                               m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+        k_force_bd<SVM_NOISE_BUFFER><<<nb, 3 * kSlotVerts, 0, m->stream>>>(
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     else
-        k_force_bd<SVM_NOISE_PHILOX><<<nb, kFB, 0, m->stream>>>(force_args(m, m->cur), m->nVertices, m->force,
-                                                               m->pos[nxt], noise, seed, m->stepCounter, np, fp);
+        k_force_bd<SVM_NOISE_PHILOX><<<nb, 3 * kSlotVerts, 0, m->stream>>>(
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp);
     return check_launch();
 }
 

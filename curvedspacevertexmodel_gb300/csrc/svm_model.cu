@@ -100,7 +100,8 @@ __device__ double block_sum(double v) {
 // predecessor and the included angle at the vertex (the per-corner terms of
 // computeGeometryCPU, sphericalVertexModel.cpp:257-276).  With `t1test`, also marks every edge
 // (v, u), v < u, shorter than the T1 threshold (sphericalVertexModel.cpp:469-481).
-__global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph,
+// One thread per vertex (large vertex counts: keeps each vertex's shared values in registers).
+__global__ void k_corners_v(const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph,
                           const int4* __restrict__ vcell, const int4* __restrict__ vlast,
                           const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
                           const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV,
@@ -148,6 +149,66 @@ __global__ void k_corners(const double4_32a* __restrict__ pos, double4_32a* __re
             }
         }
     }
+}
+
+// Blocks of 3 kCornerVerts threads, three per vertex (small vertex counts, where one thread per
+// vertex leaves the FP64 pipe short of warps): thread (v, j) first evaluates the vertex's
+// neighbour j (its position, p x u_j with its norm, the arc, and the T1 test of that edge), then,
+// after a block barrier, the corner of cell slot j from the neighbours' values in shared memory.
+constexpr int kCornerVerts = 64;
+constexpr int kCornerSlotsBelow = 100000;  // vertices
+struct CornerShared {
+    double cx[3 * kCornerVerts], cy[3 * kCornerVerts], cz[3 * kCornerVerts], n[3 * kCornerVerts];
+    double ux[3 * kCornerVerts], uy[3 * kCornerVerts], uz[3 * kCornerVerts], arc[3 * kCornerVerts];
+};
+
+__global__ void __launch_bounds__(3 * kCornerVerts) k_corners_s(
+    const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph, const int4* __restrict__ vcell,
+    const int4* __restrict__ vlast, const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
+    const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV, double R, int t1test,
+    double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
+    __shared__ CornerShared sh;
+    const int t = threadIdx.x, vi = t / 3, j = t - 3 * (t / 3), b = 3 * vi;
+    const int v = blockIdx.x * kCornerVerts + vi;
+    const bool live = v < nV;
+    D3 p{0.0, 0.0, 0.0};
+    int4 nb = make_int4(0, 0, 0, 0);
+    if (live) {
+        p = ld3(pos, v);
+        if (j == 0) vsph[v] = sph_coords(p);
+        nb = vnbr[v];
+        // neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v in
+        // its three cells are its three neighbours, as are the successors)
+        const int u = comp(nb, j);
+        const D3 U = ld3(pos, u);
+        const D3 C = cross3(p, U);
+        const double arc = geodesic(U, p, R);
+        sh.cx[t] = C.x; sh.cy[t] = C.y; sh.cz[t] = C.z; sh.n[t] = sqrt(dot3(C, C));
+        sh.ux[t] = U.x; sh.uy[t] = U.y; sh.uz[t] = U.z; sh.arc[t] = arc;
+        // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475); `arc` is that
+        // geodesic, bitwise (its cosine's products commute exactly)
+        if (t1test && v < u && arc < t1Threshold) {
+            const int q = 3 * v + j;
+            atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
+            atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
+            atomicAdd(t1.count, 1);
+        }
+    }
+    __syncthreads();
+    if (!live) return;
+    const int s = j;
+    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
+    const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
+    double2 cr;
+    if (jl >= 0 && jx >= 0) {
+        const int l = b + jl, x = b + jx;
+        cr = make_double2(sh.arc[l], included_angle_pre(D3{sh.cx[x], sh.cy[x], sh.cz[x]}, D3{sh.cx[l], sh.cy[l], sh.cz[l]},
+                                                        sh.n[x], sh.n[l], D3{sh.ux[l], sh.uy[l], sh.uz[l]}));
+    } else {  // inconsistent lists: evaluate directly
+        const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
+        cr = make_double2(geodesic(pl, p, R), included_angle(pl, p, px));
+    }
+    corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
 }
 
 // Per cell: centroid (sum of ring vertices in ring order, renormalised), perimeter and angle sum
@@ -991,9 +1052,15 @@ int launch_corners(svm_model* m, bool t1test) {
     }
     double lo, hi;
     t1_bracket(m->t1Threshold, m->R, &lo, &hi);
-    k_corners<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
-        m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
-        m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
+    // both kernels write the same values; the slot-parallel one is faster below ~100k vertices
+    if (m->nVertices < kCornerSlotsBelow)
+        k_corners_s<<<(m->nVertices + kCornerVerts - 1) / kCornerVerts, 3 * kCornerVerts, 0, m->stream>>>(
+            m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+            m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
+    else
+        k_corners_v<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
+            m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+            m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
     m->cornersValid = true;
     return check_launch();
 }
