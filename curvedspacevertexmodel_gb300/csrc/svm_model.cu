@@ -432,8 +432,122 @@ __device__ __forceinline__ D3 renorm_exact(D3 p, double R) {
 
 // One flip as testAndPerformT1TransitionsCPU does it (sphericalVertexModel.cpp:483-599).
 // Returns false when the flip is forbidden or does not fit the ring capacity.
+//
+// Rings of capacity 16 (the default) take a faster path: the four rings the flip reads and
+// rewrites are loaded once as four 16-byte vectors each, searched and edited in thread-local
+// copies (L1), and stored back whole; every value written is the same as the general path's.
+struct Ring16 {
+    int r[16];
+    int n;
+};
+__device__ __forceinline__ void ring16_load(const ApplyArgs& A, int cell, Ring16& R) {
+    const int4* q = reinterpret_cast<const int4*>(A.ring + (long)cell * 16);
+    const int4 a = q[0], b = q[1], c = q[2], d = q[3];
+    R.r[0] = a.x; R.r[1] = a.y; R.r[2] = a.z; R.r[3] = a.w; R.r[4] = b.x; R.r[5] = b.y; R.r[6] = b.z; R.r[7] = b.w;
+    R.r[8] = c.x; R.r[9] = c.y; R.r[10] = c.z; R.r[11] = c.w; R.r[12] = d.x; R.r[13] = d.y; R.r[14] = d.z; R.r[15] = d.w;
+    R.n = A.ringCount[cell];
+}
+__device__ __forceinline__ void ring16_store(int* dst, const Ring16& R) {
+    int4* q = reinterpret_cast<int4*>(dst);
+    q[0] = make_int4(R.r[0], R.r[1], R.r[2], R.r[3]);
+    q[1] = make_int4(R.r[4], R.r[5], R.r[6], R.r[7]);
+    q[2] = make_int4(R.r[8], R.r[9], R.r[10], R.r[11]);
+    q[3] = make_int4(R.r[12], R.r[13], R.r[14], R.r[15]);
+}
+// ring_neighbours, ring_remove and ring_insert_after on a local copy
+__device__ __forceinline__ void ring16_neighbours(const Ring16& R, int target, int& vlast, int& vnext) {
+    const int n = R.n;
+    vlast = R.r[n - 2];
+    int vcur = R.r[n - 1];
+    vnext = vcur;
+    for (int k = 0; k < n; ++k) {
+        vnext = R.r[k];
+        if (vcur == target) break;
+        vlast = vcur;
+        vcur = vnext;
+    }
+}
+__device__ __forceinline__ void ring16_remove(Ring16& R, int target) {
+    const int n = R.n;
+    int idx = 0;
+    for (int k = 0; k < n - 1; ++k) {
+        if (R.r[k] == target) idx += 1;
+        R.r[k] = R.r[idx];
+        idx += 1;
+    }
+    R.n = n - 1;
+}
+__device__ __forceinline__ void ring16_insert_after(Ring16& R, int after, int added) {
+    const int n = R.n;
+    int k = 0;
+    while (k < n && R.r[k] != after) ++k;
+    for (int j = n; j > k + 1; --j) R.r[j] = R.r[j - 1];
+    R.r[k + 1] = added;
+    R.n = n + 1;
+}
+
+__device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs);
+
+__device__ bool t1_flip16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings) {
+    const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
+    cs.w = -1;
+    for (int ff = 0; ff < 3; ++ff) {
+        const int t = compRef(A.vcell, v2, ff);
+        if (t != c[0] && t != c[1] && t != c[2]) cs.w = t;
+    }
+    Ring16 Rc[3], Rw;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) ring16_load(A, c[q], Rc[q]);
+    if (cs.w >= 0) ring16_load(A, cs.w, Rw);
+    cs.x = cs.y = cs.z = -1;
+    int qx = 0, qy = 0, qz = 0, yl = 0, yx = 0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        int vl, vx;
+        ring16_neighbours(Rc[q], v1, vl, vx);
+        if (vl == v2) { cs.x = c[q]; qx = q; }
+        else if (vx == v2) { cs.z = c[q]; qz = q; }
+        else { cs.y = c[q]; qy = q; yl = vl; yx = vx; }
+    }
+    if (cs.x < 0 || cs.y < 0 || cs.z < 0 || cs.w < 0) { atomicOr(A.status, SVM_DEV_BAD_TOPOLOGY); return false; }
+    Ring16& RX = Rc[qx];
+    Ring16& RY = Rc[qy];
+    Ring16& RZ = Rc[qz];
+    vs.x = yl; vs.y = yx;
+    int vl, vx;
+    ring16_neighbours(Rw, v2, vl, vx);
+    vs.w = vl; vs.z = vx;
+    // forbid a T1 that would shrink a triangular cell (sphericalVertexModel.cpp:485-487)
+    if (RX.n == 3 || RZ.n == 3) return false;
+    if (RY.n + 1 > 16 || Rw.n + 1 > 16) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    if (undo) {
+        undo->v1 = v1; undo->v2 = v2; undo->b = vs.y; undo->c = vs.z;
+        undo->cells[0] = cs.x; undo->cells[1] = cs.y; undo->cells[2] = cs.z; undo->cells[3] = cs.w;
+        undo->p1 = apos4(A, v1); undo->p2 = apos4(A, v2);
+        undo->vc1 = A.vcell[v1]; undo->vc2 = A.vcell[v2];
+        undo->vn[0] = A.vnbr[v1]; undo->vn[1] = A.vnbr[v2]; undo->vn[2] = A.vnbr[vs.y]; undo->vn[3] = A.vnbr[vs.z];
+        undo->counts[0] = RX.n; undo->counts[1] = RY.n; undo->counts[2] = RZ.n; undo->counts[3] = Rw.n;
+        ring16_store(undoRings, RX);
+        ring16_store(undoRings + 16, RY);
+        ring16_store(undoRings + 32, RZ);
+        ring16_store(undoRings + 48, Rw);
+    }
+    t1_flip_positions(A, v1, v2, cs, vs);
+    ring16_remove(RX, v2);
+    ring16_insert_after(RY, v1, v2);
+    ring16_remove(RZ, v1);
+    ring16_insert_after(Rw, v2, v1);
+    ring16_store(A.ring + (long)cs.x * 16, RX);
+    ring16_store(A.ring + (long)cs.y * 16, RY);
+    ring16_store(A.ring + (long)cs.z * 16, RZ);
+    ring16_store(A.ring + (long)cs.w * 16, Rw);
+    A.ringCount[cs.x] = RX.n; A.ringCount[cs.y] = RY.n; A.ringCount[cs.z] = RZ.n; A.ringCount[cs.w] = Rw.n;
+    return true;
+}
+
 __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo = nullptr,
                         int* undoRings = nullptr) {
+    if (A.Wc == 16) return t1_flip16(A, v1, v2, cs, vs, undo, undoRings);
     const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
     cs.w = -1;
     for (int ff = 0; ff < 3; ++ff) {
@@ -470,6 +584,17 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
             for (int k = 0; k < n; ++k) undoRings[q * A.Wc + k] = A.ring[(long)cell * A.Wc + k];
         }
     }
+    t1_flip_positions(A, v1, v2, cs, vs);
+    ring_remove(A, cs.x, v2);
+    ring_insert_after(A, cs.y, v1, v2);
+    ring_remove(A, cs.z, v1);
+    ring_insert_after(A, cs.w, v2, v1);
+    return true;
+}
+
+// The rotation and separation of v1 and v2 and the rewiring of the vertex lists
+// (sphericalVertexModel.cpp:513-573), shared by both paths of t1_flip.
+__device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs) {
     D3 p1 = apos(A, v1), p2 = apos(A, v2);
     D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
     mid = renorm_exact(mid, 1.0);
@@ -493,11 +618,6 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
         if (compRef(A.vnbr, v1, k) == vs.y) compRef(A.vnbr, v1, k) = vs.z;
         if (compRef(A.vnbr, v2, k) == vs.z) compRef(A.vnbr, v2, k) = vs.y;
     }
-    ring_remove(A, cs.x, v2);
-    ring_insert_after(A, cs.y, v1, v2);
-    ring_remove(A, cs.z, v1);
-    ring_insert_after(A, cs.w, v2, v1);
-    return true;
 }
 
 // Ring bookkeeping (vrpos/vlast/vnext) and corners of the cells whose rings a T1 pass changed,
