@@ -87,8 +87,36 @@ __host__ __device__ inline void t1_bracket(double t, double R, double* lo, doubl
     *lo = c - 1e-9;
     *hi = c + 1e-9;
 }
-__device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, double cosLo, double cosHi) {
+// A pre-test decides the edges away from the threshold without square roots or divisions:
+// sin^2(angle) = |p1 x p2|^2 / (|p1|^2 |p2|^2) against sin^2(a) (1 -/+ eps) (s2Lo, s2Hi), a = t / R,
+// for angles below pi / 2 (p1.p2 > 0) and above 3e-7 (|p1 x p2|^2 > 1e-13 |p1|^2 |p2|^2: closer
+// to 0, c can round to 1 or past it, where the reference's acos is 0 or NaN).  The formula's
+// decision is c > c* with c* within 1e-30 of cos(a), and c within 5e-16 of the cosine of the angle;
+// outside the band, the cosine differs from cos(a) by at least a^2 eps / 2 >= 5e-13, and the
+// pre-test's own relative error is below 1e-9 / a, so every decision it takes is the formula's.
+// eps = max(1e-6, 1e-12 / a^2); thresholds of 0 or of 1 radian or more skip the pre-test.
+__host__ inline void t1_sin2_bracket(double t, double R, double* lo, double* hi) {
+    const double a = t / R;
+    if (!(a > 0.0 && a < 1.0)) {   // never decides: xx < -d and xx > 2 d are impossible
+        *lo = -1.0;
+        *hi = 2.0;
+        return;
+    }
+    const double s = sin(a);
+    double eps = 1e-12 / (a * a);
+    if (eps < 1e-6) eps = 1e-6;
+    *lo = s * s * (1.0 - eps);
+    *hi = s * s * (1.0 + eps);
+}
+__device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, double cosLo, double cosHi,
+                                             double s2Lo, double s2Hi) {
     const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
+    if (num > 0) {
+        const D3 x = cross3(p1, p2);
+        const double xx = dot3(x, x), d = dot3(p1, p1) * dot3(p2, p2);
+        if (xx < s2Lo * d && xx > 1e-13 * d) return true;
+        if (xx > s2Hi * d) return false;
+    }
     const double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
     const double c = num / den;
     if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
@@ -250,6 +278,7 @@ struct T1Scratch {
     int* undoRings = nullptr;      // old rings of the four cells, 4*Wc ints per entry
     int* ctr = nullptr;            // [0] pending, [1] next, [2] undo entries, [3] rollback, [4] executed
     int* stats = nullptr;          // svm_model_t1_stats counters
+    unsigned long long* clocks = nullptr;  // svm_model_t1_clocks: SM cycles per phase (null: off)
     int cap = 0, undoCap = 0;
 };
 constexpr int kFootprint = 14;     // 8 vertex slots + 6 cell slots (duplicates allowed)

@@ -327,16 +327,17 @@ __global__ void k_move(double4_32a* __restrict__ pos, const double* __restrict__
 // Standalone T1 edge test (gpu_vm_test_edges_for_T1, sphericalVertexModel.cu:225-273).
 __global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __restrict__ pos32,
                           const double* __restrict__ repR, const int4* __restrict__ vnbr, int nV, double R,
-                          double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
+                          double t1Threshold, double cosLo, double cosHi, double s2Lo, double s2Hi, T1Scratch t1) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const int4 nb = vnbr[v];
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int u = comp(nb, s);
+        if (!(v < u)) continue;
         const bool shortEdge = pos32 ? arc32(pos32[v], pos32[u], (float)repR[rep_of(pos32[v])]) < (float)t1Threshold
-                                     : shorter_than(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi);
-        if (v < u && shortEdge) {
+                                     : shorter_than(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi, s2Lo, s2Hi);
+        if (shortEdge) {
             const int q = 3 * v + s;
             atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
             atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
@@ -348,6 +349,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __r
 // ---- T1 apply ------------------------------------------------------------------------------
 struct ApplyArgs {
     double cosLo, cosHi;   // shorter_than bracket of cos(t1Threshold / R)
+    double s2Lo, s2Hi;     // and its pre-test bracket of sin^2(t1Threshold / R)
     float4* pos32;         // FP32 positions in the mixed-precision form, else null
     const double* repR;    // per-replica radius (mixed form)
     double4_32a* pos;
@@ -415,10 +417,14 @@ __device__ void ring_insert_after(const ApplyArgs& A, int cell, int after, int a
 }
 
 // rodriguesRotation (inc/functions.h:175-181)
-__device__ __forceinline__ D3 rodrigues(D3 v, D3 k, double theta) {
+// with c = cos(theta), s = sin(theta) given.  A flip rotates by theta = -det kPI / 2, det = +-1;
+// kPI / 2 falls short of pi / 2 by kPILo / 2, so cos(theta) = sin(kPILo / 2), which is kPILo / 2
+// to double precision (the cubic term is 1e-49), and sin(theta) = -det cos(kPILo / 2), which
+// rounds to -det (1 - 1.9e-33 is within half an ulp of 1).
+constexpr double kCosHalfPi = 0.5 * kPILo;
+__device__ __forceinline__ D3 rodrigues(D3 v, D3 k, double c, double s) {
     const D3 cp{__dsub_rn(__dmul_rn(k.y, v.z), __dmul_rn(k.z, v.y)), __dsub_rn(__dmul_rn(k.z, v.x), __dmul_rn(k.x, v.z)),
                 __dsub_rn(__dmul_rn(k.x, v.y), __dmul_rn(k.y, v.x))};
-    const double c = cos(theta), s = sin(theta);
     const double w = __dmul_rn(1.0 - c, __dadd_rn(__dadd_rn(__dmul_rn(k.x, v.x), __dmul_rn(k.y, v.y)), __dmul_rn(k.z, v.z)));
     return D3{__dadd_rn(__dadd_rn(__dmul_rn(c, v.x), __dmul_rn(s, cp.x)), __dmul_rn(w, k.x)),
               __dadd_rn(__dadd_rn(__dmul_rn(c, v.y), __dmul_rn(s, cp.y)), __dmul_rn(w, k.y)),
@@ -601,9 +607,9 @@ __device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4
     const D3 vC = apos(A, vs.z);
     double det = vC.x * (p1.y * p2.z - p1.z * p2.y) + vC.y * (p1.z * p2.x - p1.x * p2.z) + vC.z * (p1.x * p2.y - p1.y * p2.x);
     det = det > 0 ? 1. : -1.;
-    const double theta = -0.5 * det * kPI;
-    p1 = rodrigues(p1, mid, theta);
-    p2 = rodrigues(p2, mid, theta);
+    // theta = -0.5 det kPI (sphericalVertexModel.cpp:507-508)
+    p1 = rodrigues(p1, mid, kCosHalfPi, -det);
+    p2 = rodrigues(p2, mid, kCosHalfPi, -det);
     const D3 diff{__dmul_rn(0.5, __dsub_rn(p1.x, p2.x)), __dmul_rn(0.5, __dsub_rn(p1.y, p2.y)), __dmul_rn(0.5, __dsub_rn(p1.z, p2.z))};
     p1 = D3{__dadd_rn(p1.x, diff.x), __dadd_rn(p1.y, diff.y), __dadd_rn(p1.z, diff.z)};
     p2 = D3{__dsub_rn(p2.x, diff.x), __dsub_rn(p2.y, diff.y), __dsub_rn(p2.z, diff.z)};
@@ -669,7 +675,7 @@ __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
     const int u = compRef(A.vnbr, v, s);
     if (!(v < u)) return false;
     if (A.pos32) return arc32(A.pos32[v], A.pos32[u], (float)aR(A, v)) < (float)A.t1Threshold;
-    return shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi);
+    return shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
 }
 
 // Applies the flagged T1 flips in the order of the CPU loop (ascending vertex1, then slot),
@@ -887,6 +893,15 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
     int* undoRingsB = t1.undoRings + (long)seg * undoPer * 4 * A.Wc;
     if (tid == 0) { nCur = 0; nTouchedB = 0; flag = 0; sNext = 0; sUndo = 0; sRollback = 0; sExec = 0; sFlips = 0; nWordsHit = 0; }
     __syncthreads();
+    // phase clocks (block 0, thread 0; svm_model_t1_clocks): extraction, reserve, run, release, end
+    const bool clk = t1.clocks && seg == 0 && tid == 0;
+    long long c0 = clk ? clock64() : 0, c1 = c0;
+    auto lap = [&](int slot) {
+        if (!clk) return;
+        c1 = clock64();
+        atomicAdd(t1.clocks + slot, (unsigned long long)(c1 - c0));
+        c0 = c1;
+    };
     // 1. the segment's flagged positions, ascending: the bitmap words whose summary bit is set
     //    (a superset of the non-empty words) into `nxt`, then their set bits inside [qLo, qHi)
     const int wLo = qLo >> 5, wHi = (qHi + 31) >> 5;  // words [wLo, wHi)
@@ -937,6 +952,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
     const int nOrig = nCur;
     int rounds = 0;
     bool rollback = flag != 0;  // more candidates than the slice holds: k_t1_apply takes them all
+    lap(0);
     // 2. rounds
     while (!rollback && nCur > 0) {
         ++rounds;
@@ -951,6 +967,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
             if (late) atomicExch(&sRollback, 1);
         }
         __syncthreads();
+        lap(1);
         if (sRollback) {
             // release this round's reservations before leaving
             for (int i = tid; i < nCur; i += blockDim.x) {
@@ -1029,6 +1046,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
                 }
         }
         __syncthreads();
+        lap(2);
         // release this round's reservations
         for (int i = tid; i < nCur; i += blockDim.x) {
             const int* f = fpB + (long)i * kFootprint;
@@ -1039,6 +1057,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
         if (tid == 0) { nCur = min(sNext, capB); sNext = 0; }
         int* t = cur; cur = nxt; nxt = t;
         __syncthreads();
+        lap(3);
         if (sRollback) rollback = true;
     }
     __syncthreads();
@@ -1089,6 +1108,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
         amLast = atomicAdd(t1.ctr + 7, 1) == (int)gridDim.x - 1;
     }
     __syncthreads();
+    lap(4);
     if (!amLast) return;
     if (tid == 0) t1.stats[4] += *(volatile int*)(t1.ctr + 6);
     // summary bits of words that are now empty
@@ -1161,6 +1181,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
     A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
     t1_bracket(m->t1Threshold, m->R, &A.cosLo, &A.cosHi);
+    t1_sin2_bracket(m->t1Threshold, m->R, &A.s2Lo, &A.s2Hi);
     return A;
 }
 
@@ -1250,8 +1271,25 @@ int launch_t1_apply(svm_model* m, int bump) {
     return check_launch();
 }
 
-// One fused Brownian timestep (see the file header).
-static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise, uint64_t seed) {
+// The T1 edge test on its own (k_t1_test: the decisions of the test fused into the corner
+// kernels), for a state whose corners are not needed before the positions change again.
+int launch_t1_test(svm_model* m) {
+    PhaseTimer pt(m, SVM_PHASE_CORNERS);
+    double lo, hi, s2lo, s2hi;
+    t1_bracket(m->t1Threshold, m->R, &lo, &hi);
+    t1_sin2_bracket(m->t1Threshold, m->R, &s2lo, &s2hi);
+    k_t1_test<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
+        m->pos[m->cur], m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr, m->repR, m->vnbr,
+        m->nVertices, m->R, m->t1Threshold, lo, hi, s2lo, s2hi, m->t1);
+    return check_launch();
+}
+
+// One fused Brownian timestep (see the file header).  With `deferCorners` the moved state gets
+// only the T1 test and flips, and its corners are left invalid: the next step computes them (for
+// callers that replace the positions between steps, whose corners would otherwise be computed
+// twice).  Positions, topology and every later value are the same either way.
+static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, const double* noise, uint64_t seed,
+                   bool deferCorners = false) {
     int rc = SVM_OK;
     if (m->nRep > 1 && !capturing(m->stream) && (rc = update_rep_noise(m, dt, mu))) return rc;
     rc = launch_geometry(m);
@@ -1270,6 +1308,13 @@ static int bd_step(svm_model* m, double T, double dt, double mu, int noiseMode, 
     }
     if (rc || (rc = check_launch())) return rc;
     m->cur = nxt;
+    if (deferCorners) {
+        m->cornersValid = false;
+        if (!m->restricted && (rc = launch_t1_test(m))) return rc;
+        rc = launch_t1_apply(m, 1);
+        m->cornersValid = false;  // the patch of touched cells leaves the others stale
+        return rc;
+    }
     // corners of the moved state, with the T1 edge test fused in
     rc = launch_corners(m, !m->restricted);
     if (rc) return rc;
@@ -1465,7 +1510,7 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.pass, m->t1.listA, m->t1.listB, m->t1.listOrig, m->t1.fp, m->t1.comList, m->t1.resV,
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
                     m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->dap32, m->repR, m->repNp, m->repCellOff,
-                    m->repVertOff,
+                    m->repVertOff, m->t1.clocks,
                     m->repFlag, m->repScal};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
@@ -1602,13 +1647,7 @@ int svm_model_compute_energy(svm_model* m, double* e) {
 
 int svm_model_enforce_topology(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
-    double lo, hi;
-    svm::t1_bracket(m->t1Threshold, m->R, &lo, &hi);
-    k_t1_test<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
-        m->pos[m->cur], m->precision == SVM_PRECISION_MIXED ? m->pos32[m->cur] : nullptr, m->repR, m->vnbr,
-        m->nVertices, m->R,
-        m->t1Threshold, lo, hi, m->t1);
-    if (svm::check_launch()) return SVM_ERR_CUDA;
+    if (svm::launch_t1_test(m)) return SVM_ERR_CUDA;
     // the patch of touched cells writes corners; all of them are recomputed before their next use
     int rc = svm::launch_t1_apply(m, 0);
     m->cornersValid = false;
@@ -1783,6 +1822,25 @@ int svm_model_t1_stats(svm_model* m, int* st) {
     return SVM_OK;
 }
 
+int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5) {
+    if (!m) return SVM_ERR_ARG;
+    if (cycles5 && m->t1.clocks) {
+        SVM_CUDA(cudaStreamSynchronize(m->stream));
+        SVM_CUDA(cudaMemcpy(cycles5, m->t1.clocks, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    }
+    if (enable && !m->t1.clocks) {
+        SVM_CUDA(cudaMalloc(&m->t1.clocks, 8 * sizeof(unsigned long long)));
+    }
+    if (!enable && m->t1.clocks) {
+        SVM_CUDA(cudaStreamSynchronize(m->stream));
+        cudaFree(m->t1.clocks);
+        m->t1.clocks = nullptr;
+    }
+    if (m->t1.clocks) SVM_CUDA(cudaMemset(m->t1.clocks, 0, 8 * sizeof(unsigned long long)));
+    m->paramsVersion++;  // captured graphs hold the old pointer
+    return SVM_OK;
+}
+
 int svm_model_synchronize(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     SVM_CUDA(cudaStreamSynchronize(m->stream));
@@ -1824,7 +1882,8 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
         }
         m->cornersValid = false;
     }
-    int rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+    // a caller that passes positions in is likely to replace them again before the next step
+    int rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed, posIn != nullptr);
     if (rc) return rc;
     if (energyOut) {
         k_energy<<<svm::blocksFor(m->nCells), svm::kBlock, 0, m->stream>>>(m->ap, m->pref, m->Kr, m->nCells,

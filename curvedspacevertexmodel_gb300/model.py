@@ -276,6 +276,13 @@ class sphericalVertexModel:
     def synchronize(self):
         call("svm_model_synchronize", self._h)
 
+    def t1Clocks(self, enable: bool = True):
+        """SM cycles of the parallel T1 pass's phases since the last call (extraction, reserve,
+        flips, release, end) and re-arms the counters (or turns them off)."""
+        out = np.zeros(5, dtype=np.uint64)
+        call("svm_model_t1_clocks", self._h, int(enable), out)
+        return dict(zip(("extract", "reserve", "flip", "release", "end"), map(int, out)))
+
     def saveState(self) -> dict:
         """Positions and connectivity (host copies) for loadState."""
         rings, counts = self.rings()

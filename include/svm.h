@@ -154,6 +154,10 @@ int svm_model_take_flips(svm_model* m, int* pairs, int capacity, int* count);
  * the test, edges that ran in the parallel rounds, flips, parallel rounds, passes replayed one flip
  * at a time after a rollback.  (The reference's T1 loop keeps no such counters.) */
 int svm_model_t1_stats(svm_model* m, int* stats6);
+/* SM cycles spent by the first segment of the parallel T1 pass in its phases since the last call
+ * (extraction of the flagged edges, reservation, flips, release, end), when cycles5 is non-NULL
+ * and the counters are on; then (re)arms them (enable != 0) or turns them off. */
+int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5);
 int svm_model_synchronize(svm_model* m);
 /* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
  * z, unused) per vertex in the FP64 form, float4 in the mixed form.  Valid until the next step,

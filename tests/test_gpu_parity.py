@@ -386,3 +386,31 @@ def test_host_io_step_equals_the_call_sequence(svm, gold):
     e_seq = b.computeEnergy()
     assert np.array_equal(out.reshape(-1, 3), b.returnPositions())
     assert e_io.value == e_seq
+
+
+def test_host_io_steps_chained_with_flips(svm):
+    """Chained svm_brownian_step_io calls (each step's positions fed back in) follow the
+    device-resident step loop bit for bit over steps with T1 flips: positions, topology, flip
+    count and energies.  (The host-io step defers the moved state's corners to the next step.)"""
+    import ctypes as C
+    from curvedspacevertexmodel_gb300 import _lib
+    a, _ = stabilised(svm, 3000, seed=11, stab=40, steps=60)
+    b, _ = stabilised(svm, 3000, seed=11, stab=40, steps=60)
+    for m in (a, b):
+        m.setT1Threshold(0.08)   # flips every step
+    a.t1Stats(), b.t1Stats()   # counters restart
+    pos = np.ascontiguousarray(a.returnPositions()).reshape(-1)
+    out = np.empty_like(pos)
+    e_io = C.c_double()
+    for k in range(25):
+        _lib.call("svm_brownian_step_io", a.handle, 0.05, 0.01, 1.0, 4242 + k, pos, out, C.byref(e_io))
+        _lib.call("svm_brownian_step", b.handle, 0.05, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, 4242 + k)
+        pos, out = out, pos
+    assert np.array_equal(pos.reshape(-1, 3), b.returnPositions())
+    assert np.array_equal(a.vertexNeighbors(), b.vertexNeighbors())
+    r1, c1 = a.rings()
+    r2, c2 = b.rings()
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    fa, fb = a.t1Stats()["flips"], b.t1Stats()["flips"]
+    assert fa == fb and fa > 25
+    assert a.computeEnergy() == b.computeEnergy()
