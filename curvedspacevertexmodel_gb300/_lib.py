@@ -24,6 +24,7 @@ SVM_DEV_RING_OVERFLOW = 0x1
 SVM_DEV_T1_OVERFLOW = 0x2
 SVM_DEV_CELLLIST_OVERFLOW = 0x4
 SVM_DEV_BAD_TOPOLOGY = 0x8
+SVM_DEV_T1_TIMEOUT = 0x10
 SVM_NOISE_PHILOX = 0
 SVM_NOISE_BUFFER = 1
 PHASES = ("corners", "cells", "fallback", "force", "t1_apply", "move")
@@ -93,6 +94,7 @@ SIGNATURES = {
     "svm_model_take_flips": (i32, [vp, ip, i32, C.POINTER(i32)]),
     "svm_model_synchronize": (i32, [vp]),
     "svm_model_t1_clocks": (i32, [vp, i32, _nullable(np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS"))]),
+    "svm_model_set_t1_blocks": (i32, [vp, i32]),
     "svm_model_t1_stats": (i32, [vp, ip]),
     "svm_model_profile": (i32, [vp, i32]),
     "svm_model_profile_read": (i32, [vp, dp, ip]),

@@ -255,6 +255,14 @@ struct UndoEntry {
     int logIdx;                    // the flip's entry in the flip log
 };
 
+// Counters of one parallel T1 pass: in shared memory for a single-block pass, in global memory
+// (T1Scratch::ctl) for a pass spread over a cooperative grid, with the grid barrier's words.
+struct T1Ctl {
+    int nCur, flag, nWordsHit, undo, late, rollback, exec, flips, next[2];
+    unsigned barCount, barGen;
+};
+constexpr int kT1CtlInts = sizeof(T1Ctl) / sizeof(int);
+
 struct T1Scratch {
     unsigned* bits = nullptr;      // one bit per (vertex, slot) position, 3*Nv bits
     unsigned* summary = nullptr;   // one bit per word of `bits`
@@ -279,6 +287,7 @@ struct T1Scratch {
     int* ctr = nullptr;            // [0] pending, [1] next, [2] undo entries, [3] rollback, [4] executed
     int* stats = nullptr;          // svm_model_t1_stats counters
     unsigned long long* clocks = nullptr;  // svm_model_t1_clocks: SM cycles per phase (null: off)
+    T1Ctl* ctl = nullptr;          // counters of a cooperative pass (inside the ctr allocation)
     int cap = 0, undoCap = 0;
 };
 constexpr int kFootprint = 14;     // 8 vertex slots + 6 cell slots (duplicates allowed)
@@ -296,6 +305,7 @@ struct svm_model {
     cudaStream_t stream = nullptr;
     int cur = 0;                       // index of the current position buffer
     bool cornersValid = false;         // corner/vsph arrays match the current state
+    int t1Blocks = 0;                  // svm_model_set_t1_blocks (0: automatic)
     double4_32a* pos[2] = {nullptr, nullptr};
     double4_32a* vsph = nullptr;
     int4 *vcell = nullptr, *vnbr = nullptr, *vlast = nullptr, *vnext = nullptr, *vrpos = nullptr;

@@ -827,6 +827,7 @@ __device__ __forceinline__ void t1_footprint(const ApplyArgs& A, int p, int* f) 
 
 constexpr int kParThreads = 1024;       // one segment: the whole sphere
 constexpr int kParThreadsBatch = 256;   // one segment per replica
+constexpr int kCoopThreads = 128;       // per block of a cooperative single-sphere pass
 
 // Block-wide exclusive scan of one int per thread; returns the block total in *total.
 __device__ int block_excl_scan(int v, int* total) {
@@ -855,6 +856,36 @@ __device__ int block_excl_scan(int v, int* total) {
     return before;
 }
 
+// Barrier of all blocks of a cooperative launch (co-resident by construction): the last block
+// to arrive resets the count and advances the generation; the others poll the generation, at most
+// kBarrierSpins times, after which the wait gives up and the barrier returns false.  Fences before
+// the arrival and after the wait order every block's writes before the barrier with every read
+// after it.
+constexpr int kBarrierSpins = 1 << 20;  // at least 67 ms with 64 ns naps
+__device__ bool grid_barrier(T1Ctl* ctl) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned gen = *(volatile unsigned*)&ctl->barGen;
+        __threadfence();
+        if (atomicAdd(&ctl->barCount, 1u) == gridDim.x - 1) {
+            *(volatile unsigned*)&ctl->barCount = 0u;
+            __threadfence();
+            atomicAdd(&ctl->barGen, 1u);
+        } else {
+            int spins = 0;
+            while (*(volatile unsigned*)&ctl->barGen == gen) {
+                if (++spins > kBarrierSpins) { ok = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
 // Applies the flagged flips with the result of the CPU's sequential order, in parallel rounds of
 // deterministic reservations: every pending position writes its own value into the footprint
 // cells (atomicMin); a position whose whole footprint holds its value runs (test, flip,
@@ -864,22 +895,41 @@ __device__ int block_excl_scan(int v, int* total) {
 // detected through the per-vertex/per-cell record of the highest position that ran, and then
 // every flip of the pass is undone and the bitmap restored for k_t1_apply, which then applies
 // the flips one by one.  On success *t1.count is cleared so k_t1_apply returns at once.
-// One block per segment of the position space: the whole sphere, or one replica of a batch (whose
-// flagged edges share no vertex or cell with another replica's, and whose positions are a
-// contiguous range).  A block's lists, footprints, commit list and undo log are its own slices of
-// the scratch arrays; the touched-cell list and the flip log are shared (atomic appends).  A block
-// whose pass is not the sequential order undoes its own flips, marks their log entries invalid
-// (pass -1) and restores its segment's flags, which k_t1_apply then replays; the counter of
-// flagged positions drops by the positions of every block that succeeded.  The last block to
-// finish (ticket) folds the round count into the statistics and clears summary bits whose bitmap
-// words are empty.
-__global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scratch t1, const int* __restrict__ segOff,
+//
+// kCoop = false: one block per segment of the position space: the whole sphere, or one replica
+// of a batch (whose flagged edges share no vertex or cell with another replica's, and whose
+// positions are a contiguous range).  A block's lists, footprints, commit list and undo log are
+// its own slices of the scratch arrays; the touched-cell list and the flip log are shared (atomic
+// appends).  A block whose pass is not the sequential order undoes its own flips, marks their log
+// entries invalid (pass -1) and restores its segment's flags, which k_t1_apply then replays; the
+// counter of flagged positions drops by the positions of every block that succeeded.  The last
+// block to finish (ticket) folds the round count into the statistics and clears summary bits
+// whose bitmap words are empty.
+// kCoop = true: one segment (the whole sphere) over all blocks of a cooperative launch, so that the
+// flips' FP64 work spreads over many SMs instead of one: block 0 extracts the flagged positions,
+// position i of a round runs on block i mod gridDim.x, the phases are separated by grid barriers
+// instead of block barriers, the counters live in global memory (t1.ctl), and block 0 alone
+// finishes the pass (rollback, statistics, cleanup).  Same decisions, same results.
+template <bool kCoop>
+__global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_parallel(ApplyArgs A, T1Scratch t1, const int* __restrict__ segOff,
                                                              int listPad, int undoPer) {
-    __shared__ int nCur, nTouchedB, flag, sNext, sUndo, sRollback, sExec, sFlips, nWordsHit;
-    const int tid = threadIdx.x, seg = blockIdx.x;
+    __shared__ T1Ctl sctl;
+    T1Ctl* ctl = kCoop ? t1.ctl : &sctl;
+    const int tid = threadIdx.x, seg = kCoop ? 0 : blockIdx.x;
+    const bool leader = !kCoop || blockIdx.x == 0;  // extracts the positions and finishes the pass
+    // this thread's first position of a round and the stride (positions spread over the blocks)
+    const int gi = kCoop ? blockIdx.x + gridDim.x * tid : tid;
+    const int gs = kCoop ? gridDim.x * blockDim.x : blockDim.x;
     // one segment and nothing flagged: nothing to do.  (With several segments every block runs:
-    // the last one to finish does the pass's cleanup.)
-    if (gridDim.x == 1 && *t1.count == 0) return;
+    // the last one to finish does the pass's cleanup.)  The count is read by every block before
+    // the first grid barrier, so before block 0 can change it.
+    if ((kCoop || gridDim.x == 1) && *t1.count == 0) return;
+    auto group_sync = [&]() -> bool {
+        if (!kCoop) { __syncthreads(); return true; }
+        if (grid_barrier(ctl)) return true;
+        if (tid == 0) atomicOr(A.status, SVM_DEV_T1_TIMEOUT);
+        return false;
+    };
     const int qLo = segOff ? 3 * segOff[seg] : 0;
     const int qHi = segOff ? 3 * segOff[seg + 1] : 3 * A.nV;
     const int base = qLo / 2 + listPad * seg;
@@ -891,10 +941,14 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
     int* comB = t1.comList + (long)base * kFootprint;
     UndoEntry* undoB = t1.undo + (long)seg * undoPer;
     int* undoRingsB = t1.undoRings + (long)seg * undoPer * 4 * A.Wc;
-    if (tid == 0) { nCur = 0; nTouchedB = 0; flag = 0; sNext = 0; sUndo = 0; sRollback = 0; sExec = 0; sFlips = 0; nWordsHit = 0; }
+    // a cooperative pass starts from zeroed counters (cleared with the launch's memset)
+    if (!kCoop && tid == 0) {
+        sctl.nCur = 0; sctl.flag = 0; sctl.nWordsHit = 0; sctl.undo = 0; sctl.rollback = 0; sctl.exec = 0;
+        sctl.flips = 0; sctl.next[0] = 0; sctl.next[1] = 0; sctl.late = 0;
+    }
     __syncthreads();
     // phase clocks (block 0, thread 0; svm_model_t1_clocks): extraction, reserve, run, release, end
-    const bool clk = t1.clocks && seg == 0 && tid == 0;
+    const bool clk = t1.clocks && seg == 0 && blockIdx.x == 0 && tid == 0;
     long long c0 = clk ? clock64() : 0, c1 = c0;
     auto lap = [&](int slot) {
         if (!clk) return;
@@ -905,72 +959,81 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
     // 1. the segment's flagged positions, ascending: the bitmap words whose summary bit is set
     //    (a superset of the non-empty words) into `nxt`, then their set bits inside [qLo, qHi)
     const int wLo = qLo >> 5, wHi = (qHi + 31) >> 5;  // words [wLo, wHi)
-    for (int base2 = wLo >> 5; base2 < ((wHi + 31) >> 5); base2 += blockDim.x) {
-        const int sw = base2 + tid;
-        unsigned sword = sw < ((wHi + 31) >> 5) && sw < t1.nSummary ? t1.summary[sw] : 0u;
-        // keep the summary bits of words inside [wLo, wHi)
-        if (sw == (wLo >> 5)) sword &= ~0u << (wLo & 31);
-        if (sw == ((wHi - 1) >> 5) && (wHi & 31)) sword &= (1u << (wHi & 31)) - 1u;
-        int tot;
-        const int off = block_excl_scan(__popc(sword), &tot);
-        unsigned x = sword;
-        int at = nWordsHit + off;
-        while (x) {
-            const int b = __ffs(x) - 1;
-            x &= x - 1u;
-            const int w = sw * 32 + b;
-            if (w < t1.nWords && at < capB) nxt[at] = w;
-            ++at;
+    if (leader) {
+        for (int base2 = wLo >> 5; base2 < ((wHi + 31) >> 5); base2 += blockDim.x) {
+            const int sw = base2 + tid;
+            unsigned sword = sw < ((wHi + 31) >> 5) && sw < t1.nSummary ? t1.summary[sw] : 0u;
+            // keep the summary bits of words inside [wLo, wHi)
+            if (sw == (wLo >> 5)) sword &= ~0u << (wLo & 31);
+            if (sw == ((wHi - 1) >> 5) && (wHi & 31)) sword &= (1u << (wHi & 31)) - 1u;
+            int tot;
+            const int off = block_excl_scan(__popc(sword), &tot);
+            unsigned x = sword;
+            int at = ctl->nWordsHit + off;
+            while (x) {
+                const int b = __ffs(x) - 1;
+                x &= x - 1u;
+                const int w = sw * 32 + b;
+                if (w < t1.nWords && at < capB) nxt[at] = w;
+                ++at;
+            }
+            __syncthreads();
+            if (tid == 0) ctl->nWordsHit = min(ctl->nWordsHit + tot, capB);
+            __syncthreads();
         }
-        __syncthreads();
-        if (tid == 0) nWordsHit = min(nWordsHit + tot, capB);
-        __syncthreads();
-    }
-    const int nHit = nWordsHit;
-    for (int b0 = 0; b0 < nHit; b0 += blockDim.x) {
-        const int i = b0 + tid;
-        const int w = i < nHit ? nxt[i] : -1;
-        unsigned word = (w >= 0 && w < t1.nWords) ? t1.bits[w] : 0u;
-        if (w == (qLo >> 5)) word &= ~0u << (qLo & 31);
-        if (w >= 0 && w == ((qHi - 1) >> 5) && (qHi & 31)) word &= (1u << (qHi & 31)) - 1u;
-        int tot;
-        const int off = block_excl_scan(__popc(word), &tot);
-        if (nCur + tot > capB) { if (tid == 0) flag = 1; __syncthreads(); break; }
-        unsigned x = word;
-        int at = nCur + off;
-        while (x) {
-            const int b = __ffs(x) - 1;
-            x &= x - 1u;
-            cur[at] = w * 32 + b;
-            orig[at] = w * 32 + b;
-            ++at;
+        const int nHit = ctl->nWordsHit;
+        for (int b0 = 0; b0 < nHit; b0 += blockDim.x) {
+            const int i = b0 + tid;
+            const int w = i < nHit ? nxt[i] : -1;
+            unsigned word = (w >= 0 && w < t1.nWords) ? t1.bits[w] : 0u;
+            if (w == (qLo >> 5)) word &= ~0u << (qLo & 31);
+            if (w >= 0 && w == ((qHi - 1) >> 5) && (qHi & 31)) word &= (1u << (qHi & 31)) - 1u;
+            int tot;
+            const int off = block_excl_scan(__popc(word), &tot);
+            const int n0 = ctl->nCur;
+            if (n0 + tot > capB) { if (tid == 0) ctl->flag = 1; __syncthreads(); break; }
+            unsigned x = word;
+            int at = n0 + off;
+            while (x) {
+                const int b = __ffs(x) - 1;
+                x &= x - 1u;
+                cur[at] = w * 32 + b;
+                orig[at] = w * 32 + b;
+                ++at;
+            }
+            __syncthreads();
+            if (tid == 0) ctl->nCur = n0 + tot;
+            __syncthreads();
         }
-        __syncthreads();
-        if (tid == 0) nCur += tot;
-        __syncthreads();
     }
-    const int nOrig = nCur;
+    if (!group_sync()) return;
+    // uniform over the group from here on: every thread reads the same counters after a barrier
+    const int nOrig = *(volatile int*)&ctl->nCur;
+    int nCur = nOrig;
+    int par = 0;  // the round's next-list counter: ctl->next[par]
     int rounds = 0;
-    bool rollback = flag != 0;  // more candidates than the slice holds: k_t1_apply takes them all
+    bool rollback = *(volatile int*)&ctl->flag != 0;  // more candidates than the slice holds: k_t1_apply takes them all
     lap(0);
     // 2. rounds
     while (!rollback && nCur > 0) {
         ++rounds;
         // reserve
-        for (int i = tid; i < nCur; i += blockDim.x) {
+        for (int i = gi; i < nCur; i += gs) {
             const int p = cur[i];
             int* f = fpB + (long)i * kFootprint;
             t1_footprint(A, p, f);
             bool late = false;
             for (int k = 0; k < 8; ++k) { late |= t1.comV[f[k]] > p; atomicMin(t1.resV + f[k], p); }
             for (int k = 8; k < kFootprint; ++k) { late |= t1.comC[f[k]] > p; atomicMin(t1.resC + f[k], p); }
-            if (late) atomicExch(&sRollback, 1);
+            if (late) atomicExch(&ctl->late, 1);
         }
-        __syncthreads();
+        if (!group_sync()) return;
         lap(1);
-        if (sRollback) {
+        // `late` is written only while reserving and `rollback` only while running, so each is
+        // read after the barrier that ends its phase, by every block alike
+        if (*(volatile int*)&ctl->late) {
             // release this round's reservations before leaving
-            for (int i = tid; i < nCur; i += blockDim.x) {
+            for (int i = gi; i < nCur; i += gs) {
                 const int* f = fpB + (long)i * kFootprint;
                 for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
                 for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
@@ -979,27 +1042,27 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
             break;
         }
         // run the positions that hold their whole footprint
-        for (int i = tid; i < nCur; i += blockDim.x) {
+        for (int i = gi; i < nCur; i += gs) {
             const int p = cur[i];
             const int* f = fpB + (long)i * kFootprint;
             bool ready = true;
             for (int k = 0; k < 8; ++k) ready &= t1.resV[f[k]] == p;
             for (int k = 8; k < kFootprint; ++k) ready &= t1.resC[f[k]] == p;
             if (!ready) {
-                const int ni = atomicAdd(&sNext, 1);
+                const int ni = atomicAdd(&ctl->next[par], 1);
                 if (ni < capB) nxt[ni] = p;
-                else atomicExch(&sRollback, 1);
+                else atomicExch(&ctl->rollback, 1);
                 continue;
             }
-            const int ci = atomicAdd(&sExec, 1);
-            if (ci >= capB) { atomicExch(&sRollback, 1); continue; }
+            const int ci = atomicAdd(&ctl->exec, 1);
+            if (ci >= capB) { atomicExch(&ctl->rollback, 1); continue; }
             for (int k = 0; k < kFootprint; ++k) comB[(long)ci * kFootprint + k] = f[k];
             for (int k = 0; k < 8; ++k) atomicMax(t1.comV + f[k], p);
             for (int k = 8; k < kFootprint; ++k) atomicMax(t1.comC + f[k], p);
             atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
             if (!t1_candidate(A, p)) continue;
-            const int ui = atomicAdd(&sUndo, 1);
-            if (ui >= undoPer) { atomicExch(&sRollback, 1); continue; }
+            const int ui = atomicAdd(&ctl->undo, 1);
+            if (ui >= undoPer) { atomicExch(&ctl->rollback, 1); continue; }
             const int v1 = p / 3, v2 = compRef(A.vnbr, v1, p - 3 * v1);
             int4 cs, vs;
             UndoEntry* u = undoB + ui;
@@ -1007,7 +1070,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
                 u->v1 = -1;  // nothing was written
                 continue;
             }
-            atomicAdd(&sFlips, 1);
+            atomicAdd(&ctl->flips, 1);
             const int fc = atomicAdd(t1.flipCount, 1);
             u->logIdx = fc;
             if (fc < t1.flipLogCap) {
@@ -1017,9 +1080,8 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
             const int tc = atomicAdd(t1.ctr + 5, 4);
             if (tc + 4 <= t1.touchedCap) {
                 t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
-                atomicAdd(&nTouchedB, 4);
             } else {
-                atomicExch(&sRollback, 1);
+                atomicExch(&ctl->rollback, 1);
             }
             // re-test the 18 slots of the six vertices whose slots or positions the flip changed:
             // all tests first (independent loads that overlap), then the flagging
@@ -1039,32 +1101,34 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
                     const unsigned bit = 1u << (r & 31);
                     if (!(atomicOr(t1.bits + (r >> 5), bit) & bit)) {
                         atomicOr(t1.summary + (r >> 10), 1u << ((r >> 5) & 31));
-                        const int ni = atomicAdd(&sNext, 1);
+                        const int ni = atomicAdd(&ctl->next[par], 1);
                         if (ni < capB) nxt[ni] = r;
-                        else atomicExch(&sRollback, 1);
+                        else atomicExch(&ctl->rollback, 1);
                     }
                 }
         }
-        __syncthreads();
+        if (!group_sync()) return;
         lap(2);
-        // release this round's reservations
-        for (int i = tid; i < nCur; i += blockDim.x) {
+        // release this round's reservations; the other next-list counter starts the next round at 0
+        for (int i = gi; i < nCur; i += gs) {
             const int* f = fpB + (long)i * kFootprint;
             for (int k = 0; k < 8; ++k) t1.resV[f[k]] = kResFree;
             for (int k = 8; k < kFootprint; ++k) t1.resC[f[k]] = kResFree;
         }
-        __syncthreads();
-        if (tid == 0) { nCur = min(sNext, capB); sNext = 0; }
+        if (leader && tid == 0) ctl->next[par ^ 1] = 0;
+        if (!group_sync()) return;
+        nCur = min(*(volatile int*)&ctl->next[par], capB);
+        par ^= 1;
         int* t = cur; cur = nxt; nxt = t;
-        __syncthreads();
         lap(3);
-        if (sRollback) rollback = true;
+        if (*(volatile int*)&ctl->rollback) rollback = true;
     }
-    __syncthreads();
+    if (!group_sync()) return;
+    if (!leader) return;
     if (rollback) {
         if (tid == 0) {
             // undo this segment's flips, newest first, and invalidate their log entries
-            const int nu = min(sUndo, undoPer);
+            const int nu = min(*(volatile int*)&ctl->undo, undoPer);
             for (int i = nu - 1; i >= 0; --i) {
                 const UndoEntry& u = undoB[i];
                 if (u.v1 < 0) continue;
@@ -1088,7 +1152,7 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
         }
     }
     __syncthreads();
-    const int ne = min(sExec, capB);
+    const int ne = min(*(volatile int*)&ctl->exec, capB);
     for (int i = tid; i < ne; i += blockDim.x) {
         const int* f = comB + (long)i * kFootprint;
         for (int k = 0; k < 8; ++k) t1.comV[f[k]] = -1;
@@ -1101,11 +1165,11 @@ __global__ void __launch_bounds__(kParThreads) k_t1_parallel(ApplyArgs A, T1Scra
         atomicMax(t1.ctr + 6, rounds);
         if (rollback) atomicAdd(t1.stats + 5, 1);
         else {
-            atomicAdd(t1.stats + 3, sFlips);
+            atomicAdd(t1.stats + 3, *(volatile int*)&ctl->flips);
             atomicSub(t1.count, nOrig);
         }
         __threadfence();
-        amLast = atomicAdd(t1.ctr + 7, 1) == (int)gridDim.x - 1;
+        amLast = kCoop || atomicAdd(t1.ctr + 7, 1) == (int)gridDim.x - 1;
     }
     __syncthreads();
     lap(4);
@@ -1257,15 +1321,51 @@ int launch_geometry(svm_model* m) {
     return launch_cells(m);
 }
 
+// Blocks of a single sphere's parallel T1 pass: one, or a cooperative grid of about one block per
+// 3000 vertices (from 20000 vertices on, at most the co-resident count), or the count set by
+// svm_model_set_t1_blocks.
+static int t1_coop_blocks(svm_model* m) {
+    static int maxCoop = 0;  // co-resident blocks of k_t1_parallel<true> on this device
+    if (maxCoop == 0) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_t1_parallel<true>, kCoopThreads, 0);
+        maxCoop = std::max(1, sms * perSm);
+    }
+    int n = m->t1Blocks;
+    if (n == 0) n = m->nVertices < 20000 ? 1 : std::max(8, std::min(152, m->nVertices / 3000));
+    return std::min(n, maxCoop);
+}
+
 int launch_t1_apply(svm_model* m, int bump) {
     PhaseTimer pt(m, SVM_PHASE_T1APPLY, 3);
-    // touched-cell count (ctr[5]), per-pass round maximum (ctr[6]) and block ticket (ctr[7])
-    if (cudaMemsetAsync(m->t1.ctr + 5, 0, 3 * sizeof(int), m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    // touched-cell count (ctr[5]), per-pass round maximum (ctr[6]), block ticket (ctr[7]) and the
+    // cooperative pass's counters and barrier (t1.ctl, after them)
+    if (cudaMemsetAsync(m->t1.ctr + 5, 0, (3 + kT1CtlInts) * sizeof(int), m->stream) != cudaSuccess)
+        return SVM_ERR_CUDA;
     const bool batch = m->nRep > 1;
     const int nSeg = batch ? m->nRep : 1;
-    k_t1_parallel<<<nSeg, batch ? kParThreadsBatch : kParThreads, 0, m->stream>>>(
-        apply_args(m, bump), m->t1, batch ? m->repVertOff : nullptr, batch ? kListPadBatch : kListPad,
-        m->t1.undoCap / nSeg);
+    const int coop = batch ? 1 : t1_coop_blocks(m);
+    if (coop > 1) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(coop);
+        cfg.blockDim = dim3(kCoopThreads);
+        cfg.stream = m->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const int* noSeg = nullptr;
+        if (cudaLaunchKernelEx(&cfg, k_t1_parallel<true>, apply_args(m, bump), m->t1, noSeg, kListPad,
+                               m->t1.undoCap) != cudaSuccess)
+            return SVM_ERR_CUDA;
+    } else {
+        k_t1_parallel<false><<<nSeg, batch ? kParThreadsBatch : kParThreads, 0, m->stream>>>(
+            apply_args(m, bump), m->t1, batch ? m->repVertOff : nullptr, batch ? kListPadBatch : kListPad,
+            m->t1.undoCap / nSeg);
+    }
     k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
     k_t1_patch<<<2 * 152, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
     return check_launch();
@@ -1473,7 +1573,8 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->t1.comC, nC * sizeof(int));
     alloc((void**)&m->t1.undo, (size_t)m->t1.undoCap * sizeof(svm::UndoEntry));
     alloc((void**)&m->t1.undoRings, (size_t)m->t1.undoCap * 4 * Wc * sizeof(int));
-    alloc((void**)&m->t1.ctr, 8 * sizeof(int));
+    alloc((void**)&m->t1.ctr, (8 + svm::kT1CtlInts) * sizeof(int));
+    if (ok) m->t1.ctl = reinterpret_cast<svm::T1Ctl*>(m->t1.ctr + 8);
     alloc((void**)&m->t1.stats, 8 * sizeof(int));
     alloc((void**)&m->t1.flipCount, sizeof(int));
     alloc((void**)&m->t1.touched, (size_t)m->t1.touchedCap * sizeof(int));
@@ -1819,6 +1920,13 @@ int svm_model_t1_stats(svm_model* m, int* st) {
     SVM_CUDA(cudaMemcpy(h, m->t1.stats, sizeof(h), cudaMemcpyDeviceToHost));
     for (int i = 0; i < 6; ++i) st[i] = h[i];
     SVM_CUDA(cudaMemset(m->t1.stats, 0, 6 * sizeof(int)));
+    return SVM_OK;
+}
+
+int svm_model_set_t1_blocks(svm_model* m, int blocks) {
+    if (!m || blocks < 0) return SVM_ERR_ARG;
+    m->t1Blocks = blocks;
+    m->paramsVersion++;  // captured graphs hold the old launch
     return SVM_OK;
 }
 

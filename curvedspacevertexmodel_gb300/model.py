@@ -276,6 +276,11 @@ class sphericalVertexModel:
     def synchronize(self):
         call("svm_model_synchronize", self._h)
 
+    def setT1Blocks(self, blocks: int = 0):
+        """Blocks of the parallel T1 pass (0 automatic, 1 one block, n a cooperative grid of n);
+        performance only, the results do not depend on it."""
+        call("svm_model_set_t1_blocks", self._h, int(blocks))
+
     def t1Clocks(self, enable: bool = True):
         """SM cycles of the parallel T1 pass's phases since the last call (extraction, reserve,
         flips, release, end) and re-arms the counters (or turns them off)."""

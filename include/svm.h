@@ -43,6 +43,8 @@ extern "C" {
 #define SVM_DEV_T1_OVERFLOW 0x2     /* T1 bookkeeping capacity exceeded */
 #define SVM_DEV_CELLLIST_OVERFLOW 0x4 /* more points in a bin than the slot table holds */
 #define SVM_DEV_BAD_TOPOLOGY 0x8    /* an edge's cells could not be classified */
+#define SVM_DEV_T1_TIMEOUT 0x10     /* a grid barrier of the multi-block T1 pass gave up waiting
+                                       (the state of that pass is undefined) */
 
 /* Noise sources of the Brownian step. */
 #define SVM_NOISE_PHILOX 0     /* in-kernel counter-based Philox4x32-10 + Box-Muller */
@@ -158,6 +160,11 @@ int svm_model_t1_stats(svm_model* m, int* stats6);
  * (extraction of the flagged edges, reservation, flips, release, end), when cycles5 is non-NULL
  * and the counters are on; then (re)arms them (enable != 0) or turns them off. */
 int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5);
+/* Blocks of a single sphere's parallel T1 pass: 0 = automatic (a cooperative grid of about one
+ * block per 3000 vertices from 20000 vertices on, else one block), 1 = one block, n > 1 = a
+ * cooperative grid of n blocks (capped at the device's co-resident count).  Performance only:
+ * the flips and every later value are the same for any count.  Ignored by batches. */
+int svm_model_set_t1_blocks(svm_model* m, int blocks);
 int svm_model_synchronize(svm_model* m);
 /* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
  * z, unused) per vertex in the FP64 form, float4 in the mixed form.  Valid until the next step,

@@ -290,9 +290,11 @@ def test_area_fallback_matches_oracle(svm, oracle_mod):
     assert rel_err(gm.returnForces(), om.forces()) < RTOL_FORCE
 
 
-def test_mass_t1_matches_oracle(svm, oracle_mod):
+@pytest.mark.parametrize("blocks", [1, 4, 64])
+def test_mass_t1_matches_oracle(svm, oracle_mod, blocks):
     """Hundreds of shortened edges, many sharing vertices and cells, in one enforceTopology pass:
-    the parallel pass must give the flips, connectivity and positions of the CPU's sequential loop."""
+    the parallel pass must give the flips, connectivity and positions of the CPU's sequential loop,
+    in one block and spread over a cooperative grid."""
     n = 2000
     pts = svm.random_cell_centres(17, n)
     topo = svm.Topology(pts)
@@ -305,6 +307,7 @@ def test_mass_t1_matches_oracle(svm, oracle_mod):
         pos[u] *= R / np.linalg.norm(pos[u])
     gm = svm.sphericalVertexModel(n, topology=topo, radius=R)
     gm.setT1Threshold(0.04)
+    gm.setT1Blocks(blocks)
     gm.setPositions(pos)
     om = oracle_mod.OracleModel(pos, topo.rings, topo.ringCounts, topo.vertexCells, topo.vertexNeighbors, R)
     om.set_t1_threshold(0.04)
@@ -414,3 +417,29 @@ def test_host_io_steps_chained_with_flips(svm):
     fa, fb = a.t1Stats()["flips"], b.t1Stats()["flips"]
     assert fa == fb and fa > 25
     assert a.computeEnergy() == b.computeEnergy()
+
+
+def test_t1_pass_block_count_does_not_change_the_run(svm):
+    """N = 20k (whose automatic T1 pass is a cooperative grid) against the same run with the pass
+    in one block and in 152 blocks: positions, connectivity and flips bit for bit over 40 steps at
+    a raised threshold (several hundred flips a step)."""
+    runs = []
+    for blocks in (1, 0, 152):
+        m, bd = stabilised(svm, 20000, seed=21, stab=60, steps=40)
+        m.setT1Threshold(0.06)
+        m.setT1Blocks(blocks)
+        m.takeFlips(1 << 20)
+        bd.noise.setReproducibleSeed(5)
+        bd.run(20)
+        for _ in range(20):
+            bd.integrateEquationOfMotion()
+        runs.append((m.returnPositions(), m.vertexNeighbors(), m.rings(32), m.takeFlips(1 << 20),
+                     m.deviceStatus()))
+    ref = runs[0]
+    assert len(ref[3]) > 1000
+    for r in runs[1:]:
+        assert np.array_equal(r[0], ref[0])
+        assert np.array_equal(r[1], ref[1])
+        assert np.array_equal(r[2][0], ref[2][0]) and np.array_equal(r[2][1], ref[2][1])
+        assert np.array_equal(r[3], ref[3])
+        assert r[4] == 0

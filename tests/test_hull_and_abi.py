@@ -155,6 +155,7 @@ def test_abi_rejects_bad_arguments_without_a_device(svm):
                "svm_model_destroy", "svm_fire_destroy", "svm_mlp_destroy", "svm_tuner_destroy"):
         assert getattr(L, fn)(None) == ERR_ARG, fn
     assert L.svm_model_set_precision(None, 1) == ERR_ARG
+    assert L.svm_model_set_t1_blocks(None, 0) == ERR_ARG
     assert L.svm_brownian_step_io(None, 0.0, 0.01, 1.0, 1, None, None, None) == ERR_ARG
     assert L.svm_energy_noalloc(None, None, 1.0, 10, None, None) == ERR_ARG
     cnt = C.c_int()
