@@ -493,61 +493,104 @@ __device__ __forceinline__ void ring16_insert_after(Ring16& R, int after, int ad
 }
 
 __device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs);
+__device__ void t1_move_pair(const ApplyArgs& A, int v1, int v2, D3 p1, D3 p2, D3 vC);
+// Replaces `from` by `to` in the three slots of a vertex's list.
+__device__ __forceinline__ void slots_replace(int4& a, int from, int to) {
+    if (a.x == from) a.x = to;
+    if (a.y == from) a.y = to;
+    if (a.z == from) a.z = to;
+}
 
-__device__ bool t1_flip16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings) {
-    const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
+// A flip of 16-entry rings in three parts: t1_plan16 reads the two vertices' lists and the four
+// rings, classifies the cells (cs), finds the outer neighbours (vs) and checks that the flip is
+// allowed; t1_move_pair moves v1 and v2; t1_commit16 writes the undo entry, the rewired vertex
+// lists (edited in registers, stored whole) and the edited rings.  The loads are grouped by level
+// of dependence so that a flip waits for memory a few times instead of once per access.
+struct FlipPlan16 {
+    int4 c1, c2, n1, n2, ny, nz;   // vertex lists of v1, v2 and of the outer neighbours vs.y, vs.z
+    Ring16 Rc[3], Rw;              // the rings of v1's three cells and of v2's fourth cell
+    int qx, qy, qz;                // which of Rc is cell cs.x, cs.y, cs.z
+};
+__device__ bool t1_plan16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, FlipPlan16& F) {
+    F.c1 = A.vcell[v1]; F.c2 = A.vcell[v2]; F.n1 = A.vnbr[v1]; F.n2 = A.vnbr[v2];
+    const int c[3] = {F.c1.x, F.c1.y, F.c1.z};
     cs.w = -1;
     for (int ff = 0; ff < 3; ++ff) {
-        const int t = compRef(A.vcell, v2, ff);
+        const int t = comp(F.c2, ff);
         if (t != c[0] && t != c[1] && t != c[2]) cs.w = t;
     }
-    Ring16 Rc[3], Rw;
 #pragma unroll
-    for (int q = 0; q < 3; ++q) ring16_load(A, c[q], Rc[q]);
-    if (cs.w >= 0) ring16_load(A, cs.w, Rw);
+    for (int q = 0; q < 3; ++q) ring16_load(A, c[q], F.Rc[q]);
+    if (cs.w >= 0) ring16_load(A, cs.w, F.Rw);
     cs.x = cs.y = cs.z = -1;
-    int qx = 0, qy = 0, qz = 0, yl = 0, yx = 0;
+    F.qx = F.qy = F.qz = 0;
+    int yl = 0, yx = 0;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         int vl, vx;
-        ring16_neighbours(Rc[q], v1, vl, vx);
-        if (vl == v2) { cs.x = c[q]; qx = q; }
-        else if (vx == v2) { cs.z = c[q]; qz = q; }
-        else { cs.y = c[q]; qy = q; yl = vl; yx = vx; }
+        ring16_neighbours(F.Rc[q], v1, vl, vx);
+        if (vl == v2) { cs.x = c[q]; F.qx = q; }
+        else if (vx == v2) { cs.z = c[q]; F.qz = q; }
+        else { cs.y = c[q]; F.qy = q; yl = vl; yx = vx; }
     }
     if (cs.x < 0 || cs.y < 0 || cs.z < 0 || cs.w < 0) { atomicOr(A.status, SVM_DEV_BAD_TOPOLOGY); return false; }
-    Ring16& RX = Rc[qx];
-    Ring16& RY = Rc[qy];
-    Ring16& RZ = Rc[qz];
     vs.x = yl; vs.y = yx;
     int vl, vx;
-    ring16_neighbours(Rw, v2, vl, vx);
+    ring16_neighbours(F.Rw, v2, vl, vx);
     vs.w = vl; vs.z = vx;
     // forbid a T1 that would shrink a triangular cell (sphericalVertexModel.cpp:485-487)
-    if (RX.n == 3 || RZ.n == 3) return false;
-    if (RY.n + 1 > 16 || Rw.n + 1 > 16) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    if (F.Rc[F.qx].n == 3 || F.Rc[F.qz].n == 3) return false;
+    if (F.Rc[F.qy].n + 1 > 16 || F.Rw.n + 1 > 16) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    F.ny = A.vnbr[vs.y];
+    F.nz = A.vnbr[vs.z];
+    return true;
+}
+// p1, p2: the old positions of v1 and v2.
+__device__ void t1_commit16(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs, FlipPlan16& F,
+                            UndoEntry* undo, int* undoRings, D3 p1, D3 p2) {
+    Ring16& RX = F.Rc[F.qx];
+    Ring16& RY = F.Rc[F.qy];
+    Ring16& RZ = F.Rc[F.qz];
+    const bool yz = vs.y == vs.z;  // a vertex next to both (never v1 or v2 themselves)
     if (undo) {
         undo->v1 = v1; undo->v2 = v2; undo->b = vs.y; undo->c = vs.z;
         undo->cells[0] = cs.x; undo->cells[1] = cs.y; undo->cells[2] = cs.z; undo->cells[3] = cs.w;
-        undo->p1 = apos4(A, v1); undo->p2 = apos4(A, v2);
-        undo->vc1 = A.vcell[v1]; undo->vc2 = A.vcell[v2];
-        undo->vn[0] = A.vnbr[v1]; undo->vn[1] = A.vnbr[v2]; undo->vn[2] = A.vnbr[vs.y]; undo->vn[3] = A.vnbr[vs.z];
-        undo->counts[0] = RX.n; undo->counts[1] = RY.n; undo->counts[2] = RZ.n; undo->counts[3] = Rw.n;
+        undo->p1 = make_double4_32a(p1.x, p1.y, p1.z, 0.0); undo->p2 = make_double4_32a(p2.x, p2.y, p2.z, 0.0);
+        undo->vc1 = F.c1; undo->vc2 = F.c2;
+        undo->vn[0] = F.n1; undo->vn[1] = F.n2; undo->vn[2] = F.ny; undo->vn[3] = F.nz;
+        undo->counts[0] = RX.n; undo->counts[1] = RY.n; undo->counts[2] = RZ.n; undo->counts[3] = F.Rw.n;
         ring16_store(undoRings, RX);
         ring16_store(undoRings + 16, RY);
         ring16_store(undoRings + 32, RZ);
-        ring16_store(undoRings + 48, Rw);
+        ring16_store(undoRings + 48, F.Rw);
     }
-    t1_flip_positions(A, v1, v2, cs, vs);
+    // the slot rewiring of t1_flip_positions, slot by slot in the same order (for a shared outer
+    // neighbour both of its replacements apply, the first one first)
+    slots_replace(F.c1, cs.z, cs.w);
+    slots_replace(F.c2, cs.x, cs.y);
+    slots_replace(F.ny, v1, v2);
+    if (yz) slots_replace(F.ny, v2, v1);
+    else slots_replace(F.nz, v2, v1);
+    slots_replace(F.n1, vs.y, vs.z);
+    slots_replace(F.n2, vs.z, vs.y);
+    A.vcell[v1] = F.c1; A.vcell[v2] = F.c2; A.vnbr[v1] = F.n1; A.vnbr[v2] = F.n2; A.vnbr[vs.y] = F.ny;
+    if (!yz) A.vnbr[vs.z] = F.nz;
     ring16_remove(RX, v2);
     ring16_insert_after(RY, v1, v2);
     ring16_remove(RZ, v1);
-    ring16_insert_after(Rw, v2, v1);
+    ring16_insert_after(F.Rw, v2, v1);
     ring16_store(A.ring + (long)cs.x * 16, RX);
     ring16_store(A.ring + (long)cs.y * 16, RY);
     ring16_store(A.ring + (long)cs.z * 16, RZ);
-    ring16_store(A.ring + (long)cs.w * 16, Rw);
-    A.ringCount[cs.x] = RX.n; A.ringCount[cs.y] = RY.n; A.ringCount[cs.z] = RZ.n; A.ringCount[cs.w] = Rw.n;
+    ring16_store(A.ring + (long)cs.w * 16, F.Rw);
+    A.ringCount[cs.x] = RX.n; A.ringCount[cs.y] = RY.n; A.ringCount[cs.z] = RZ.n; A.ringCount[cs.w] = F.Rw.n;
+}
+__device__ bool t1_flip16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings) {
+    FlipPlan16 F;
+    if (!t1_plan16(A, v1, v2, cs, vs, F)) return false;
+    const D3 p1 = apos(A, v1), p2 = apos(A, v2);
+    t1_move_pair(A, v1, v2, p1, p2, apos(A, vs.z));
+    t1_commit16(A, v1, v2, cs, vs, F, undo, undoRings, p1, p2);
     return true;
 }
 
@@ -601,10 +644,21 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
 // The rotation and separation of v1 and v2 and the rewiring of the vertex lists
 // (sphericalVertexModel.cpp:513-573), shared by both paths of t1_flip.
 __device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs) {
-    D3 p1 = apos(A, v1), p2 = apos(A, v2);
+    t1_move_pair(A, v1, v2, apos(A, v1), apos(A, v2), apos(A, vs.z));
+    for (int k = 0; k < 3; ++k) {
+        if (compRef(A.vcell, v1, k) == cs.z) compRef(A.vcell, v1, k) = cs.w;
+        if (compRef(A.vcell, v2, k) == cs.x) compRef(A.vcell, v2, k) = cs.y;
+        if (compRef(A.vnbr, vs.y, k) == v1) compRef(A.vnbr, vs.y, k) = v2;
+        if (compRef(A.vnbr, vs.z, k) == v2) compRef(A.vnbr, vs.z, k) = v1;
+        if (compRef(A.vnbr, v1, k) == vs.y) compRef(A.vnbr, v1, k) = vs.z;
+        if (compRef(A.vnbr, v2, k) == vs.z) compRef(A.vnbr, v2, k) = vs.y;
+    }
+}
+// The rotation of v1 and v2 by a quarter turn about their midpoint and their separation
+// (sphericalVertexModel.cpp:495-515), from their positions and that of the third vertex vC.
+__device__ void t1_move_pair(const ApplyArgs& A, int v1, int v2, D3 p1, D3 p2, D3 vC) {
     D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
     mid = renorm_exact(mid, 1.0);
-    const D3 vC = apos(A, vs.z);
     double det = vC.x * (p1.y * p2.z - p1.z * p2.y) + vC.y * (p1.z * p2.x - p1.x * p2.z) + vC.z * (p1.x * p2.y - p1.y * p2.x);
     det = det > 0 ? 1. : -1.;
     // theta = -0.5 det kPI (sphericalVertexModel.cpp:507-508)
@@ -616,14 +670,56 @@ __device__ void t1_flip_positions(const ApplyArgs& A, int v1, int v2, const int4
     const double R = aR(A, v1);
     apos_st(A, v1, renorm_exact(p1, R));
     apos_st(A, v2, renorm_exact(p2, R));
-    for (int k = 0; k < 3; ++k) {
-        if (compRef(A.vcell, v1, k) == cs.z) compRef(A.vcell, v1, k) = cs.w;
-        if (compRef(A.vcell, v2, k) == cs.x) compRef(A.vcell, v2, k) = cs.y;
-        if (compRef(A.vnbr, vs.y, k) == v1) compRef(A.vnbr, vs.y, k) = v2;
-        if (compRef(A.vnbr, vs.z, k) == v2) compRef(A.vnbr, vs.z, k) = v1;
-        if (compRef(A.vnbr, v1, k) == vs.y) compRef(A.vnbr, v1, k) = vs.z;
-        if (compRef(A.vnbr, v2, k) == vs.z) compRef(A.vnbr, v2, k) = vs.y;
+}
+constexpr unsigned kFull = 0xffffffffu;
+// t1_move_pair by a whole warp: the rotation and renormalisation of v1 on the even lanes and of v2
+// on the odd ones, the rest on every lane alike (an FP64 instruction costs a warp the same
+// whatever its active lanes, so the pair takes two-thirds of the instructions of one thread).
+// Lane 0 stores v1, lane 1 stores v2; the values are t1_move_pair's.
+__device__ void t1_move_pair_warp(const ApplyArgs& A, int v1, int v2, D3 p1, D3 p2, D3 vC, int lane) {
+    D3 mid{__dmul_rn(0.5, __dadd_rn(p1.x, p2.x)), __dmul_rn(0.5, __dadd_rn(p1.y, p2.y)), __dmul_rn(0.5, __dadd_rn(p1.z, p2.z))};
+    mid = renorm_exact(mid, 1.0);
+    double det = vC.x * (p1.y * p2.z - p1.z * p2.y) + vC.y * (p1.z * p2.x - p1.x * p2.z) + vC.z * (p1.x * p2.y - p1.y * p2.x);
+    det = det > 0 ? 1. : -1.;
+    const bool second = lane & 1;
+    const D3 q = rodrigues(second ? p2 : p1, mid, kCosHalfPi, -det);
+    const D3 o{__shfl_xor_sync(kFull, q.x, 1), __shfl_xor_sync(kFull, q.y, 1), __shfl_xor_sync(kFull, q.z, 1)};
+    const D3 r1 = second ? o : q, r2 = second ? q : o;
+    const D3 diff{__dmul_rn(0.5, __dsub_rn(r1.x, r2.x)), __dmul_rn(0.5, __dsub_rn(r1.y, r2.y)), __dmul_rn(0.5, __dsub_rn(r1.z, r2.z))};
+    const D3 w = second ? D3{__dsub_rn(r2.x, diff.x), __dsub_rn(r2.y, diff.y), __dsub_rn(r2.z, diff.z)}
+                        : D3{__dadd_rn(r1.x, diff.x), __dadd_rn(r1.y, diff.y), __dadd_rn(r1.z, diff.z)};
+    const D3 n = renorm_exact(w, aR(A, v1));
+    if (lane == 0) apos_st(A, v1, n);
+    else if (lane == 1) apos_st(A, v2, n);
+}
+__device__ __forceinline__ int4 shfl0(int4 a) {
+    return make_int4(__shfl_sync(kFull, a.x, 0), __shfl_sync(kFull, a.y, 0), __shfl_sync(kFull, a.z, 0),
+                     __shfl_sync(kFull, a.w, 0));
+}
+// t1_flip by a whole warp (every lane calls it with the same arguments; p1, p2 are the old
+// positions of v1 and v2): lane 0 plans and commits the topology, the warp moves the pair.  Same
+// writes as t1_flip; the warp's lanes see them after it returns.
+__device__ bool t1_flip_warp(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings,
+                             D3 p1, D3 p2, int lane) {
+    int ok = 0;
+    if (A.Wc != 16) {  // other ring capacities: lane 0 alone
+        if (lane == 0) ok = t1_flip(A, v1, v2, cs, vs, undo, undoRings) ? 1 : 0;
+        ok = __shfl_sync(kFull, ok, 0);
+        cs = shfl0(cs);
+        vs = shfl0(vs);
+        __syncwarp();
+        return ok != 0;
     }
+    FlipPlan16 F;
+    if (lane == 0) ok = t1_plan16(A, v1, v2, cs, vs, F) ? 1 : 0;
+    ok = __shfl_sync(kFull, ok, 0);
+    if (!ok) return false;
+    cs = shfl0(cs);
+    vs = shfl0(vs);
+    t1_move_pair_warp(A, v1, v2, p1, p2, apos(A, vs.z), lane);
+    if (lane == 0) t1_commit16(A, v1, v2, cs, vs, F, undo, undoRings, p1, p2);
+    __syncwarp();
+    return true;
 }
 
 // Ring bookkeeping (vrpos/vlast/vnext) and corners of the cells whose rings a T1 pass changed,
@@ -668,6 +764,25 @@ __device__ void t1_undo(const ApplyArgs& A, const UndoEntry& u, const int* undoR
         A.ringCount[cell] = u.counts[q];
         for (int k = 0; k < u.counts[q]; ++k) A.ring[(long)cell * A.Wc + k] = undoRings[q * A.Wc + k];
     }
+}
+
+// A position as the T1 test reads it: FP64, or FP32 with the replica index (mixed form; the
+// conversions to double and back are exact).
+struct TPos { double x, y, z; int rep; };
+__device__ __forceinline__ TPos tpos(const ApplyArgs& A, int i) {
+    if (A.pos32) {
+        const float4 q = A.pos32[i];
+        return TPos{q.x, q.y, q.z, rep_of(q)};
+    }
+    const D3 p = ld3(A.pos, i);
+    return TPos{p.x, p.y, p.z, 0};
+}
+// The length test of t1_candidate on positions already loaded (a = vertex v, b = neighbour u).
+__device__ __forceinline__ bool t1_short(const ApplyArgs& A, const TPos& a, const TPos& b) {
+    if (A.pos32)
+        return arc32(make_float4((float)a.x, (float)a.y, (float)a.z, 0.f), make_float4((float)b.x, (float)b.y, (float)b.z, 0.f),
+                     (float)A.repR[a.rep]) < (float)A.t1Threshold;
+    return shorter_than(D3{a.x, a.y, a.z}, D3{b.x, b.y, b.z}, A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
 }
 
 __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
@@ -825,9 +940,14 @@ __device__ __forceinline__ void t1_footprint(const ApplyArgs& A, int p, int* f) 
     f[8] = c1.x; f[9] = c1.y; f[10] = c1.z; f[11] = c2.x; f[12] = c2.y; f[13] = c2.z;
 }
 
-constexpr int kParThreads = 1024;       // one segment: the whole sphere
+// Vertex a of (v1, v2, vs.x, vs.y, vs.z, vs.w): the six whose slots a flip re-tests.
+__device__ __forceinline__ int pick_aff(int a, int v1, int v2, const int4& vs) {
+    return a == 0 ? v1 : a == 1 ? v2 : a == 2 ? vs.x : a == 3 ? vs.y : a == 4 ? vs.z : vs.w;
+}
+
+constexpr int kParThreads = 512;        // one segment: the whole sphere
 constexpr int kParThreadsBatch = 256;   // one segment per replica
-constexpr int kCoopThreads = 128;       // per block of a cooperative single-sphere pass
+constexpr int kCoopThreads = 256;       // per block of a cooperative single-sphere pass
 
 // Block-wide exclusive scan of one int per thread; returns the block total in *total.
 __device__ int block_excl_scan(int v, int* total) {
@@ -917,9 +1037,14 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
     T1Ctl* ctl = kCoop ? t1.ctl : &sctl;
     const int tid = threadIdx.x, seg = kCoop ? 0 : blockIdx.x;
     const bool leader = !kCoop || blockIdx.x == 0;  // extracts the positions and finishes the pass
-    // this thread's first position of a round and the stride (positions spread over the blocks)
+    // this thread's first position of a round and the stride (reserve and release phases), and
+    // this warp's (run phase: one warp per position).  Consecutive positions go to different
+    // blocks of a cooperative grid.
+    const int lane = tid & 31, warps = blockDim.x >> 5;
     const int gi = kCoop ? blockIdx.x + gridDim.x * tid : tid;
     const int gs = kCoop ? gridDim.x * blockDim.x : blockDim.x;
+    const int wi = kCoop ? blockIdx.x + gridDim.x * (tid >> 5) : (tid >> 5);
+    const int ws = kCoop ? gridDim.x * warps : warps;
     // one segment and nothing flagged: nothing to do.  (With several segments every block runs:
     // the last one to finish does the pass's cleanup.)  The count is read by every block before
     // the first grid barrier, so before block 0 can change it.
@@ -1041,63 +1166,79 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
             rollback = true;
             break;
         }
-        // run the positions that hold their whole footprint
-        for (int i = gi; i < nCur; i += gs) {
+        // run the positions that hold their whole footprint: one warp per position, its lanes
+        // sharing the reservation checks, the pair's rotation and the 18 re-tests (decisions and
+        // every write as for one thread per position)
+        for (int i = wi; i < nCur; i += ws) {
             const int p = cur[i];
             const int* f = fpB + (long)i * kFootprint;
-            bool ready = true;
-            for (int k = 0; k < 8; ++k) ready &= t1.resV[f[k]] == p;
-            for (int k = 8; k < kFootprint; ++k) ready &= t1.resC[f[k]] == p;
-            if (!ready) {
-                const int ni = atomicAdd(&ctl->next[par], 1);
-                if (ni < capB) nxt[ni] = p;
-                else atomicExch(&ctl->rollback, 1);
+            // the edge (f[0], f[1]) is p's; its positions load alongside the reservation words (if
+            // p does not hold its footprint they may be changing, and are not used)
+            const int v1 = f[0], v2 = f[1];
+            const TPos P1 = tpos(A, v1), P2 = tpos(A, v2);
+            const int fk = lane < kFootprint ? f[lane] : 0;
+            bool held = true;
+            if (lane < kFootprint) held = (lane < 8 ? t1.resV[fk] : t1.resC[fk]) == p;
+            if (!__all_sync(kFull, held)) {
+                if (lane == 0) {
+                    const int ni = atomicAdd(&ctl->next[par], 1);
+                    if (ni < capB) nxt[ni] = p;
+                    else atomicExch(&ctl->rollback, 1);
+                }
                 continue;
             }
-            const int ci = atomicAdd(&ctl->exec, 1);
-            if (ci >= capB) { atomicExch(&ctl->rollback, 1); continue; }
-            for (int k = 0; k < kFootprint; ++k) comB[(long)ci * kFootprint + k] = f[k];
-            for (int k = 0; k < 8; ++k) atomicMax(t1.comV + f[k], p);
-            for (int k = 8; k < kFootprint; ++k) atomicMax(t1.comC + f[k], p);
-            atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
-            if (!t1_candidate(A, p)) continue;
-            const int ui = atomicAdd(&ctl->undo, 1);
-            if (ui >= undoPer) { atomicExch(&ctl->rollback, 1); continue; }
-            const int v1 = p / 3, v2 = compRef(A.vnbr, v1, p - 3 * v1);
+            int ci = 0;
+            if (lane == 0) ci = atomicAdd(&ctl->exec, 1);
+            ci = __shfl_sync(kFull, ci, 0);
+            if (ci >= capB) { if (lane == 0) atomicExch(&ctl->rollback, 1); continue; }
+            if (lane < kFootprint) {
+                comB[(long)ci * kFootprint + lane] = fk;
+                atomicMax((lane < 8 ? t1.comV : t1.comC) + fk, p);
+            }
+            if (lane == 0) atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
+            if (!(v1 < v2 && t1_short(A, P1, P2))) continue;  // t1_candidate(A, p), on every lane alike
+            int ui = 0;
+            if (lane == 0) ui = atomicAdd(&ctl->undo, 1);
+            ui = __shfl_sync(kFull, ui, 0);
+            if (ui >= undoPer) { if (lane == 0) atomicExch(&ctl->rollback, 1); continue; }
             int4 cs, vs;
             UndoEntry* u = undoB + ui;
-            if (!t1_flip(A, v1, v2, cs, vs, u, undoRingsB + (long)ui * 4 * A.Wc)) {
-                u->v1 = -1;  // nothing was written
+            if (!t1_flip_warp(A, v1, v2, cs, vs, u, undoRingsB + (long)ui * 4 * A.Wc, D3{P1.x, P1.y, P1.z},
+                              D3{P2.x, P2.y, P2.z}, lane)) {
+                if (lane == 0) u->v1 = -1;  // nothing was written
                 continue;
             }
-            atomicAdd(&ctl->flips, 1);
-            const int fc = atomicAdd(t1.flipCount, 1);
-            u->logIdx = fc;
-            if (fc < t1.flipLogCap) {
-                int* e = t1.flipLog + 4 * fc;
-                e[0] = *t1.pass; e[1] = p; e[2] = v1; e[3] = v2;
-            }
-            const int tc = atomicAdd(t1.ctr + 5, 4);
-            if (tc + 4 <= t1.touchedCap) {
-                t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
-            } else {
-                atomicExch(&ctl->rollback, 1);
-            }
-            // re-test the 18 slots of the six vertices whose slots or positions the flip changed:
-            // all tests first (independent loads that overlap), then the flagging
-            const int aff[6] = {v1, v2, vs.x, vs.y, vs.z, vs.w};
-            bool again[18];
-#pragma unroll
-            for (int a = 0; a < 6; ++a)
-#pragma unroll
-                for (int sl = 0; sl < 3; ++sl) {
-                    const int r = 3 * aff[a] + sl;
-                    again[3 * a + sl] = r > p && r < qHi && t1_candidate(A, r);
+            if (lane == 0) {
+                atomicAdd(&ctl->flips, 1);
+                const int fc = atomicAdd(t1.flipCount, 1);
+                u->logIdx = fc;
+                if (fc < t1.flipLogCap) {
+                    int* e = t1.flipLog + 4 * fc;
+                    e[0] = *t1.pass; e[1] = p; e[2] = v1; e[3] = v2;
                 }
-            for (int a = 0; a < 6; ++a)
-                for (int sl = 0; sl < 3; ++sl) {
-                    const int r = 3 * aff[a] + sl;
-                    if (!again[3 * a + sl]) continue;
+                const int tc = atomicAdd(t1.ctr + 5, 4);
+                if (tc + 4 <= t1.touchedCap) {
+                    t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
+                } else {
+                    atomicExch(&ctl->rollback, 1);
+                }
+            }
+            // re-test the 18 slots of the six vertices whose slots or positions the flip changed
+            // (t1_candidate on each): lane l < 18 tests slot l % 3 of vertex l / 3 of
+            // (v1, v2, vs.x, vs.y, vs.z, vs.w); lane 0 then flags the new candidates in that order
+            bool again = false;
+            if (lane < 18) {
+                const int a = lane / 3, sl = lane - 3 * (lane / 3);
+                const int v = pick_aff(a, v1, v2, vs);
+                const int r = 3 * v + sl;
+                const int w = compRef(A.vnbr, v, sl);
+                again = r > p && r < qHi && v < w && t1_short(A, tpos(A, v), tpos(A, w));
+            }
+            const unsigned hits = __ballot_sync(kFull, again);
+            if (lane == 0) {
+                for (unsigned m = hits; m; m &= m - 1u) {
+                    const int l = __ffs(m) - 1;
+                    const int r = 3 * pick_aff(l / 3, v1, v2, vs) + (l - 3 * (l / 3));
                     const unsigned bit = 1u << (r & 31);
                     if (!(atomicOr(t1.bits + (r >> 5), bit) & bit)) {
                         atomicOr(t1.summary + (r >> 10), 1u << ((r >> 5) & 31));
@@ -1106,6 +1247,7 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
                         else atomicExch(&ctl->rollback, 1);
                     }
                 }
+            }
         }
         if (!group_sync()) return;
         lap(2);
