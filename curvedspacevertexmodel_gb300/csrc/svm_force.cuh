@@ -108,11 +108,20 @@ __device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
     return f;
 }
 
+// The geodesic-length gradient at v towards its ring predecessor in cell slot s, in Cartesian
+// form: vertex_force's gG[s].  Each neighbour of v is the predecessor in one of its cells and the
+// successor in another, so the three of them cover both terms of every slot.
+__device__ __forceinline__ D3 slot_geodesic(const ForceArgs& A, int v, int s) {
+    const double4_32a sv = A.vsph[v];
+    return from_basis(sv, grad_geodesic(sv, A.vsph[comp(A.vlast[v], s)]));
+}
+
 // The contribution of cell slot s to the force on vertex v: one term of vertex_force's (or
 // vertex_force_vec's) sum, with the same operations, so that summing the three terms in slot order
 // and skipping a NaN term, as those functions do, gives the same force bit for bit.  Lets three
-// threads share a vertex (more warps in flight when the vertex count is small).
-__device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s) {
+// threads share a vertex (more warps in flight when the vertex count is small).  gG: the vertex's
+// three slot_geodesic values (reference form only).
+__device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s, const D3* gG) {
     const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
     const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
     if (A.vec) {
@@ -137,10 +146,11 @@ __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s) {
     const double4_32a sl = A.vsph[L], sx = A.vsph[X];
     const double pp = 2.0 * dP;
     const double aa = 2.0 * A.Kr * dA;
+    const int jx = X == lasts.x ? 0 : (X == lasts.y ? 1 : (X == lasts.z ? 2 : -1));
     D3 fs{0.0, 0.0, 0.0}, t;
-    t = from_basis(sv, grad_geodesic(sv, sl));
+    t = pick3(gG, s);
     fs = sub3(fs, scl3(pp, t));
-    t = from_basis(sv, grad_geodesic(sv, sx));
+    t = jx >= 0 ? pick3(gG, jx) : from_basis(sv, grad_geodesic(sv, sx));
     fs = sub3(fs, scl3(pp, t));
     t = from_basis(sv, grad_triangle(sv, sl, sc, p, pl, cp, A.R));
     fs = sub3(fs, scl3(aa, t));
@@ -150,24 +160,39 @@ __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s) {
 }
 
 // Block-level force of kSlotVerts vertices by 3 kSlotVerts threads (thread 3 i + s computes slot s
-// of vertex i of the block); threads i < kSlotVerts receive vertex i's force in slot order.
+// of vertex i of the block); threads i < kSlotVerts receive vertex i's force in slot order.  The
+// geodesic gradients of the reference form are evaluated once per neighbour (thread 3 i + s for
+// the predecessor in slot s) and shared through the block.
 constexpr int kSlotVerts = 64;
 struct SlotShared { double x[3 * kSlotVerts], y[3 * kSlotVerts], z[3 * kSlotVerts]; };
 __device__ __forceinline__ D3 block_slot_force(const ForceArgs& A, int nV, SlotShared& sh) {
     const int t = threadIdx.x, base = blockIdx.x * kSlotVerts;
     const int vi = t / 3, s = t - 3 * (t / 3);
     const int v = base + vi;
-    if (v < nV) {
-        const D3 fs = slot_force(A, v, s);
-        sh.x[t] = fs.x; sh.y[t] = fs.y; sh.z[t] = fs.z;
+    if (!A.vec) {
+        if (v < nV) {
+            const D3 g = slot_geodesic(A, v, s);
+            sh.x[t] = g.x; sh.y[t] = g.y; sh.z[t] = g.z;
+        }
+        __syncthreads();
     }
+    D3 fs{0.0, 0.0, 0.0};
+    if (v < nV) {
+        D3 gG[3];
+        if (!A.vec)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) gG[j] = D3{sh.x[3 * vi + j], sh.y[3 * vi + j], sh.z[3 * vi + j]};
+        fs = slot_force(A, v, s, gG);
+    }
+    __syncthreads();
+    if (v < nV) { sh.x[t] = fs.x; sh.y[t] = fs.y; sh.z[t] = fs.z; }
     __syncthreads();
     D3 f{0.0, 0.0, 0.0};
     if (t < kSlotVerts && base + t < nV) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            const D3 fs{sh.x[3 * t + q], sh.y[3 * t + q], sh.z[3 * t + q]};
-            if (!isnan(fs.x)) f = add3(f, fs);
+            const D3 fq{sh.x[3 * t + q], sh.y[3 * t + q], sh.z[3 * t + q]};
+            if (!isnan(fq.x)) f = add3(f, fq);
         }
     }
     return f;
@@ -191,17 +216,60 @@ __device__ __forceinline__ double u53(unsigned a, unsigned b) {
     const unsigned long long x = ((unsigned long long)a << 21) ^ (unsigned long long)(b >> 11);
     return ((double)(x & ((1ull << 53) - 1)) + 0.5) * 0x1.0p-53;
 }
-// Three standard normals for (vertex, step) by Box-Muller on two Philox draws.
-__device__ __forceinline__ D3 philox_normals3(uint64_t seed, unsigned long long step, int v) {
+
+// Standard normals by the ziggurat method (G. Marsaglia and W. W. Tsang, "The Ziggurat Method for
+// Generating Random Variables", J. Stat. Softw. 5(8), 2000) with 256 layers of equal area v under
+// f(x) = exp(-x^2/2): layer i >= 1 is the box [0, x_i) x [f(x_i), f(x_{i+1})), layer 0 the box
+// [0, v / f(r)) x [0, f(r)) together with the tail beyond r = x_1.  A uniform layer, sign and
+// u in [0, 1) give x = u x_i, accepted at once when x < x_{i+1} (98.5% of draws); otherwise layer 0
+// samples the tail (Marsaglia's x = -ln(u1) / r, y = -ln(u2), accepted when 2y > x^2) and the other
+// layers test the wedge against f(x), starting over on rejection.  The bits: one Philox draw's
+// 64-bit halves for the fast path, a fresh draw per retry.
+struct ZigTable {
+    double x[257];  // x_0 = v / f(r), x_1 = r, ..., x_256 = 0
+    double f[257];  // f(x_i) (f_0 unused)
+};
+constexpr double kZigR = 3.654152885361009;  // r for 256 layers
+// Layer, sign and a 53-bit u in [0, 1) from 64 bits.
+__device__ __forceinline__ double zig_draw(const ZigTable* __restrict__ Z, unsigned a, unsigned b, int& i, bool& neg) {
+    i = (int)(a & 255u);
+    neg = (a >> 8) & 1u;
+    const unsigned long long n = ((unsigned long long)(a >> 9) << 30) | (unsigned long long)(b >> 2);
+    return (double)n * 0x1.0p-53 * __ldg(Z->x + i);
+}
+static __device__ __noinline__ double zig_slow(const ZigTable* __restrict__ Z, int i, double x, bool neg, uint4 ctr, uint2 key) {
+    for (int attempt = 0; attempt < 32; ++attempt) {  // each round fails with probability < 0.02
+        ctr.w += 1u;
+        const uint4 r = philox4x32_10(ctr, key);
+        if (i == 0) {
+            const double xt = -log(u53(r.x, r.y)) / kZigR, y = -log(u53(r.z, r.w));
+            if (y + y > xt * xt) return neg ? -(kZigR + xt) : kZigR + xt;
+            continue;
+        }
+        const double y = __ldg(Z->f + i) + u53(r.x, r.y) * (__ldg(Z->f + i + 1) - __ldg(Z->f + i));
+        if (y < exp(-0.5 * x * x)) return neg ? -x : x;
+        x = zig_draw(Z, r.z, r.w, i, neg);
+        if (x < __ldg(Z->x + i + 1)) return neg ? -x : x;
+    }
+    return neg ? -x : x;
+}
+__device__ __forceinline__ double zig_normal(const ZigTable* __restrict__ Z, unsigned a, unsigned b, uint4 ctr, uint2 key) {
+    int i;
+    bool neg;
+    const double x = zig_draw(Z, a, b, i, neg);
+    if (x < __ldg(Z->x + i + 1)) return neg ? -x : x;
+    return zig_slow(Z, i, x, neg, ctr, key);
+}
+// Three standard normals for (vertex, step): two Philox draws (counter words 0 and 1) give the
+// three fast-path draws; normal j retries on counter words 64 (j + 1) + 1, 2, ...
+__device__ __forceinline__ D3 philox_normals3(const ZigTable* __restrict__ Z, uint64_t seed, unsigned long long step, int v) {
     const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
-    const uint4 r0 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 0u), key);
-    const uint4 r1 = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 1u), key);
-    const double a = sqrt(-2.0 * log(u53(r0.x, r0.y)));
-    double s0, c0;
-    sincospi(2.0 * u53(r0.z, r0.w), &s0, &c0);
-    const double b = sqrt(-2.0 * log(u53(r1.x, r1.y)));
-    const double c1 = cospi(2.0 * u53(r1.z, r1.w));
-    return D3{a * c0, a * s0, b * c1};
+    const uint4 c0 = make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 0u);
+    const uint4 r0 = philox4x32_10(c0, key);
+    const uint4 r1 = philox4x32_10(make_uint4(c0.x, c0.y, c0.z, 1u), key);
+    return D3{zig_normal(Z, r0.x, r0.y, make_uint4(c0.x, c0.y, c0.z, 64u), key),
+              zig_normal(Z, r0.z, r0.w, make_uint4(c0.x, c0.y, c0.z, 128u), key),
+              zig_normal(Z, r1.x, r1.y, make_uint4(c0.x, c0.y, c0.z, 192u), key)};
 }
 
 // disp_d = xi_d sqrt(2 dt mu T) + F_d dt mu (brownianDynamics.cpp:37-44), products rounded

@@ -402,6 +402,7 @@ int mixed_max_block_force();
 int max_block_cells_batch();
 void batch_tuner_untimed(svm_model* m, int calls);
 // FP64 force kernels (svm_force_kernels.cu)
+int zig_init();  // the device's normal-sampling table (svm_force_kernels.cu), before the first Brownian step
 int launch_force_fp64(svm_model* m);
 int launch_force_bd_fp64(svm_model* m, double np, double fp, int noiseMode, const double* noise, uint64_t seed,
                          int nxt);

@@ -1735,7 +1735,7 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     cudaMemset(m->t1.comC, 0xff, nC * sizeof(int));
     std::vector<double2> pref(nC, make_double2(1.0, 3.8));
     cudaMemcpy(m->pref, pref.data(), nC * sizeof(double2), cudaMemcpyHostToDevice);
-    if (cudaDeviceSynchronize() != cudaSuccess) { svm_model_destroy(m); return SVM_ERR_CUDA; }
+    if (cudaDeviceSynchronize() != cudaSuccess || zig_init() != SVM_OK) { svm_model_destroy(m); return SVM_ERR_CUDA; }
     *out = m;
     return SVM_OK;
 }

@@ -227,7 +227,9 @@ def test_graph_run_equals_step_loop(svm, gold):
 
 
 def test_philox_noise_statistics(svm):
-    """Brownian displacements with negligible forces: tangential variance 2 dt mu T per direction."""
+    """Brownian displacements with negligible forces over four steps: the tangential components are
+    standard normals times sqrt(2 dt mu T) (variance, mean, kurtosis, two- and three-sigma tail
+    fractions), as the in-kernel Philox + ziggurat sampler must give."""
     n = 20000
     m = svm.sphericalVertexModel(n, svm.noiseSource())
     m.setScalarModelParameter(0.0)
@@ -238,11 +240,25 @@ def test_philox_noise_statistics(svm):
     T, dt = 1e6, 1e-8
     bd.setT(T)
     bd.setDeltaT(dt)
-    p0 = m.returnPositions()
-    bd.integrateEquationOfMotion()
-    d = m.returnPositions() - p0
-    var = np.mean(np.sum(d * d, axis=1)) / 2.0  # two tangential directions
-    assert abs(var / (2 * dt * T) - 1.0) < 0.03
+    z = []
+    for _ in range(4):
+        p0 = m.returnPositions()
+        bd.integrateEquationOfMotion()
+        d = m.returnPositions() - p0
+        nrm = p0 / np.linalg.norm(p0, axis=1, keepdims=True)
+        ref = np.where(np.abs(nrm[:, 2:3]) < 0.9, np.array([[0.0, 0.0, 1.0]]), np.array([[1.0, 0.0, 0.0]]))
+        e1 = np.cross(nrm, ref)
+        e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+        e2 = np.cross(nrm, e1)
+        z.append(np.sum(d * e1, axis=1))
+        z.append(np.sum(d * e2, axis=1))
+    z = np.concatenate(z) / np.sqrt(2 * dt * T)
+    k = z.size  # 320k samples
+    assert abs(np.mean(z * z) - 1.0) < 0.01
+    assert abs(np.mean(z)) < 5.0 / np.sqrt(k)
+    assert abs(np.mean(z ** 4) / np.mean(z * z) ** 2 - 3.0) < 0.05
+    assert abs(np.mean(np.abs(z) > 2.0) - 0.0455003) < 0.002
+    assert abs(np.mean(np.abs(z) > 3.0) - 0.0026998) < 0.0005
 
 
 def test_large_sphere_invariants(svm):
@@ -325,15 +341,13 @@ def test_mass_t1_matches_oracle(svm, oracle_mod, blocks):
 
 def test_t1_trajectory_n20k_matches_oracle(svm, oracle_mod):
     """N = 20k from the stabilised preparation: 30 Brownian steps with the reference's noise stream
-    on both sides; the T1 flips (CPU order) and the connectivity agree at every step; the median
-    vertex stays at the last-bit level and the tail near collapsing edges below 1e-3 R."""
+    on both sides, the oracle restarted from the device's state before every step; the T1 flips
+    (CPU order), the connectivity and the positions agree after every step.  (Run freely, the two
+    drift apart at the last-bit level through acos, and after some steps an edge within rounding of
+    the threshold is decided differently; restarting each step keeps every decision comparable.)"""
     n = 20000
     m, _ = stabilised(svm, n, seed=8, stab=100, steps=100)
     R = m.radius
-    rings, counts = m.rings(32)
-    om = oracle_mod.OracleModel(m.returnPositions(), rings, counts, m.vertexCellNeighbors(), m.vertexNeighbors(), R)
-    om.set_preferred(1.0, 3.8)
-    om.set_t1_threshold(0.04)
     bd = svm.brownianDynamics()
     bd.setModel(m)
     bd.setT(0.01)
@@ -341,22 +355,24 @@ def test_t1_trajectory_n20k_matches_oracle(svm, oracle_mod):
     m.takeFlips(1 << 20)  # drop the preparation's flips
     total = 0
     for step in range(30):
+        rings, counts = m.rings(32)
+        om = oracle_mod.OracleModel(m.returnPositions(), rings, counts, m.vertexCellNeighbors(), m.vertexNeighbors(), R)
+        om.set_preferred(1.0, 3.8)
+        om.set_t1_threshold(0.04)
         xi = noise.normals(3 * m.nVertices)
         bd.injectNoise(xi)
         bd.integrateEquationOfMotion()
         om.brownian_step_noise(xi, 0.01, 0.01, 1.0)
         fg, fo = m.takeFlips(1 << 20), om.flips()
         assert np.array_equal(fg, fo), step
+        assert same_rings(m, om, 32), step
+        assert np.array_equal(m.vertexNeighbors(), om.vertex_neighbors()), step
+        # one step from the same state: the reference's 1/theta^2-conditioned gradients at
+        # collapsing edges amplify acos's last-bit differences, the bulk stays at the last bit
+        d = np.abs(m.returnPositions() - om.positions()).max(axis=1) / R
+        assert np.quantile(d, 0.5) < 1e-13 and d.max() < 1e-6, (step, np.quantile(d, 0.5), d.max())
         total += len(fo)
     assert total > 30
-    assert same_rings(m, om, 32)
-    assert np.array_equal(m.vertexNeighbors(), om.vertex_neighbors())
-    # At R = 40 the arcs are ten times shorter than at N = 200, so the 1/theta^2 conditioning of
-    # the reference's gradients is ~100 times stronger: the few vertices at collapsing edges
-    # separate visibly while the bulk stays at the last-bit level.
-    d = np.abs(m.returnPositions() - om.positions()).max(axis=1) / R
-    q = {p: float(np.quantile(d, p)) for p in (0.5, 0.99, 0.999, 1.0)}
-    assert q[0.5] < 1e-9 and q[0.99] < 1e-5 and q[1.0] < 1e-3, q
 
 
 def test_fire_outliving_its_model(svm, gold):
