@@ -78,6 +78,13 @@ __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
     return R * acos(num / den);
 }
+// |p| as geodesic and sph_coords evaluate it (same operations, so the same value)
+__device__ __forceinline__ double pos_norm(D3 p) { return sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
+// geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
+__device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
+    const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
+    return R * acos(num / (n1 * n2));
+}
 // The T1 length test geodesic(p1, p2) < t, i.e. R acos(c) < t with c = p1.p2 / (|p1||p2|).  acos
 // is decreasing, so away from c = cos(t / R) the answer is c > cos(t / R); the formula itself is
 // evaluated only when c lies within [cosLo, cosHi], a bracket around cos(t / R) of half-width
@@ -187,13 +194,13 @@ __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
 // Spherical coordinates of a point as the reference's gradients compute them
 // (sphericalDomain.h:218-232, 251-261): cos t = z/|p|, sin t = sqrt(1 - cos^2 t),
 // cos p = x / sqrt(x^2+y^2), sin p = y / sqrt(x^2+y^2).
-__device__ __forceinline__ double4_32a sph_coords(D3 p) {
-    double r = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+__device__ __forceinline__ double4_32a sph_coords_n(D3 p, double r) {  // r = pos_norm(p)
     double cosT = p.z / r;
     double sinT = sqrt(1. - cosT * cosT);
     double rxy = sqrt(p.x * p.x + p.y * p.y);
     return make_double4_32a(cosT, sinT, p.x / rxy, p.y / rxy);
 }
+__device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n(p, pos_norm(p)); }
 
 // gradientGeodesicDistance (sphericalDomain.h:248-273) in the (theta, phi) basis of v1:
 // returns (d/dtheta, d/dphi) components.
@@ -308,6 +315,7 @@ struct svm_model {
     int t1Blocks = 0;                  // svm_model_set_t1_blocks (0: automatic)
     double4_32a* pos[2] = {nullptr, nullptr};
     double4_32a* vsph = nullptr;
+    double* vnorm = nullptr;           // |p| per vertex, from the last corner pass (FP64 form)
     int4 *vcell = nullptr, *vnbr = nullptr, *vlast = nullptr, *vnext = nullptr, *vrpos = nullptr;
     int* ring = nullptr;
     int* ringCount = nullptr;

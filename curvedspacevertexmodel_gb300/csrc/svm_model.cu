@@ -101,7 +101,14 @@ __device__ double block_sum(double v) {
 // computeGeometryCPU, sphericalVertexModel.cpp:257-276).  With `t1test`, also marks every edge
 // (v, u), v < u, shorter than the T1 threshold (sphericalVertexModel.cpp:469-481).
 // One thread per vertex (large vertex counts: keeps each vertex's shared values in registers).
-__global__ void k_corners_v(const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph,
+// |p| of every vertex, once per corner pass: each is read by the vertex and its three neighbours.
+__global__ void k_vnorm(const double4_32a* __restrict__ pos, double* __restrict__ vnorm, int nV) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nV) vnorm[v] = pos_norm(ld3(pos, v));
+}
+
+__global__ void k_corners_v(const double4_32a* __restrict__ pos, const double* __restrict__ vnorm,
+                            double4_32a* __restrict__ vsph,
                           const int4* __restrict__ vcell, const int4* __restrict__ vlast,
                           const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
                           const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV,
@@ -109,7 +116,8 @@ __global__ void k_corners_v(const double4_32a* __restrict__ pos, double4_32a* __
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const D3 p = ld3(pos, v);
-    vsph[v] = sph_coords(p);
+    const double np = vnorm[v];
+    vsph[v] = sph_coords_n(p, np);
     const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v], nb = vnbr[v];
     // per neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v
     // in its three cells are its three neighbours, as are the successors)
@@ -120,7 +128,7 @@ __global__ void k_corners_v(const double4_32a* __restrict__ pos, double4_32a* __
         U[j] = ld3(pos, comp(nb, j));
         C[j] = cross3(p, U[j]);
         nC[j] = sqrt(dot3(C[j], C[j]));
-        arc[j] = geodesic(U[j], p, R);
+        arc[j] = geodesic_n(U[j], p, vnorm[comp(nb, j)], np, R);
     }
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
@@ -163,7 +171,7 @@ struct CornerShared {
 };
 
 __global__ void __launch_bounds__(3 * kCornerVerts) k_corners_s(
-    const double4_32a* __restrict__ pos, double4_32a* __restrict__ vsph, const int4* __restrict__ vcell,
+    const double4_32a* __restrict__ pos, const double* __restrict__ vnorm, double4_32a* __restrict__ vsph, const int4* __restrict__ vcell,
     const int4* __restrict__ vlast, const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
     const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV, double R, int t1test,
     double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
@@ -175,14 +183,15 @@ __global__ void __launch_bounds__(3 * kCornerVerts) k_corners_s(
     int4 nb = make_int4(0, 0, 0, 0);
     if (live) {
         p = ld3(pos, v);
-        if (j == 0) vsph[v] = sph_coords(p);
+        const double np = vnorm[v];
+        if (j == 0) vsph[v] = sph_coords_n(p, np);
         nb = vnbr[v];
         // neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v in
         // its three cells are its three neighbours, as are the successors)
         const int u = comp(nb, j);
         const D3 U = ld3(pos, u);
         const D3 C = cross3(p, U);
-        const double arc = geodesic(U, p, R);
+        const double arc = geodesic_n(U, p, vnorm[u], np, R);
         sh.cx[t] = C.x; sh.cy[t] = C.y; sh.cz[t] = C.z; sh.n[t] = sqrt(dot3(C, C));
         sh.ux[t] = U.x; sh.uy[t] = U.y; sh.uz[t] = U.z; sh.arc[t] = arc;
         // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475); `arc` is that
@@ -1399,14 +1408,15 @@ int launch_corners(svm_model* m, bool t1test) {
     }
     double lo, hi;
     t1_bracket(m->t1Threshold, m->R, &lo, &hi);
+    k_vnorm<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
     // both kernels write the same values; the slot-parallel one is faster below ~100k vertices
     if (m->nVertices < kCornerSlotsBelow)
         k_corners_s<<<(m->nVertices + kCornerVerts - 1) / kCornerVerts, 3 * kCornerVerts, 0, m->stream>>>(
-            m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+            m->pos[m->cur], m->vnorm, m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
             m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
     else
         k_corners_v<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
-            m->pos[m->cur], m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
+            m->pos[m->cur], m->vnorm, m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
             m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
     m->cornersValid = true;
     return check_launch();
@@ -1670,6 +1680,7 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->pos[0], nV * sizeof(double4_32a));
     alloc((void**)&m->pos[1], nV * sizeof(double4_32a));
     alloc((void**)&m->vsph, nV * sizeof(double4_32a));
+    alloc((void**)&m->vnorm, nV * sizeof(double));
     alloc((void**)&m->vcell, nV * sizeof(int4));
     alloc((void**)&m->vnbr, nV * sizeof(int4));
     alloc((void**)&m->vlast, nV * sizeof(int4));
@@ -1746,7 +1757,7 @@ int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (svm_fire* F : m->fires) svm::fire_detach(F);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
