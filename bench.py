@@ -141,10 +141,11 @@ def algorithmic_bytes_step(nv: int) -> int:
     return 94 * nv
 
 
-# From profiles/k_force_bd_k_corners_n1m_full.md (ncu --set full, N = 1M cells): DRAM bytes read +
-# written per vertex by one k_force_bd launch, and the FP64 pipe's busy fraction in that kernel.
-FORCE_BD_DRAM_BYTES_PER_VERTEX = 1.381e9 / 1_999_996
-FORCE_BD_FP64_PIPE_PCT = 85.3
+# From an ncu --set full capture of k_force_bd at N = 1M cells (the profiling case of this package,
+# --cells 1000000 --stab 2 --steps 1): DRAM bytes read + written per vertex by one launch, and the
+# FP64 pipe's busy fraction in that kernel.
+FORCE_BD_DRAM_BYTES_PER_VERTEX = (1.247151e9 + 0.124883e9) / 1_999_996
+FORCE_BD_FP64_PIPE_PCT = 83.4
 
 
 def peaks():
@@ -316,7 +317,7 @@ def run_ours(args):
                      "traffic": traffic, "kernel": "k_force_bd" if names[dom] == "force" else f"k_{names[dom]}",
                      "peak_source": peak_kind,
                      "fp64_pipe_busy_pct_ncu": FORCE_BD_FP64_PIPE_PCT,
-                     "note": "FP64-pipe bound (ncu: FP64 pipe 85% busy, DRAM 3%); HBM fraction is small by construction",
+                     "note": "FP64-pipe bound (ncu: FP64 pipe 83% busy, DRAM 3%); HBM fraction is small by construction",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
         "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
         "warm_l2_ms_per_step": warm_ms,

@@ -323,6 +323,43 @@ __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ r
     if (dap32) dap32[c].x = (float)(area - pref[c].x);
 }
 
+// k_fallback with the fan's triangles spread over eight threads per cell (the triangle areas are
+// FP64 acos chains; one thread per cell leaves the FP64 pipe short of warps), then summed in the
+// CPU's order by the cell's first thread: the same areas bit for bit.  Ring capacity <= 32.
+constexpr int kFanCells = 32;  // cells per block of 8 * kFanCells threads
+template <class PT>
+__global__ void __launch_bounds__(8 * kFanCells) k_fallback_fan(
+    const PT* __restrict__ pos, const int* __restrict__ ring, const int* __restrict__ ringCount,
+    const PT* __restrict__ cellPos, int Wc, int nC, double R0, const int* __restrict__ fallbackFlag,
+    const int* __restrict__ repFlag, const double* __restrict__ repR, double2* __restrict__ ap,
+    const double2* __restrict__ pref = nullptr, float2* __restrict__ dap32 = nullptr) {
+    if (!repFlag && *fallbackFlag == 0) return;
+    __shared__ double tri[kFanCells][32];
+    const int lc = threadIdx.x >> 3, k0 = threadIdx.x & 7;
+    const int c = blockIdx.x * kFanCells + lc;
+    bool live = c < nC;
+    int n = 0;
+    if (live) {
+        n = ringCount[c];
+        const int* rg = ring + (long)c * Wc;
+        const int rep = rep_of(pos[rg[0]]);
+        live = !repFlag || repFlag[rep] != 0;
+        if (live) {
+            const double R = repR ? repR[rep] : R0;
+            const D3 cp = ld3(cellPos, c);
+            // triangle k of the CPU's loop: (centroid, ring[k - 2], ring[k - 1]), indices mod n
+            for (int k = k0; k < n; k += 8)
+                tri[lc][k] = triangle_area(cp, ld3(pos, rg[(k + n - 2) % n]), ld3(pos, rg[(k + n - 1) % n]), R);
+        }
+    }
+    __syncthreads();
+    if (!live || k0 != 0) return;
+    double area = 0.0;
+    for (int k = 0; k < n; ++k) area += tri[lc][k];
+    ap[c].x = area;
+    if (dap32) dap32[c].x = (float)(area - pref[c].x);
+}
+
 // ---- forces and integration ------------------------------------------------------------------
 
 // moveParticles (sphericalVertexModel.cpp:111-148): p <- move(p, scale * disp), in place.
@@ -955,7 +992,7 @@ __device__ __forceinline__ int pick_aff(int a, int v1, int v2, const int4& vs) {
 }
 
 constexpr int kParThreads = 512;        // one segment: the whole sphere
-constexpr int kParThreadsBatch = 256;   // one segment per replica
+constexpr int kParThreadsBatch = 128;   // one segment per replica (4 resident blocks per SM at 128 registers)
 constexpr int kCoopThreads = 256;       // per block of a cooperative single-sphere pass
 
 // Block-wide exclusive scan of one int per thread; returns the block total in *total.
@@ -1175,9 +1212,12 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
             rollback = true;
             break;
         }
-        // run the positions that hold their whole footprint: one warp per position, its lanes
-        // sharing the reservation checks, the pair's rotation and the 18 re-tests (decisions and
-        // every write as for one thread per position)
+        // run the positions that hold their whole footprint.  While the round's positions fit the
+        // warps: one warp per position, its lanes sharing the reservation checks, the pair's
+        // rotation and the 18 re-tests (an FP64 warp instruction costs the same for 1 or 32 lanes,
+        // so a flip's FP64 chain shortens ~2.6x); beyond that (segments with many flips in a
+        // round): one thread per position.  The same decisions and writes either way.
+        if (nCur <= ws) {
         for (int i = wi; i < nCur; i += ws) {
             const int p = cur[i];
             const int* f = fpB + (long)i * kFootprint;
@@ -1257,6 +1297,63 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
                     }
                 }
             }
+        }
+        } else {
+        for (int i = gi; i < nCur; i += gs) {
+            const int p = cur[i];
+            const int* f = fpB + (long)i * kFootprint;
+            bool ready = true;
+            for (int k = 0; k < 8; ++k) ready &= t1.resV[f[k]] == p;
+            for (int k = 8; k < kFootprint; ++k) ready &= t1.resC[f[k]] == p;
+            if (!ready) {
+                const int ni = atomicAdd(&ctl->next[par], 1);
+                if (ni < capB) nxt[ni] = p;
+                else atomicExch(&ctl->rollback, 1);
+                continue;
+            }
+            const int ci = atomicAdd(&ctl->exec, 1);
+            if (ci >= capB) { atomicExch(&ctl->rollback, 1); continue; }
+            for (int k = 0; k < kFootprint; ++k) comB[(long)ci * kFootprint + k] = f[k];
+            for (int k = 0; k < 8; ++k) atomicMax(t1.comV + f[k], p);
+            for (int k = 8; k < kFootprint; ++k) atomicMax(t1.comC + f[k], p);
+            atomicAnd(t1.bits + (p >> 5), ~(1u << (p & 31)));
+            if (!t1_candidate(A, p)) continue;
+            const int ui = atomicAdd(&ctl->undo, 1);
+            if (ui >= undoPer) { atomicExch(&ctl->rollback, 1); continue; }
+            const int v1 = f[0], v2 = f[1];
+            int4 cs, vs;
+            UndoEntry* u = undoB + ui;
+            if (!t1_flip(A, v1, v2, cs, vs, u, undoRingsB + (long)ui * 4 * A.Wc)) {
+                u->v1 = -1;  // nothing was written
+                continue;
+            }
+            atomicAdd(&ctl->flips, 1);
+            const int fc = atomicAdd(t1.flipCount, 1);
+            u->logIdx = fc;
+            if (fc < t1.flipLogCap) {
+                int* e = t1.flipLog + 4 * fc;
+                e[0] = *t1.pass; e[1] = p; e[2] = v1; e[3] = v2;
+            }
+            const int tc = atomicAdd(t1.ctr + 5, 4);
+            if (tc + 4 <= t1.touchedCap) {
+                t1.touched[tc] = cs.x; t1.touched[tc + 1] = cs.y; t1.touched[tc + 2] = cs.z; t1.touched[tc + 3] = cs.w;
+            } else {
+                atomicExch(&ctl->rollback, 1);
+            }
+            const int aff[6] = {v1, v2, vs.x, vs.y, vs.z, vs.w};
+            for (int a = 0; a < 6; ++a)
+                for (int sl = 0; sl < 3; ++sl) {
+                    const int r = 3 * aff[a] + sl;
+                    if (!(r > p && r < qHi && t1_candidate(A, r))) continue;
+                    const unsigned bit = 1u << (r & 31);
+                    if (!(atomicOr(t1.bits + (r >> 5), bit) & bit)) {
+                        atomicOr(t1.summary + (r >> 10), 1u << ((r >> 5) & 31));
+                        const int ni = atomicAdd(&ctl->next[par], 1);
+                        if (ni < capB) nxt[ni] = r;
+                        else atomicExch(&ctl->rollback, 1);
+                    }
+                }
+        }
         }
         if (!group_sync()) return;
         lap(2);
@@ -1401,7 +1498,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
 }
 
 int launch_corners(svm_model* m, bool t1test) {
-    PhaseTimer pt(m, SVM_PHASE_CORNERS);
+    PhaseTimer pt(m, SVM_PHASE_CORNERS, m->precision == SVM_PRECISION_MIXED ? 1 : 2);  // FP64: k_vnorm too
     if (m->precision == SVM_PRECISION_MIXED) {
         m->cornersValid = true;
         return m->nRep > 1 ? batch_tuned_corners(m, t1test) : mixed_launch_corners(m, t1test);
@@ -1456,7 +1553,17 @@ static int launch_cells(svm_model* m) {
     }
     PhaseTimer pt(m, SVM_PHASE_FALLBACK);
     const int nb = blocksFor(m->nCells);
-    if (mixed)
+    if (m->Wc <= 32) {
+        const int nf = (m->nCells + kFanCells - 1) / kFanCells;
+        if (mixed)
+            k_fallback_fan<float4><<<nf, 8 * kFanCells, 0, m->stream>>>(
+                m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc, m->nCells, m->R, m->fallbackFlag,
+                batch ? m->repFlag : nullptr, m->repR, m->ap, m->pref, m->dap32);
+        else
+            k_fallback_fan<double4_32a><<<nf, 8 * kFanCells, 0, m->stream>>>(
+                m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc, m->nCells, m->R, m->fallbackFlag, nullptr,
+                nullptr, m->ap);
+    } else if (mixed)
         k_fallback<float4><<<nb, kBlock, 0, m->stream>>>(m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc,
                                                          m->nCells, m->R, m->fallbackFlag, batch ? m->repFlag : nullptr,
                                                          m->repR, m->ap, m->pref, m->dap32);

@@ -7,7 +7,9 @@ as the reference driver does), `equil` graph-replayed steps at the run parameter
 `steps` Brownian steps at T = 0.01, P0 = 3.8, dt = 0.01
 (T1 threshold 0.04), one launch per kernel per step (no graph), and prints the energy per cell.
 With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*); with --replicas R
-a batch of R replicas runs instead (stabilisation, then `steps` steps at per-replica P0 and T).
+a batch of R replicas runs instead (stabilisation, then `steps` steps at per-replica P0 and T);
+with --fire K the `steps` Brownian steps are followed by K FIRE iterations (energyMinimizerFIRE,
+the reference's default parameters, force tolerance 1e-12 so that all K run).
 """
 from __future__ import annotations
 
@@ -29,6 +31,7 @@ def main():
     ap.add_argument("--replicas", type=int, default=0,
                     help="instead: a batch of this many replicas, N log-uniform in [100, 5000] (seeded), "
                          "P0 U[3.6, 3.95], T logU[1e-4, 1e-1]")
+    ap.add_argument("--fire", type=int, default=0, help="FIRE iterations after the Brownian steps")
     args = ap.parse_args()
     t0 = time.time()
     if args.replicas:
@@ -70,6 +73,11 @@ def main():
         m.precision = "mixed"
     for _ in range(args.steps):
         bd.integrateEquationOfMotion()
+    if args.fire:
+        fire = svm.energyMinimizerFIRE(m)
+        fire.setMaximumIterations(args.fire)
+        fire.setForceCutoff(1e-12)
+        fire.minimize()
     m.computeGeometry()
     print(f"cells {args.cells} vertices {m.nVertices} energy/cell {m.computeEnergy() / args.cells:.6g} "
           f"status {m.deviceStatus()} wall {time.time() - t0:.1f} s")

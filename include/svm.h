@@ -47,7 +47,7 @@ extern "C" {
                                        (the state of that pass is undefined) */
 
 /* Noise sources of the Brownian step. */
-#define SVM_NOISE_PHILOX 0     /* in-kernel counter-based Philox4x32-10 + Box-Muller */
+#define SVM_NOISE_PHILOX 0     /* in-kernel counter-based Philox4x32-10 bits, ziggurat normals */
 #define SVM_NOISE_BUFFER 1     /* standard normals supplied by the caller, vertex-major [3*Nv] */
 
 /* FIRE stopping criteria. */
