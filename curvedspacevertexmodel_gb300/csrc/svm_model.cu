@@ -107,101 +107,116 @@ __global__ void k_vnorm(const double4_32a* __restrict__ pos, double* __restrict_
     if (v < nV) vnorm[v] = pos_norm(ld3(pos, v));
 }
 
-__global__ void k_corners_v(const double4_32a* __restrict__ pos, const double* __restrict__ vnorm,
-                            double4_32a* __restrict__ vsph,
-                          const int4* __restrict__ vcell, const int4* __restrict__ vlast,
-                          const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
-                          const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV,
-                          double R, int t1test, double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nV) return;
-    const D3 p = ld3(pos, v);
-    const double np = vnorm[v];
-    vsph[v] = sph_coords_n(p, np);
-    const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v], nb = vnbr[v];
-    // per neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v
-    // in its three cells are its three neighbours, as are the successors)
-    D3 U[3], C[3];
-    double nC[3], arc[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        U[j] = ld3(pos, comp(nb, j));
-        C[j] = cross3(p, U[j]);
-        nC[j] = sqrt(dot3(C[j], C[j]));
-        arc[j] = geodesic_n(U[j], p, vnorm[comp(nb, j)], np, R);
+// Position of the n-th (from 0) set bit of m, n < popc(m).
+__device__ __forceinline__ int nth_set(unsigned m, int n) {
+    int pos = 0, c = __popc(m & 0xFFFFu);
+    if (n >= c) { n -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xFFu);
+    if (n >= c) { n -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xFu);
+    if (n >= c) { n -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (n >= c) { n -= c; m >>= 2; pos += 2; }
+    return pos + ((n >= (int)(m & 1u)) ? 1 : 0);
+}
+
+// Edge terms of the corner pass, once per edge: for every edge (v, u) with v < u, stored at slot
+// e = 3 v + j (u = vnbr[v][j]): p_v x p_u with its norm, and the arc geodesic(p_u, p_v) (both
+// endpoints' corners read them; from u's side the cross product is the exact negative and the arc
+// and norm are the same bit for bit, since the products commute); with `t1test`, the T1 test of
+// the edge (sphericalVertexModel.cpp:469-481).  Also each vertex's spherical coordinates.  A
+// warp's owned edges (about half of its 96 slots) are compacted over its lanes first, so that the
+// FP64 work runs on full warps.
+__global__ void k_edges(const double4_32a* __restrict__ pos, const double* __restrict__ vnorm,
+                        double4_32a* __restrict__ vsph, const int4* __restrict__ vnbr,
+                        double4_32a* __restrict__ edgeC, double* __restrict__ edgeArc, int nV, double R, int t1test,
+                        double t1Threshold, T1Scratch t1) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const bool live = v < nV;
+    int4 nb = make_int4(-1, -1, -1, -1);
+    if (live) {
+        nb = vnbr[v];
+        vsph[v] = sph_coords_n(ld3(pos, v), vnorm[v]);
     }
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-        const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
-        double2 cr;
-        if (jl >= 0 && jx >= 0) {
-            cr = make_double2(pick3(arc, jl), included_angle_pre(pick3(C, jx), pick3(C, jl), pick3(nC, jx),
-                                                                 pick3(nC, jl), pick3(U, jl)));
-        } else {  // inconsistent lists: evaluate directly
-            const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
-            cr = make_double2(geodesic(pl, p, R), included_angle(pl, p, px));
-        }
-        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
-    }
-    if (t1test) {
-        // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475); arc[j] is
-        // that geodesic, bitwise (its cosine's products commute exactly)
-#pragma unroll
-        for (int s = 0; s < 3; ++s) {
-            const int u = comp(nb, s);
-            if (v < u && arc[s] < t1Threshold) {
-                const int q = 3 * v + s;
-                atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
-                atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
-                atomicAdd(t1.count, 1);
-            }
+    const unsigned b0 = __ballot_sync(0xffffffffu, live && v < nb.x);
+    const unsigned b1 = __ballot_sync(0xffffffffu, live && v < nb.y);
+    const unsigned b2 = __ballot_sync(0xffffffffu, live && v < nb.z);
+    const int n0 = __popc(b0), n1 = __popc(b1), total = n0 + n1 + __popc(b2);
+    const int base = v - lane;
+    for (int k = lane; k < total; k += 32) {
+        int j, src;
+        if (k < n0) { j = 0; src = nth_set(b0, k); }
+        else if (k < n0 + n1) { j = 1; src = nth_set(b1, k - n0); }
+        else { j = 2; src = nth_set(b2, k - n0 - n1); }
+        const int w = base + src, u = comp(vnbr[w], j);
+        const D3 p = ld3(pos, w), U = ld3(pos, u);
+        const D3 C = cross3(p, U);
+        const double arc = geodesic_n(U, p, vnorm[u], vnorm[w], R);
+        const int e = 3 * w + j;
+        edgeC[e] = make_double4_32a(C.x, C.y, C.z, sqrt(dot3(C, C)));
+        edgeArc[e] = arc;
+        // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475)
+        if (t1test && arc < t1Threshold) {
+            atomicOr(&t1.bits[e >> 5], 1u << (e & 31));
+            atomicOr(&t1.summary[e >> 10], 1u << ((e >> 5) & 31));
+            atomicAdd(t1.count, 1);
         }
     }
 }
 
-// Blocks of 3 kCornerVerts threads, three per vertex (small vertex counts, where one thread per
-// vertex leaves the FP64 pipe short of warps): thread (v, j) first evaluates the vertex's
-// neighbour j (its position, p x u_j with its norm, the arc, and the T1 test of that edge), then,
-// after a block barrier, the corner of cell slot j from the neighbours' values in shared memory.
+// The edge terms of slot j of vertex v (neighbour u) from its owner: C = p_v x p_u, its norm and
+// the arc.  False if u does not list v (inconsistent lists).
+__device__ __forceinline__ bool edge_terms(int v, int j, int u, const int4* __restrict__ vnbr,
+                                           const double4_32a* __restrict__ edgeC,
+                                           const double* __restrict__ edgeArc, D3& C, double& nC, double& arc) {
+    int e;
+    bool neg = false;
+    if (v < u) {
+        e = 3 * v + j;
+    } else {
+        const int ju = nbr_slot(vnbr[u], v);
+        if (ju < 0) return false;
+        e = 3 * u + ju;
+        neg = true;
+    }
+    const double4_32a q = edgeC[e];
+    C = neg ? D3{-q.x, -q.y, -q.z} : D3{q.x, q.y, q.z};
+    nC = q.w;
+    arc = edgeArc[e];
+    return true;
+}
+
+// k_corner with three threads per vertex (below ~100k vertices, where one thread per vertex
+// leaves the FP64 pipe short of warps): thread (v, j) fetches the edge terms of neighbour j into
+// shared memory, then, after a block barrier, computes the corner of cell slot j.
 constexpr int kCornerVerts = 64;
 constexpr int kCornerSlotsBelow = 100000;  // vertices
 struct CornerShared {
     double cx[3 * kCornerVerts], cy[3 * kCornerVerts], cz[3 * kCornerVerts], n[3 * kCornerVerts];
     double ux[3 * kCornerVerts], uy[3 * kCornerVerts], uz[3 * kCornerVerts], arc[3 * kCornerVerts];
+    int ok[kCornerVerts];
 };
-
-__global__ void __launch_bounds__(3 * kCornerVerts) k_corners_s(
-    const double4_32a* __restrict__ pos, const double* __restrict__ vnorm, double4_32a* __restrict__ vsph, const int4* __restrict__ vcell,
-    const int4* __restrict__ vlast, const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
-    const int4* __restrict__ vnbr, double2* __restrict__ corner, int Wc, int nV, double R, int t1test,
-    double t1Threshold, double cosLo, double cosHi, T1Scratch t1) {
+__global__ void __launch_bounds__(3 * kCornerVerts) k_corner_s(
+    const double4_32a* __restrict__ pos, const int4* __restrict__ vcell, const int4* __restrict__ vlast,
+    const int4* __restrict__ vnext, const int4* __restrict__ vrpos, const int4* __restrict__ vnbr,
+    const double4_32a* __restrict__ edgeC, const double* __restrict__ edgeArc, double2* __restrict__ corner, int Wc,
+    int nV, double R) {
     __shared__ CornerShared sh;
     const int t = threadIdx.x, vi = t / 3, j = t - 3 * (t / 3), b = 3 * vi;
     const int v = blockIdx.x * kCornerVerts + vi;
     const bool live = v < nV;
-    D3 p{0.0, 0.0, 0.0};
+    if (j == 0) sh.ok[vi] = 1;
+    __syncthreads();
     int4 nb = make_int4(0, 0, 0, 0);
     if (live) {
-        p = ld3(pos, v);
-        const double np = vnorm[v];
-        if (j == 0) vsph[v] = sph_coords_n(p, np);
         nb = vnbr[v];
-        // neighbour u_j: position, p x u_j and its norm, and the arc (the ring predecessors of v in
-        // its three cells are its three neighbours, as are the successors)
         const int u = comp(nb, j);
         const D3 U = ld3(pos, u);
-        const D3 C = cross3(p, U);
-        const double arc = geodesic_n(U, p, vnorm[u], np, R);
-        sh.cx[t] = C.x; sh.cy[t] = C.y; sh.cz[t] = C.z; sh.n[t] = sqrt(dot3(C, C));
+        D3 C{0.0, 0.0, 0.0};
+        double nC = 0.0, arc = 0.0;
+        if (!edge_terms(v, j, u, vnbr, edgeC, edgeArc, C, nC, arc)) sh.ok[vi] = 0;
+        sh.cx[t] = C.x; sh.cy[t] = C.y; sh.cz[t] = C.z; sh.n[t] = nC;
         sh.ux[t] = U.x; sh.uy[t] = U.y; sh.uz[t] = U.z; sh.arc[t] = arc;
-        // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475); `arc` is that
-        // geodesic, bitwise (its cosine's products commute exactly)
-        if (t1test && v < u && arc < t1Threshold) {
-            const int q = 3 * v + j;
-            atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
-            atomicOr(&t1.summary[q >> 10], 1u << ((q >> 5) & 31));
-            atomicAdd(t1.count, 1);
-        }
     }
     __syncthreads();
     if (!live) return;
@@ -209,15 +224,49 @@ __global__ void __launch_bounds__(3 * kCornerVerts) k_corners_s(
     const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
     const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
     double2 cr;
-    if (jl >= 0 && jx >= 0) {
+    if (sh.ok[vi] && jl >= 0 && jx >= 0) {
         const int l = b + jl, x = b + jx;
         cr = make_double2(sh.arc[l], included_angle_pre(D3{sh.cx[x], sh.cy[x], sh.cz[x]}, D3{sh.cx[l], sh.cy[l], sh.cz[l]},
                                                         sh.n[x], sh.n[l], D3{sh.ux[l], sh.uy[l], sh.uz[l]}));
     } else {  // inconsistent lists: evaluate directly
-        const D3 pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
+        const D3 p = ld3(pos, v), pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
         cr = make_double2(geodesic(pl, p, R), included_angle(pl, p, px));
     }
     corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
+}
+
+// Per vertex: for each of its three cells, the arc from the ring predecessor and the included
+// angle at the vertex (the per-corner terms of computeGeometryCPU, sphericalVertexModel.cpp:257-276)
+// from the edge terms of k_edges.
+__global__ void k_corner(const double4_32a* __restrict__ pos, const int4* __restrict__ vcell,
+                         const int4* __restrict__ vlast, const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
+                         const int4* __restrict__ vnbr, const double4_32a* __restrict__ edgeC,
+                         const double* __restrict__ edgeArc, double2* __restrict__ corner, int Wc, int nV, double R) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const int4 nb = vnbr[v], cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v];
+    D3 C[3], U[3];
+    double nC[3], arc[3];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int u = comp(nb, j);
+        U[j] = ld3(pos, u);
+        ok &= edge_terms(v, j, u, vnbr, edgeC, edgeArc, C[j], nC[j], arc[j]);
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
+        double2 cr;
+        if (ok && jl >= 0 && jx >= 0) {
+            cr = make_double2(pick3(arc, jl), included_angle_pre(pick3(C, jx), pick3(C, jl), pick3(nC, jx),
+                                                                 pick3(nC, jl), pick3(U, jl)));
+        } else {  // inconsistent lists: evaluate directly
+            const D3 p = ld3(pos, v), pl = ld3(pos, comp(lasts, s)), px = ld3(pos, comp(nexts, s));
+            cr = make_double2(geodesic(pl, p, R), included_angle(pl, p, px));
+        }
+        corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
+    }
 }
 
 // Per cell: centroid (sum of ring vertices in ring order, renormalised), perimeter and angle sum
@@ -1498,23 +1547,25 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
 }
 
 int launch_corners(svm_model* m, bool t1test) {
-    PhaseTimer pt(m, SVM_PHASE_CORNERS, m->precision == SVM_PRECISION_MIXED ? 1 : 2);  // FP64: k_vnorm too
+    PhaseTimer pt(m, SVM_PHASE_CORNERS, m->precision == SVM_PRECISION_MIXED ? 1 : 3);  // FP64: k_vnorm, k_edges, k_corner
     if (m->precision == SVM_PRECISION_MIXED) {
         m->cornersValid = true;
         return m->nRep > 1 ? batch_tuned_corners(m, t1test) : mixed_launch_corners(m, t1test);
     }
-    double lo, hi;
-    t1_bracket(m->t1Threshold, m->R, &lo, &hi);
+    if (!m->edgeC) return SVM_ERR_ARG;  // FP64 corners exist for single spheres only
     k_vnorm<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
-    // both kernels write the same values; the slot-parallel one is faster below ~100k vertices
+    k_edges<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->vsph, m->vnbr, m->edgeC,
+                                                              m->edgeArc, m->nVertices, m->R, t1test ? 1 : 0,
+                                                              m->t1Threshold, m->t1);
+    // both corner kernels write the same values; the three-thread one is faster below ~100k vertices
     if (m->nVertices < kCornerSlotsBelow)
-        k_corners_s<<<(m->nVertices + kCornerVerts - 1) / kCornerVerts, 3 * kCornerVerts, 0, m->stream>>>(
-            m->pos[m->cur], m->vnorm, m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
-            m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
+        k_corner_s<<<(m->nVertices + kCornerVerts - 1) / kCornerVerts, 3 * kCornerVerts, 0, m->stream>>>(
+            m->pos[m->cur], m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->edgeC, m->edgeArc, m->corner, m->Wc,
+            m->nVertices, m->R);
     else
-        k_corners_v<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(
-            m->pos[m->cur], m->vnorm, m->vsph, m->vcell, m->vlast, m->vnext, m->vrpos, m->vnbr, m->corner, m->Wc, m->nVertices,
-            m->R, t1test ? 1 : 0, m->t1Threshold, lo, hi, m->t1);
+        k_corner<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vcell, m->vlast, m->vnext,
+                                                                   m->vrpos, m->vnbr, m->edgeC, m->edgeArc, m->corner,
+                                                                   m->Wc, m->nVertices, m->R);
     m->cornersValid = true;
     return check_launch();
 }
@@ -1788,6 +1839,10 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->pos[1], nV * sizeof(double4_32a));
     alloc((void**)&m->vsph, nV * sizeof(double4_32a));
     alloc((void**)&m->vnorm, nV * sizeof(double));
+    if (nRep == 1) {  // the FP64 corner pass's edge terms (batches run in the mixed form only)
+        alloc((void**)&m->edgeC, 3 * (size_t)nV * sizeof(double4_32a));
+        alloc((void**)&m->edgeArc, 3 * (size_t)nV * sizeof(double));
+    }
     alloc((void**)&m->vcell, nV * sizeof(int4));
     alloc((void**)&m->vnbr, nV * sizeof(int4));
     alloc((void**)&m->vlast, nV * sizeof(int4));
@@ -1864,7 +1919,7 @@ int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (svm_fire* F : m->fires) svm::fire_detach(F);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
