@@ -32,7 +32,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FMA_SOURCES: set = set()
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
 
 def _nvcc() -> str:
