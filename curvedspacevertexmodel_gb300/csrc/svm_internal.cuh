@@ -379,6 +379,16 @@ struct svm_model {
     // bumped by every setter whose value a captured graph bakes in (Kr, threshold, restriction)
     unsigned paramsVersion = 0;
     unsigned bdGraphVersion = ~0u;
+    // graph cache for svm_brownian_step_io with pinned host buffers, one per position-buffer role
+    struct IoGraph {
+        cudaGraphExec_t exec = nullptr;
+        double T = 0, dt = 0, mu = 0;
+        uint64_t seed = 0;
+        const void *in = nullptr, *out = nullptr;
+        unsigned version = ~0u;
+        int precision = -1;
+    } ioGraph[2];
+    double* ioEnergy = nullptr;        // page-locked landing slot of the graph's energy copy
 };
 
 namespace svm {

@@ -1930,6 +1930,9 @@ int svm_model_destroy(svm_model* m) {
                     m->repFlag, m->repScal};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
+    for (auto& g : m->ioGraph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (m->ioEnergy) cudaFreeHost(m->ioEnergy);
     svm::batch_release(m);
     for (auto& v : m->profEvents) for (cudaEvent_t e : v) cudaEventDestroy(e);
     if (m->ownStream && m->stream) cudaStreamDestroy(m->stream);
@@ -2291,9 +2294,64 @@ int svm_brownian_step(svm_model* m, double T, double dt, double mu, int mode, co
 // synchronisation: positions H2D (optional), the step (Philox noise), the energy of the geometry
 // the step's forces used (what computeEnergy returns after a timestep, sphericalVertexModel.cpp:
 // 150-160) and the new positions D2H (optional).
+namespace svm {
+static bool pinned(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeHost;
+}
+}  // namespace svm
+
+static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
+                            double* posOut, double* energyOut);
+
 int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
                          double* posOut, double* energyOut) {
     if (!m) return SVM_ERR_ARG;
+    // With both position buffers page-locked (and no per-phase profiling) the whole sequence,
+    // copies included, is one graph launch: captured once per position-buffer role and reused
+    // while the parameters, buffers and form stay the same.  The energy lands in a page-locked slot
+    // of the model and is copied out after the synchronisation.
+    if (posIn && posOut && m->nRep == 1 && !m->prof && svm::pinned(posIn) && svm::pinned(posOut)) {
+        if (!m->ioEnergy && cudaMallocHost((void**)&m->ioEnergy, sizeof(double)) != cudaSuccess) {
+            m->ioEnergy = nullptr;
+            return SVM_ERR_CUDA;
+        }
+        auto& g = m->ioGraph[m->cur];
+        const bool reuse = g.exec && g.T == T && g.dt == dt && g.mu == mu && g.seed == seed && g.in == posIn &&
+                           g.out == posOut && g.version == m->paramsVersion && g.precision == m->precision;
+        const int cur0 = m->cur;
+        if (!reuse) {
+            if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+            cudaGraph_t graph;
+            SVM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, m->ioEnergy);
+            cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+            m->cur = cur0;
+            if (rc || ce != cudaSuccess) { cudaGetLastError(); return rc ? rc : SVM_ERR_CUDA; }
+            ce = cudaGraphInstantiate(&g.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) { g.exec = nullptr; return SVM_ERR_CUDA; }
+            g.T = T; g.dt = dt; g.mu = mu; g.seed = seed; g.in = posIn; g.out = posOut;
+            g.version = m->paramsVersion; g.precision = m->precision;
+        }
+        SVM_CUDA(cudaGraphLaunch(g.exec, m->stream));
+        // the host-side state the sequence leaves: buffers swapped, corners left to the next step
+        m->cur = 1 - cur0;
+        m->cornersValid = false;
+        SVM_CUDA(cudaStreamSynchronize(m->stream));
+        if (energyOut) *energyOut = *m->ioEnergy;
+        return SVM_OK;
+    }
+    const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, energyOut);
+    if (rc) return rc;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+// The launches of one host-io step, in stream order (no synchronisation).
+static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
+                            double* posOut, double* energyOut) {
     const bool mixedForm = m->precision == SVM_PRECISION_MIXED;
     if (posIn) {
         SVM_CUDA(cudaMemcpyAsync(m->dispBuf, posIn, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));
@@ -2325,7 +2383,6 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
         }
         SVM_CUDA(cudaMemcpyAsync(posOut, m->dispBuf, sizeof(double) * 3 * m->nVertices, cudaMemcpyDeviceToHost, m->stream));
     }
-    SVM_CUDA(cudaStreamSynchronize(m->stream));
     return SVM_OK;
 }
 

@@ -407,23 +407,34 @@ def test_host_io_step_equals_the_call_sequence(svm, gold):
     assert e_io.value == e_seq
 
 
-def test_host_io_steps_chained_with_flips(svm):
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_io_steps_chained_with_flips(svm, pinned):
     """Chained svm_brownian_step_io calls (each step's positions fed back in) follow the
     device-resident step loop bit for bit over steps with T1 flips: positions, topology, flip
-    count and energies.  (The host-io step defers the moved state's corners to the next step.)"""
+    count and energies.  (The host-io step defers the moved state's corners to the next step;
+    with page-locked buffers it runs as a replayed graph, re-captured when the seed changes.)"""
     import ctypes as C
+    import torch
     from curvedspacevertexmodel_gb300 import _lib
     a, _ = stabilised(svm, 3000, seed=11, stab=40, steps=60)
     b, _ = stabilised(svm, 3000, seed=11, stab=40, steps=60)
     for m in (a, b):
         m.setT1Threshold(0.08)   # flips every step
     a.t1Stats(), b.t1Stats()   # counters restart
-    pos = np.ascontiguousarray(a.returnPositions()).reshape(-1)
-    out = np.empty_like(pos)
+    n = 3 * a.nVertices
+    if pinned:
+        pos = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+        out = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    else:
+        pos, out = np.empty(n), np.empty(n)
+    pos[:] = a.returnPositions().reshape(-1)
     e_io = C.c_double()
     for k in range(25):
-        _lib.call("svm_brownian_step_io", a.handle, 0.05, 0.01, 1.0, 4242 + k, pos, out, C.byref(e_io))
-        _lib.call("svm_brownian_step", b.handle, 0.05, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, 4242 + k)
+        seed = 4242 + k // 10   # a new seed (a new capture) every ten steps
+        _lib.call("svm_brownian_step_io", a.handle, 0.05, 0.01, 1.0, seed, pos, out, C.byref(e_io))
+        _lib.call("svm_brownian_step", b.handle, 0.05, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, seed)
+        # both report the energy of the state the step started from (the areas of its geometry)
+        assert e_io.value == b.computeEnergy(), k
         pos, out = out, pos
     assert np.array_equal(pos.reshape(-1, 3), b.returnPositions())
     assert np.array_equal(a.vertexNeighbors(), b.vertexNeighbors())
