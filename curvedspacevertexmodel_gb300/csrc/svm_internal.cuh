@@ -180,9 +180,14 @@ __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
     return a;
 }
 // sphericalTriangleArea (sphericalDomain.h:135-166)
+// q / |q| as sphericalTriangleArea normalises each corner
+__device__ __forceinline__ D3 unit_corner(D3 q) { return scl3(1.0 / sqrt(dot3(q, q)), q); }
+__device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R);
 __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
-    D3 p1 = scl3(1.0 / sqrt(dot3(q1, q1)), q1), p2 = scl3(1.0 / sqrt(dot3(q2, q2)), q2),
-       p3 = scl3(1.0 / sqrt(dot3(q3, q3)), q3);
+    return triangle_area_unit(unit_corner(q1), unit_corner(q2), unit_corner(q3), R);
+}
+// the same from the normalised corners
+__device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R) {
     double d12 = dot3(p1, p2), d13 = dot3(p1, p3), d23 = dot3(p2, p3);
     double area = -kPI;
     area += acos((d23 - d12 * d13) / (sqrt(1 - d12 * d12) * sqrt(1 - d13 * d13)));

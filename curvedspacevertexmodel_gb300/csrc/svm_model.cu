@@ -372,39 +372,70 @@ __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ r
     if (dap32) dap32[c].x = (float)(area - pref[c].x);
 }
 
-// k_fallback with the fan's triangles spread over eight threads per cell (the triangle areas are
-// FP64 acos chains; one thread per cell leaves the FP64 pipe short of warps), then summed in the
-// CPU's order by the cell's first thread: the same areas bit for bit.  Ring capacity <= 32.
-constexpr int kFanCells = 32;  // cells per block of 8 * kFanCells threads
+// k_fallback with a block's fan triangles packed densely over its threads (the triangle areas are
+// FP64 acos chains, and the FP64 pipe charges a warp instruction whatever its active lanes) and
+// every corner normalised once (a ring vertex serves two triangles, the centroid all of them),
+// then each cell's triangles summed in the CPU's order by one thread: the same areas bit for bit.
+// kFanCells cells per block; ring capacity <= 32.
+constexpr int kFanCells = 32;
+constexpr int kFanThreads = 256;
 template <class PT>
-__global__ void __launch_bounds__(8 * kFanCells) k_fallback_fan(
+__global__ void __launch_bounds__(kFanThreads) k_fallback_fan(
     const PT* __restrict__ pos, const int* __restrict__ ring, const int* __restrict__ ringCount,
     const PT* __restrict__ cellPos, int Wc, int nC, double R0, const int* __restrict__ fallbackFlag,
     const int* __restrict__ repFlag, const double* __restrict__ repR, double2* __restrict__ ap,
     const double2* __restrict__ pref = nullptr, float2* __restrict__ dap32 = nullptr) {
     if (!repFlag && *fallbackFlag == 0) return;
-    __shared__ double tri[kFanCells][32];
-    const int lc = threadIdx.x >> 3, k0 = threadIdx.x & 7;
-    const int c = blockIdx.x * kFanCells + lc;
-    bool live = c < nC;
-    int n = 0;
-    if (live) {
-        n = ringCount[c];
-        const int* rg = ring + (long)c * Wc;
-        const int rep = rep_of(pos[rg[0]]);
-        live = !repFlag || repFlag[rep] != 0;
-        if (live) {
-            const double R = repR ? repR[rep] : R0;
-            const D3 cp = ld3(cellPos, c);
-            // triangle k of the CPU's loop: (centroid, ring[k - 2], ring[k - 1]), indices mod n
-            for (int k = k0; k < n; k += 8)
-                tri[lc][k] = triangle_area(cp, ld3(pos, rg[(k + n - 2) % n]), ld3(pos, rg[(k + n - 1) % n]), R);
+    __shared__ int cnt[kFanCells], off[kFanCells + 1], owner[kFanCells * 32];
+    __shared__ double radius[kFanCells];
+    __shared__ double ux[kFanCells * 32], uy[kFanCells * 32], uz[kFanCells * 32];
+    __shared__ double cx[kFanCells], cy[kFanCells], cz[kFanCells];
+    __shared__ double tri[kFanCells * 32];
+    const int t = threadIdx.x, c0 = blockIdx.x * kFanCells;
+    if (t < kFanCells) {
+        const int c = c0 + t;
+        int n = 0;
+        if (c < nC) {
+            n = ringCount[c];
+            const int rep = rep_of(pos[ring[(long)c * Wc]]);
+            if (repFlag && repFlag[rep] == 0) n = 0;  // this replica keeps its areas
+            radius[t] = repR ? repR[rep] : R0;
+            if (n > 0) {
+                const D3 u = unit_corner(ld3(cellPos, c));
+                cx[t] = u.x; cy[t] = u.y; cz[t] = u.z;
+            }
         }
+        cnt[t] = n;
+        // exclusive scan of the counts over the first warp
+        int incl = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (t >= o) incl += y;
+        }
+        off[t] = incl - n;
+        if (t == kFanCells - 1) off[kFanCells] = incl;
+        for (int k = 0; k < n; ++k) owner[incl - n + k] = t;
     }
     __syncthreads();
-    if (!live || k0 != 0) return;
+    const int total = off[kFanCells];
+    for (int e = t; e < total; e += kFanThreads) {  // each ring corner, normalised once
+        const int lc = owner[e];
+        const D3 u = unit_corner(ld3(pos, ring[(long)(c0 + lc) * Wc + (e - off[lc])]));
+        ux[e] = u.x; uy[e] = u.y; uz[e] = u.z;
+    }
+    __syncthreads();
+    for (int e = t; e < total; e += kFanThreads) {
+        // triangle k of cell lc in the CPU's loop: (centroid, ring[k - 2], ring[k - 1]), indices mod n
+        const int lc = owner[e], b = off[lc], n = cnt[lc], k = e - b;
+        const int i2 = b + (k + n - 2) % n, i3 = b + (k + n - 1) % n;
+        tri[e] = triangle_area_unit(D3{cx[lc], cy[lc], cz[lc]}, D3{ux[i2], uy[i2], uz[i2]}, D3{ux[i3], uy[i3], uz[i3]},
+                                    radius[lc]);
+    }
+    __syncthreads();
+    if (t >= kFanCells || cnt[t] == 0) return;
+    const int c = c0 + t;
     double area = 0.0;
-    for (int k = 0; k < n; ++k) area += tri[lc][k];
+    for (int k = 0; k < cnt[t]; ++k) area += tri[off[t] + k];
     ap[c].x = area;
     if (dap32) dap32[c].x = (float)(area - pref[c].x);
 }
@@ -1607,11 +1638,11 @@ static int launch_cells(svm_model* m) {
     if (m->Wc <= 32) {
         const int nf = (m->nCells + kFanCells - 1) / kFanCells;
         if (mixed)
-            k_fallback_fan<float4><<<nf, 8 * kFanCells, 0, m->stream>>>(
+            k_fallback_fan<float4><<<nf, kFanThreads, 0, m->stream>>>(
                 m->pos32[m->cur], m->ring, m->ringCount, m->cellPos32, m->Wc, m->nCells, m->R, m->fallbackFlag,
                 batch ? m->repFlag : nullptr, m->repR, m->ap, m->pref, m->dap32);
         else
-            k_fallback_fan<double4_32a><<<nf, 8 * kFanCells, 0, m->stream>>>(
+            k_fallback_fan<double4_32a><<<nf, kFanThreads, 0, m->stream>>>(
                 m->pos[m->cur], m->ring, m->ringCount, m->cellPos, m->Wc, m->nCells, m->R, m->fallbackFlag, nullptr,
                 nullptr, m->ap);
     } else if (mixed)
