@@ -219,6 +219,7 @@ def run_ours(args):
         bd.integrateEquationOfMotion()
     torch.cuda.synchronize()
     model.t1Stats()
+    model.fallbackCount()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")  # > L2 (129 MB)
 
     # ---- timed region: K steps, each after an L2 flush, events on the model's stream ----
@@ -245,6 +246,7 @@ def run_ours(args):
     launches = np.zeros(_lib_phase_count(), dtype=np.int32)
     _lib.call("svm_model_profile_read", model.handle, ms, launches)
     t1stats = model.t1Stats()
+    fallbacks_timed = model.fallbackCount()
     _lib.call("svm_model_profile", model.handle, 0)
     total_s, value = job_throughput(pg, float(sum(step_ms)) / 1e3, nv, args.steps, world)
     total_ms = 1e3 * total_s
@@ -267,6 +269,7 @@ def run_ours(args):
         _lib.call("svm_brownian_step_io", model.handle, PARAMS["T"], PARAMS["dt"], PARAMS["mu"], BD_SEED + rank,
                   host_pos, host_out, C.byref(energy))
         host_pos, host_out = host_out, host_pos
+    model.fallbackCount()
     if pg:
         pg.barrier()
     t0 = time.perf_counter()
@@ -275,6 +278,7 @@ def run_ours(args):
                   host_pos, host_out, C.byref(energy))
         host_pos, host_out = host_out, host_pos
     e2e_s, e2e_value = job_throughput(pg, time.perf_counter() - t0, nv, args.steps, world)
+    fallbacks_e2e = model.fallbackCount()
 
     status = model.deviceStatus()
     model.computeGeometry()
@@ -315,7 +319,11 @@ def run_ours(args):
                    "l2": "flushed before every timed step (512 MB write); state is ~40 MB < 129 MB L2",
                    "parallelism": f"replicas x{world}" if world > 1 else "single sphere, one GPU",
                    "noise": "in-kernel Philox4x32-10"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * nv, "d2h_bytes_per_step": 24 * nv + 8},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * nv, "d2h_bytes_per_step": 24 * nv + 8,
+                "area_fallback_steps": fallbacks_e2e},
+        # steps whose total-area check failed (a near-degenerate corner's angle wrapped by 2 pi) and
+        # recomputed every area with the triangle fan, as the reference's CPU path does (~0.3 ms each)
+        "area_fallback_steps": fallbacks_timed,
         "gpu_launches": int(launches.sum()),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_force_bd" if names[dom] == "force" else f"k_{names[dom]}",

@@ -336,7 +336,9 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
             const double excess = total - 4.0 * kPI * R * R;
             scalars[0] = total;
             scalars[1] = excess;
-            *fallbackFlag = fabs(excess) > 1e-6 ? 1 : 0;
+            const int taken = fabs(excess) > 1e-6 ? 1 : 0;
+            fallbackFlag[0] = taken;
+            fallbackFlag[1] += taken;  // geometry passes that took the fallback (svm_model_fallback_count)
             *ticket = 0u;
         }
     }
@@ -1894,7 +1896,7 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->partials, (size_t)m->maxPartialBlocks * 8 * sizeof(double));
     alloc((void**)&m->ticket, 8 * sizeof(unsigned));
     alloc((void**)&m->scalars, 16 * sizeof(double));
-    alloc((void**)&m->fallbackFlag, sizeof(int));
+    alloc((void**)&m->fallbackFlag, 2 * sizeof(int));  // [0] this pass's flag, [1] passes that took it
     alloc((void**)&m->status, sizeof(int));
     alloc((void**)&m->stepCounter, sizeof(unsigned long long));
     m->t1.nWords = (int)((3 * nV + 31) / 32);
@@ -2216,6 +2218,14 @@ int svm_model_area_check(svm_model* m, double* total, double* excess, int* taken
     if (total) *total = sc[0];
     if (excess) *excess = sc[1];
     if (taken) *taken = f;
+    return SVM_OK;
+}
+
+int svm_model_fallback_count(svm_model* m, int* count) {
+    if (!m || !count) return SVM_ERR_ARG;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    SVM_CUDA(cudaMemcpy(count, m->fallbackFlag + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    SVM_CUDA(cudaMemset(m->fallbackFlag + 1, 0, sizeof(int)));
     return SVM_OK;
 }
 

@@ -276,6 +276,12 @@ class sphericalVertexModel:
     def synchronize(self):
         call("svm_model_synchronize", self._h)
 
+    def fallbackCount(self) -> int:
+        """Geometry passes that took the triangle-fan area fallback since the last call."""
+        n = C.c_int()
+        call("svm_model_fallback_count", self._h, C.byref(n))
+        return n.value
+
     def setT1Blocks(self, blocks: int = 0):
         """Blocks of the parallel T1 pass (0 automatic, 1 one block, n a cooperative grid of n);
         performance only, the results do not depend on it."""

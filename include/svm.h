@@ -147,6 +147,9 @@ int svm_model_get_vertex_neighbors(svm_model* m, int* out);
 /* The last geometry pass's total-area check (sphericalVertexModel.cpp:304-310): sum of cell
  * areas, its excess over 4 pi R^2, and whether the triangle-fan fallback replaced the areas. */
 int svm_model_area_check(svm_model* m, double* totalArea, double* excess, int* fallbackTaken);
+/* Geometry passes of a single sphere that took the triangle-fan fallback since the last call
+ * (read and cleared). */
+int svm_model_fallback_count(svm_model* m, int* count);
 /* Device status word (SVM_DEV_* bits); read and cleared. */
 int svm_model_status(svm_model* m, int* deviceStatus);
 /* T1 flips performed since the last call, as (vertex1, vertex2) pairs in the order they were

@@ -301,6 +301,7 @@ def test_area_fallback_matches_oracle(svm, oracle_mod):
     om.compute_forces()
     total, excess, taken = gm.areaCheck()
     assert taken and om.fallback_count() == 1
+    assert gm.fallbackCount() >= 1 and gm.fallbackCount() == 0  # counted, then cleared
     assert abs(excess - om.excess_area()) < 1e-9 * abs(om.excess_area())
     assert rel_err(gm.areaPerimeter(), om.area_perimeter()) < 1e-12
     assert rel_err(gm.returnForces(), om.forces()) < RTOL_FORCE
