@@ -10,6 +10,8 @@ from .model import (  # noqa: F401
     energyMinimizerFIRE,
     noiseSource,
     random_cell_centres,
+    random_vertex_directors,
+    sphericalSelfPropelledParticle,
     sphericalVertexModel,
     sphericalVertexModelBatch,
     warmStartNetwork,
@@ -17,6 +19,7 @@ from .model import (  # noqa: F401
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
-    "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "sphericalVertexModel",
+    "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "random_vertex_directors",
+    "sphericalSelfPropelledParticle", "sphericalVertexModel",
     "sphericalVertexModelBatch", "warmStartNetwork",
 ]

@@ -59,6 +59,7 @@ SIGNATURES = {
     "svm_status_string": (C.c_char_p, [i32]),
     "svm_device_count": (i32, [C.POINTER(i32)]),
     "svm_random_cell_centres": (i32, [i32, i32, dp]),
+    "svm_random_vertex_directors": (i32, [i32, i32, dp, i32, dp]),
     "svm_topology_from_points": (i32, [dp, i32, pvp]),
     "svm_topology_from_triangles": (i32, [dp, i32, ip, i32, pvp]),
     "svm_topology_sizes": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
@@ -104,6 +105,9 @@ SIGNATURES = {
     "svm_energy_noalloc": (i32, [vp, vp, f64, i32, vp, vp]),
     "svm_brownian_step": (i32, [vp, f64, f64, f64, i32, vp, u64]),
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
+    "svm_model_set_directors": (i32, [vp, dp]),
+    "svm_model_get_directors": (i32, [vp, dp]),
+    "svm_spp_step": (i32, [vp, f64, f64, f64, f64, i32, dp, u64]),
     "svm_brownian_step_io": (i32, [vp, f64, f64, f64, u64, dp, dp, C.POINTER(f64)]),
     "svm_brownian_run": (i32, [vp, f64, f64, f64, u64, i32]),
     "svm_fire_create": (i32, [vp, f64, f64, f64, f64, f64, f64, i32, f64, f64, i32, pvp]),

@@ -34,3 +34,32 @@ extern "C" int svm_random_cell_centres(int seed, int n, double* out) {
     for (int i = 0; i < n; ++i) renormalise(out + 3 * i, R);
     return SVM_OK;
 }
+
+// The vertex model's random directors (sphericalVertexModel.cpp:58-70): the model's noise source
+// continues after the cell centres and the cell model's own director draws (sphericalModel.cpp:
+// 37-63, 4 nCells uniforms), two uniforms per vertex give a random unit vector, projected onto the
+// tangent plane at the vertex and normalised (sphericalDomain.h:173-177).
+extern "C" int svm_random_vertex_directors(int seed, int nCells, const double* vertexPos, int nV, double* out) {
+    if (nCells < 4 || nV < 1 || !vertexPos || !out) return SVM_ERR_ARG;
+    std::mt19937 gen(13377);
+    if (seed >= 0) gen = std::mt19937(seed);
+    auto uniform = [&]() { std::uniform_real_distribution<double> u(0.0, 1.0); return u(gen); };
+    for (long i = 0; i < 4L * nCells; ++i) uniform();
+    for (int i = 0; i < nV; ++i) {
+        const double u2 = uniform(), v2 = uniform();
+        const double phi = 2.0 * kPI * u2, theta = std::acos(2.0 * v2 - 1);
+        double n[3] = {1.0 * std::sin(theta) * std::cos(phi), 1.0 * std::sin(theta) * std::sin(phi),
+                       1.0 * std::cos(theta)};
+        const double* p = vertexPos + 3 * i;
+        double vn = 0.0, pp = 0.0;
+        vn += n[0] * p[0]; vn += n[1] * p[1]; vn += n[2] * p[2];
+        pp += p[0] * p[0]; pp += p[1] * p[1]; pp += p[2] * p[2];
+        const double s = vn / pp;
+        for (int d = 0; d < 3; ++d) n[d] = n[d] - s * p[d];
+        double nn = 0.0;
+        nn += n[0] * n[0]; nn += n[1] * n[1]; nn += n[2] * n[2];
+        const double inv = 1.0 / std::sqrt(nn);
+        for (int d = 0; d < 3; ++d) out[3 * i + d] = inv * n[d];
+    }
+    return SVM_OK;
+}

@@ -1565,6 +1565,55 @@ __global__ void k_energy(const double2* __restrict__ ap, const double2* __restri
     }
 }
 
+// ---- self-propelled particles (sphericalSelfPropelledParticle::integrateEOMCPU,
+// src/updaters/sphericalSelfPropelledParticle.cpp:16-47) on the vertex model's directors ----------
+// The displacement dt (v0 n + mu F) and the move, in place, every product and sum rounded as on the
+// CPU (the director n as the previous step left it).
+__global__ void k_spp_move(double4_32a* __restrict__ pos, const double4_32a* __restrict__ dir,
+                           const double4_32a* __restrict__ force, double dt, double mu, double v0, int nV, double R) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 n = ld3(dir, v), f = ld3(force, v);
+    const D3 d{__dmul_rn(dt, __dadd_rn(__dmul_rn(v0, n.x), __dmul_rn(mu, f.x))),
+               __dmul_rn(dt, __dadd_rn(__dmul_rn(v0, n.y), __dmul_rn(mu, f.y))),
+               __dmul_rn(dt, __dadd_rn(__dmul_rn(v0, n.z), __dmul_rn(mu, f.z)))};
+    st3(pos, v, move_exact(ld3(pos, v), d, R));
+}
+// After the move and its T1 flips: each director projected onto the tangent plane at its vertex and
+// normalised (projectToTangentPlaneAndNormalize, sphericalDomain.h:173-177), then rotated about the
+// vertex's position vector, unnormalised as the reference passes it (rodriguesRotation,
+// inc/functions.h:175-181), by theta = r amp, amp = sqrt(2 dt tau) and r uniform in [-1/2, 1/2):
+// injected (r[v]) or from Philox counter word 3 of (vertex, step).
+template <int kNoise>
+__global__ void k_spp_dirs(const double4_32a* __restrict__ pos, double4_32a* __restrict__ dir,
+                           const double* __restrict__ r, uint64_t seed,
+                           const unsigned long long* __restrict__ stepCounter, double amp, int nV) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 p = ld3(pos, v);
+    D3 n = ld3(dir, v);
+    const double s = __ddiv_rn(dot3(n, p), dot3(p, p));
+    n = D3{__dsub_rn(n.x, __dmul_rn(s, p.x)), __dsub_rn(n.y, __dmul_rn(s, p.y)), __dsub_rn(n.z, __dmul_rn(s, p.z))};
+    const double inv = 1.0 / sqrt(dot3(n, n));
+    n = D3{__dmul_rn(inv, n.x), __dmul_rn(inv, n.y), __dmul_rn(inv, n.z)};
+    double rv;
+    if (kNoise == SVM_NOISE_BUFFER) {
+        rv = r[v];
+    } else {
+        const unsigned long long step = *stepCounter;
+        const uint4 q = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 3u),
+                                      make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+        rv = u53(q.x, q.y) - 0.5;
+    }
+    const double theta = __dmul_rn(rv, amp);
+    const double c = cos(theta), sn = sin(theta);
+    const D3 cp = cross3(p, n);
+    const double w = __dmul_rn(1.0 - c, dot3(p, n));
+    st3(dir, v, D3{__dadd_rn(__dadd_rn(__dmul_rn(c, n.x), __dmul_rn(sn, cp.x)), __dmul_rn(w, p.x)),
+                   __dadd_rn(__dadd_rn(__dmul_rn(c, n.y), __dmul_rn(sn, cp.y)), __dmul_rn(w, p.y)),
+                   __dadd_rn(__dadd_rn(__dmul_rn(c, n.z), __dmul_rn(sn, cp.z)), __dmul_rn(w, p.z))});
+}
+
 // ---- launch helpers --------------------------------------------------------------------------
 static ApplyArgs apply_args(svm_model* m, int bump) {
     ApplyArgs A;
@@ -1872,6 +1921,7 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->pos[1], nV * sizeof(double4_32a));
     alloc((void**)&m->vsph, nV * sizeof(double4_32a));
     alloc((void**)&m->vnorm, nV * sizeof(double));
+    if (nRep == 1) alloc((void**)&m->dir, nV * sizeof(double4_32a));
     if (nRep == 1) {  // the FP64 corner pass's edge terms (batches run in the mixed form only)
         alloc((void**)&m->edgeC, 3 * (size_t)nV * sizeof(double4_32a));
         alloc((void**)&m->edgeArc, 3 * (size_t)nV * sizeof(double));
@@ -1952,7 +2002,7 @@ int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (svm_fire* F : m->fires) svm::fire_detach(F);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->dir, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
@@ -2425,6 +2475,40 @@ static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64
         SVM_CUDA(cudaMemcpyAsync(posOut, m->dispBuf, sizeof(double) * 3 * m->nVertices, cudaMemcpyDeviceToHost, m->stream));
     }
     return SVM_OK;
+}
+
+int svm_model_set_directors(svm_model* m, const double* in) {
+    if (!m || !in || !m->dir) return SVM_ERR_ARG;
+    return upload_vec(m, in, m->dir, m->nVertices);
+}
+int svm_model_get_directors(svm_model* m, double* out) {
+    if (!m || !out || !m->dir) return SVM_ERR_ARG;
+    return get_vec4(m, m->dir, m->nVertices, out);
+}
+
+int svm_spp_step(svm_model* m, double dt, double mu, double v0, double tau, int noiseMode, const double* uniforms,
+                 uint64_t seed) {
+    if (!m || !m->dir || m->nRep > 1 || m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
+    if (noiseMode == SVM_NOISE_BUFFER && !uniforms) return SVM_ERR_ARG;
+    if (noiseMode == SVM_NOISE_BUFFER)
+        SVM_CUDA(cudaMemcpyAsync(m->noiseBuf, uniforms, sizeof(double) * m->nVertices, cudaMemcpyHostToDevice,
+                                 m->stream));
+    int rc = svm::launch_geometry(m);
+    if (rc || (rc = svm::launch_force_fp64(m))) return rc;
+    k_spp_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->dir, m->force, dt, mu,
+                                                                            v0, m->nVertices, m->R);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    m->cornersValid = false;
+    // moveParticles: the T1 pass unless restricted, as in the Brownian step
+    if ((rc = svm::launch_corners(m, !m->restricted)) || (rc = svm::launch_t1_apply(m, 1))) return rc;
+    const double amp = sqrt(2.0 * dt * tau);
+    if (noiseMode == SVM_NOISE_BUFFER)
+        k_spp_dirs<SVM_NOISE_BUFFER><<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
+            m->pos[m->cur], m->dir, m->noiseBuf, seed, m->stepCounter, amp, m->nVertices);
+    else
+        k_spp_dirs<SVM_NOISE_PHILOX><<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
+            m->pos[m->cur], m->dir, nullptr, seed, m->stepCounter, amp, m->nVertices);
+    return svm::check_launch();
 }
 
 int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, const double* noise) {

@@ -70,6 +70,9 @@ class sphericalVertexModel {
         setT1Threshold(0.1);  // sphericalVertexModel.cpp:13
         setPreferredParameters(a0, p0);
         setScalarModelParameter(1.0);
+        std::vector<double> dirs(3 * (size_t)nv);  // sphericalVertexModel.cpp:58-70
+        check(svm_random_vertex_directors(noise.RNGSeed, n, vp.data(), nv, dirs.data()), "svm_random_vertex_directors");
+        check(svm_model_set_directors(h, dirs.data()), "svm_model_set_directors");
         computeGeometry();
     }
 
@@ -256,6 +259,23 @@ class brownianDynamics : public updater {
         check(svm_brownian_step(model->h(), temperature, deltaT, mu, SVM_NOISE_PHILOX, nullptr, seed), "brownian step");
     }
     scalar temperature = 0.0, mu = 1.0;
+    noiseSource noise;
+};
+
+// sphericalSelfPropelledParticle (src/updaters/sphericalSelfPropelledParticle.h:13-25, with the
+// parameters of vectorialVicsek.h:31-44)
+class sphericalSelfPropelledParticle : public updater {
+  public:
+    explicit sphericalSelfPropelledParticle(bool rep = true) { reproducible = rep; noise.setReproducible(rep); }
+    void setMu(scalar m) { mu = m; }
+    void setV0(scalar v) { v0 = v; }
+    void setTau(scalar t) { tau = t; }
+    void performUpdate() override { integrateEquationOfMotion(); }
+    void integrateEquationOfMotion() {
+        const uint64_t seed = noise.RNGSeed >= 0 ? (uint64_t)noise.RNGSeed : 1337u;
+        check(svm_spp_step(model->h(), deltaT, mu, v0, tau, SVM_NOISE_PHILOX, nullptr, seed), "spp step");
+    }
+    scalar mu = 1.0, v0 = 0.0, tau = 1.0;
     noiseSource noise;
 };
 

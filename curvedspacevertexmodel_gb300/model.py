@@ -72,6 +72,15 @@ def random_cell_centres(seed: int, n: int) -> np.ndarray:
     return out.reshape(n, 3)
 
 
+def random_vertex_directors(seed: int, n_cells: int, vertex_positions: np.ndarray) -> np.ndarray:
+    """The reference vertex model's initial directors for these vertex positions (the seeded
+    stream continued after the cell centres; sphericalVertexModel.cpp:58-70)."""
+    p = np.ascontiguousarray(vertex_positions, dtype=np.float64).reshape(-1)
+    out = np.empty_like(p)
+    call("svm_random_vertex_directors", int(seed), int(n_cells), p, p.size // 3, out)
+    return out.reshape(-1, 3)
+
+
 class noiseSource:
     """Seed holder mirroring src/utilities/noiseSource.h (reproducible mt19937 seed for the
     initial cell centres; the same seed keys the in-kernel Philox stream of the dynamics)."""
@@ -120,7 +129,17 @@ class sphericalVertexModel:
         call("svm_model_set_t1_threshold", h, 0.1)
         self.setPreferredParameters(a0, p0)
         self.setScalarModelParameter(1.0)
+        self.setDirectors(random_vertex_directors(self.noise.RNGSeed, self.nCells, topology.vertexPositions))
         self.computeGeometry()
+
+    def setDirectors(self, dirs: np.ndarray):
+        """Directors, one per vertex (simpleModel.h:104-113), as used by the self-propelled updater."""
+        call("svm_model_set_directors", self._h, np.ascontiguousarray(dirs, dtype=np.float64).reshape(-1))
+
+    def returnDirectors(self) -> np.ndarray:
+        out = np.empty(3 * self.nVertices)
+        call("svm_model_get_directors", self._h, out)
+        return out.reshape(-1, 3)
 
     # ---- lifetime ----
     def close(self):
@@ -412,6 +431,58 @@ class sphericalVertexModelBatch(sphericalVertexModel):
     def precision(self, p: str):
         if p != "mixed":
             raise ValueError("batches run the mixed-precision form")
+
+
+class sphericalSelfPropelledParticle:
+    """Self-propelled vertices on the sphere (src/updaters/sphericalSelfPropelledParticle.{h,cpp}):
+    disp = dt (v0 n + mu F), then each director is re-projected and rotated by a uniform angle of
+    half-width sqrt(2 dt tau) / 2 about its vertex.  The reference's GPU branch is empty; here the
+    step runs on the device, with in-kernel Philox draws or injected uniforms."""
+
+    def __init__(self, reproducible: bool = True):
+        self.noise = noiseSource(reproducible)
+        self.model = None
+        self.deltaT = 0.01
+        self.mu = 1.0
+        self.v0 = 0.0
+        self.tau = 1.0
+        self._injected = None
+
+    def setModel(self, model: sphericalVertexModel):
+        self.model = model
+
+    def setDeltaT(self, dt: float):
+        self.deltaT = float(dt)
+
+    def setMu(self, mu: float):
+        self.mu = float(mu)
+
+    def setV0(self, v0: float):
+        self.v0 = float(v0)
+
+    def setTau(self, tau: float):
+        self.tau = float(tau)
+
+    def injectNoise(self, r: np.ndarray | None):
+        """Uniform draws in [-1/2, 1/2), one per vertex, for the next step only."""
+        self._injected = None if r is None else np.ascontiguousarray(r, dtype=np.float64).reshape(-1)
+
+    def integrateEquationOfMotion(self):
+        m = self.model
+        seed = self.noise.RNGSeed if self.noise.RNGSeed >= 0 else 1337
+        if self._injected is not None:
+            call("svm_spp_step", m.handle, self.deltaT, self.mu, self.v0, self.tau, _lib.SVM_NOISE_BUFFER,
+                 self._injected, seed)
+            self._injected = None
+        else:
+            call("svm_spp_step", m.handle, self.deltaT, self.mu, self.v0, self.tau, _lib.SVM_NOISE_PHILOX, None, seed)
+
+    def performUpdate(self):
+        self.integrateEquationOfMotion()
+
+    def run(self, nSteps: int):
+        for _ in range(int(nSteps)):
+            self.integrateEquationOfMotion()
 
 
 class brownianDynamics:

@@ -63,6 +63,10 @@ int svm_device_count(int* count);
  * then scaled to R = sqrt(n / 4 pi) (sphericalVertexModel.cpp:12).  seed < 0 keeps the default
  * engine seed 13377 (src/utilities/noiseSource.h:24).  out: double[3n]. */
 int svm_random_cell_centres(int seed, int n, double* out);
+/* The reference vertex model's initial directors (one unit tangent vector per vertex, drawn from
+ * the same seeded stream after the cell centres; sphericalVertexModel.cpp:58-70) for the given
+ * vertex positions: out[3 nV]. */
+int svm_random_vertex_directors(int seed, int nCells, const double* vertexPos, int nV, double* out);
 
 /* ---- initial topology (host) ------------------------------------------------------------
  * Replaces convexHullCGALInterface::sphericalConvexHullForVertexModel
@@ -169,6 +173,17 @@ int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5);
  * the flips and every later value are the same for any count.  Ignored by batches. */
 int svm_model_set_t1_blocks(svm_model* m, int blocks);
 int svm_model_synchronize(svm_model* m);
+/* Directors (one per vertex, simpleModel.h:104-113) of a single sphere: host double[3 Nv] in or out. */
+int svm_model_set_directors(svm_model* m, const double* dirs);
+int svm_model_get_directors(svm_model* m, double* dirs);
+/* One self-propelled-particle step (sphericalSelfPropelledParticle::integrateEOMCPU,
+ * src/updaters/sphericalSelfPropelledParticle.cpp:16-47) of a single FP64 sphere: forces,
+ * disp = dt (v0 n + mu F), move with T1 unless restricted, then each director projected onto the
+ * tangent plane, normalised and rotated about its vertex's position vector by
+ * r sqrt(2 dt tau), r uniform in [-1/2, 1/2): SVM_NOISE_BUFFER takes the Nv draws from `uniforms`
+ * (host), SVM_NOISE_PHILOX draws them in-kernel from (seed, step counter, vertex). */
+int svm_spp_step(svm_model* m, double dt, double mu, double v0, double tau, int noiseMode, const double* uniforms,
+                 uint64_t seed);
 /* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
  * z, unused) per vertex in the FP64 form, float4 in the mixed form.  Valid until the next step,
  * precision switch or svm_model_destroy. */

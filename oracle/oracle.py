@@ -68,6 +68,11 @@ def orc_lib():
         _sig(lib, "orc_flip_count", C.c_int, vp)
         _sig(lib, "orc_get_flips", None, vp, _ip)
         _sig(lib, "orc_clear_flips", None, vp)
+        _sig(lib, "orc_set_directors", None, vp, _dp)
+        _sig(lib, "orc_get_directors", None, vp, _dp)
+        _sig(lib, "orc_init_directors", None, vp, vp)
+        _sig(lib, "orc_spp_step_noise", None, vp, _dp, C.c_double, C.c_double, C.c_double, C.c_double)
+        _sig(lib, "orc_noise_uniforms", None, vp, C.c_double, C.c_double, _dp, C.c_long)
         _sig(lib, "orc_last_excess_area", C.c_double, vp)
         _sig(lib, "orc_fallback_count", C.c_int, vp)
         _sig(lib, "orc_noise_create", vp, C.c_int)
@@ -104,6 +109,11 @@ class OracleNoise:
     def normals(self, count: int) -> np.ndarray:
         out = np.empty(count, dtype=np.float64)
         self.lib.orc_noise_normals(self.h, out, count)
+        return out
+
+    def uniforms(self, count: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+        out = np.empty(count, dtype=np.float64)
+        self.lib.orc_noise_uniforms(self.h, lo, hi, out, count)
         return out
 
     def cell_centres(self, n: int) -> np.ndarray:
@@ -164,6 +174,20 @@ class OracleModel:
 
     def brownian_step_noise(self, xi, T, dt, mu=1.0):
         self.lib.orc_brownian_step_noise(self.h, np.ascontiguousarray(xi, dtype=np.float64).reshape(-1), T, dt, mu)
+
+    def spp_step_noise(self, r, dt, mu, v0, tau):
+        self.lib.orc_spp_step_noise(self.h, np.ascontiguousarray(r, dtype=np.float64).reshape(-1), dt, mu, v0, tau)
+
+    def set_directors(self, d):
+        self.lib.orc_set_directors(self.h, np.ascontiguousarray(d, dtype=np.float64).reshape(-1))
+
+    def directors(self):
+        out = np.empty(3 * self.lib.orc_num_vertices(self.h), dtype=np.float64)
+        self.lib.orc_get_directors(self.h, out)
+        return out.reshape(-1, 3)
+
+    def init_directors(self, noise):
+        self.lib.orc_init_directors(self.h, noise.h)
 
     def _vec(self, name, n):
         out = np.empty(3 * n, dtype=np.float64)

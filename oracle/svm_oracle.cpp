@@ -181,6 +181,7 @@ struct orc_model {
     double Kr = 1.0, t1Threshold = 0.1;
     bool restrictedMotion = false;
     std::vector<V3> pos, forces, vel, cellPos, curV, lastV, nextV;
+    std::vector<V3> dir;                     // directors (simpleModel.h:113), one per vertex
     std::vector<double> mass;
     std::vector<int> cellNeighbors;          // [nCells*W], index c*W + k (inc/indexer.h:41-44)
     std::vector<unsigned> cellCount;         // cellNumberOfNeighbors
@@ -200,6 +201,7 @@ orc_model* orc_create(int nCells, int nVertices, int W, const double* pos, const
     m->nCells = nCells; m->N = nVertices; m->W = W;
     m->sphere.radius = radius;
     m->pos.resize(nVertices);
+    m->dir.assign(nVertices, v3(0.0, 0.0, 0.0));
     for (int i = 0; i < nVertices; ++i) m->pos[i] = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
     m->cellNeighbors.assign(cellNeighbors, cellNeighbors + (size_t)nCells * W);
     m->cellCount.assign(cellCount, cellCount + nCells);
@@ -553,6 +555,55 @@ void orc_brownian_step_noise(orc_model* m, const double* xi, double T, double dt
     for (int i = 0; i < m->N; ++i)
         for (int d = 0; d < 3; ++d) disp[3 * i + d] = xi[3 * i + d] * np + m->forces[i].x[d] * fp;
     orc_move(m, disp.data(), 1.0);
+}
+
+// ---- self-propelled particles on the vertex model's directors -----------------------------
+// projectToTangentPlaneAndNormalize (sphericalDomain.h:173-177)
+static void projectNormalize(V3& vec, const V3& n) {
+    double s = dot(vec, n) / dot(n, n);
+    vec = sub(vec, scale(s, n));
+    vec = scale(1.0 / norm(vec), vec);
+}
+void orc_set_directors(orc_model* m, const double* d) {
+    for (int i = 0; i < m->N; ++i) m->dir[i] = v3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+}
+void orc_get_directors(orc_model* m, double* out) {
+    for (int i = 0; i < m->N; ++i)
+        for (int d = 0; d < 3; ++d) out[3 * i + d] = m->dir[i].x[d];
+}
+// The vertex model's random directors (sphericalVertexModel.cpp:58-70), drawn from the noise source
+// that made the cell centres, after them.
+void orc_init_directors(orc_model* m, orc_noise* nz) {
+    for (int i = 0; i < m->N; ++i) {
+        double u2 = orc_noise_uniform(nz, 0., 1.), v2 = orc_noise_uniform(nz, 0., 1.);
+        double phi = 2.0 * kPI * u2, theta = std::acos(2.0 * v2 - 1);
+        V3 n = v3(1.0 * std::sin(theta) * std::cos(phi), 1.0 * std::sin(theta) * std::sin(phi), 1.0 * std::cos(theta));
+        projectNormalize(n, m->pos[i]);
+        m->dir[i] = n;
+    }
+}
+// sphericalSelfPropelledParticle::integrateEOMCPU (src/updaters/sphericalSelfPropelledParticle.cpp:
+// 16-47): forces; disp = dt (v0 n + mu F); move (with T1 unless restricted); then each director is
+// projected onto the tangent plane at its vertex's new position, normalised, and rotated about
+// that position vector by theta = r sqrt(2 dt tau), r the vertex's uniform draw in [-1/2, 1/2)
+// (here supplied by the caller, Nv values).
+void orc_spp_step_noise(orc_model* m, const double* r, double dt, double mu, double v0, double tau) {
+    orc_compute_forces(m);
+    std::vector<double> disp(3 * (size_t)m->N);
+    for (int i = 0; i < m->N; ++i)
+        for (int d = 0; d < 3; ++d) disp[3 * i + d] = dt * (v0 * m->dir[i].x[d] + mu * m->forces[i].x[d]);
+    orc_move(m, disp.data(), 1.0);
+    for (int i = 0; i < m->N; ++i) {
+        double theta = r[i] * std::sqrt(2.0 * dt * tau);
+        projectNormalize(m->dir[i], m->pos[i]);
+        V3 nd = m->dir[i];
+        rodrigues(nd, m->pos[i], theta);
+        m->dir[i] = nd;
+    }
+}
+// Uniform draws getRealUniform(lo, hi) (noiseSource.cpp:18-27), count of them.
+void orc_noise_uniforms(orc_noise* nz, double lo, double hi, double* out, long count) {
+    for (long i = 0; i < count; ++i) out[i] = orc_noise_uniform(nz, lo, hi);
 }
 
 // ---- FIRE (src/updaters/energyMinimizerFIRE.cpp, velocityVerlet.cpp) ----------------------
