@@ -16,10 +16,12 @@ from .model import (  # noqa: F401
     sphericalVertexModelBatch,
     warmStartNetwork,
 )
+from .trajectory import dynamicalFeatures, logSpacedIntegers, run_trajectory, vectorValueNetCDF  # noqa: F401
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
     "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "random_vertex_directors",
     "sphericalSelfPropelledParticle", "sphericalVertexModel",
-    "sphericalVertexModelBatch", "warmStartNetwork",
+    "sphericalVertexModelBatch", "warmStartNetwork", "dynamicalFeatures", "logSpacedIntegers", "run_trajectory",
+    "vectorValueNetCDF",
 ]

@@ -105,6 +105,8 @@ SIGNATURES = {
     "svm_energy_noalloc": (i32, [vp, vp, f64, i32, vp, vp]),
     "svm_brownian_step": (i32, [vp, f64, f64, f64, i32, vp, u64]),
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
+    "svm_model_set_dynamics_reference": (i32, [vp]),
+    "svm_model_dynamics": (i32, [vp, f64, f64, C.POINTER(f64), C.POINTER(f64)]),
     "svm_model_set_directors": (i32, [vp, dp]),
     "svm_model_get_directors": (i32, [vp, dp]),
     "svm_spp_step": (i32, [vp, f64, f64, f64, f64, i32, dp, u64]),

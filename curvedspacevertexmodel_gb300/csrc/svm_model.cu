@@ -1565,6 +1565,49 @@ __global__ void k_energy(const double2* __restrict__ ap, const double2* __restri
     }
 }
 
+__global__ void k_widen4(const float4* __restrict__ in, double4_32a* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) st3(out, i, ld3(in, i));
+}
+
+// dynamicalFeatures::computeMSD / computeOverlapFunction (src/analysis/dynamicalFeatures.cpp:17-53)
+// over the first `count` cells: geodesicDistance(initial, current) per cell, the squares summed
+// (NaN distances skipped) and the distances below `cutoff` counted; both divided by count.  Block
+// sums in a fixed order, then the last block.
+template <class PT>
+__global__ void k_dynamics(const double4_32a* __restrict__ ref, const PT* __restrict__ cur, int count, double R,
+                           double cutoff, double* partials, int stride, unsigned* ticket, double* out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    double sq = 0.0, in = 0.0;
+    if (c < count) {
+        const double d = geodesic(ld3(ref, c), ld3(cur, c), R);
+        if (!isnan(d)) sq = __dmul_rn(d, d);
+        if (d < cutoff) in = 1.0;
+    }
+    const double bs = block_sum(sq), bo = block_sum(in);
+    __shared__ bool amLast;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        partials[stride + blockIdx.x] = bo;
+        __threadfence();
+        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (amLast) {
+        double s = 0.0, o = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+            s += __ldcg(partials + b);
+            o += __ldcg(partials + stride + b);
+        }
+        const double ts = block_sum(s), to = block_sum(o);
+        if (threadIdx.x == 0) {
+            out[0] = ts / count;
+            out[1] = to / count;
+            *ticket = 0u;
+        }
+    }
+}
+
 // ---- self-propelled particles (sphericalSelfPropelledParticle::integrateEOMCPU,
 // src/updaters/sphericalSelfPropelledParticle.cpp:16-47) on the vertex model's directors ----------
 // The displacement dt (v0 n + mu F) and the move, in place, every product and sum rounded as on the
@@ -2002,7 +2045,7 @@ int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (svm_fire* F : m->fires) svm::fire_detach(F);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->dir, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->dir, m->cellRef, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
@@ -2474,6 +2517,43 @@ static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64
         }
         SVM_CUDA(cudaMemcpyAsync(posOut, m->dispBuf, sizeof(double) * 3 * m->nVertices, cudaMemcpyDeviceToHost, m->stream));
     }
+    return SVM_OK;
+}
+
+int svm_model_set_dynamics_reference(svm_model* m) {
+    if (!m || m->nRep > 1) return SVM_ERR_ARG;
+    if (!m->cellRef && cudaMalloc((void**)&m->cellRef, m->nCells * sizeof(double4_32a)) != cudaSuccess) {
+        m->cellRef = nullptr;
+        return SVM_ERR_CUDA;
+    }
+    if (m->precision == SVM_PRECISION_MIXED)
+        k_widen4<<<svm::blocksFor(m->nCells), svm::kBlock, 0, m->stream>>>(m->cellPos32, m->cellRef, m->nCells);
+    else
+        SVM_CUDA(cudaMemcpyAsync(m->cellRef, m->cellPos, m->nCells * sizeof(double4_32a), cudaMemcpyDeviceToDevice,
+                                 m->stream));
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_dynamics(svm_model* m, double fraction, double cutoff, double* msd, double* overlap) {
+    if (!m || !m->cellRef || !(fraction > 0.0) || fraction > 1.0) return SVM_ERR_ARG;
+    const int count = fraction < 1.0 ? (int)std::floor(m->nCells * fraction) : m->nCells;
+    if (count < 1) return SVM_ERR_ARG;
+    const int nb = svm::blocksFor(count);
+    double* part = m->partials + 2 * m->maxPartialBlocks;
+    if (m->precision == SVM_PRECISION_MIXED)
+        k_dynamics<float4><<<nb, svm::kBlock, 0, m->stream>>>(m->cellRef, m->cellPos32, count, m->R, cutoff, part,
+                                                             m->maxPartialBlocks, m->ticket + 2, m->scalars + 4);
+    else
+        k_dynamics<double4_32a><<<nb, svm::kBlock, 0, m->stream>>>(m->cellRef, m->cellPos, count, m->R, cutoff, part,
+                                                                  m->maxPartialBlocks, m->ticket + 2, m->scalars + 4);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    double r[2];
+    SVM_CUDA(cudaMemcpyAsync(r, m->scalars + 4, sizeof(r), cudaMemcpyDeviceToHost, m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    if (msd) *msd = r[0];
+    if (overlap) *overlap = r[1];
     return SVM_OK;
 }
 

@@ -173,6 +173,13 @@ int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5);
  * the flips and every later value are the same for any count.  Ignored by batches. */
 int svm_model_set_t1_blocks(svm_model* m, int blocks);
 int svm_model_synchronize(svm_model* m);
+/* Dynamical observables of the cell positions (dynamicalFeatures, src/analysis/dynamicalFeatures.cpp):
+ * svm_model_set_dynamics_reference snapshots the current cell positions (as computed by the last
+ * geometry pass) on the device; svm_model_dynamics returns, over the first floor(N fraction)
+ * cells, the mean squared geodesic displacement from them (NaN distances skipped) and the fraction
+ * of cells displaced by less than `cutoff` (the reference's default 0.5). */
+int svm_model_set_dynamics_reference(svm_model* m);
+int svm_model_dynamics(svm_model* m, double fraction, double cutoff, double* msd, double* overlap);
 /* Directors (one per vertex, simpleModel.h:104-113) of a single sphere: host double[3 Nv] in or out. */
 int svm_model_set_directors(svm_model* m, const double* dirs);
 int svm_model_get_directors(svm_model* m, double* dirs);

@@ -68,6 +68,9 @@ def orc_lib():
         _sig(lib, "orc_flip_count", C.c_int, vp)
         _sig(lib, "orc_get_flips", None, vp, _ip)
         _sig(lib, "orc_clear_flips", None, vp)
+        _sig(lib, "orc_dynamics", None, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
+             C.POINTER(C.c_double), C.POINTER(C.c_double))
+        _sig(lib, "orc_log_spaced", None, C.c_int, C.c_double, C.c_int, _ip)
         _sig(lib, "orc_set_directors", None, vp, _dp)
         _sig(lib, "orc_get_directors", None, vp, _dp)
         _sig(lib, "orc_init_directors", None, vp, vp)
@@ -448,3 +451,19 @@ class RefModel:
         rings, cnt = self.rings(W)
         return dict(pos=self.positions(), rings=rings, counts=cnt, vcells=self.vertex_cells(),
                     vnbrs=self.vertex_neighbors(), radius=self.radius)
+
+
+def dynamics(initial, current, radius, fraction=1.0, cutoff=0.5):
+    """computeMSD and computeOverlapFunction (src/analysis/dynamicalFeatures.cpp:17-53)."""
+    a = np.ascontiguousarray(initial, dtype=np.float64).reshape(-1)
+    b = np.ascontiguousarray(current, dtype=np.float64).reshape(-1)
+    msd, ov = C.c_double(), C.c_double()
+    orc_lib().orc_dynamics(a, b, a.size // 3, fraction, radius, cutoff, C.byref(msd), C.byref(ov))
+    return msd.value, ov.value
+
+
+def log_spaced(first_save, exponent, count):
+    """The first `count` save steps of logSpacedIntegers (inc/simpleUtilities.h:5-41)."""
+    out = np.empty(count, dtype=np.int32)
+    orc_lib().orc_log_spaced(int(first_save), float(exponent), int(count), out)
+    return out

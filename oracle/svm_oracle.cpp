@@ -606,6 +606,43 @@ void orc_noise_uniforms(orc_noise* nz, double lo, double hi, double* out, long c
     for (long i = 0; i < count; ++i) out[i] = orc_noise_uniform(nz, lo, hi);
 }
 
+// ---- dynamicalFeatures (src/analysis/dynamicalFeatures.cpp:6-53) --------------------------
+// computeMSD and computeOverlapFunction over the first floor(n fraction) points (all when
+// fraction >= 1), in index order; NaN distances are skipped by the MSD (the reference prints them).
+void orc_dynamics(const double* init, const double* cur, int n, double fraction, double radius, double cutoff,
+                  double* msdOut, double* overlapOut) {
+    Sphere s; s.radius = radius;
+    int N = n;
+    if (fraction < 1) N = (int)std::floor(N * fraction);
+    double msd = 0.0, overlap = 0.0;
+    for (int i = 0; i < N; ++i) {
+        V3 a = v3(init[3 * i], init[3 * i + 1], init[3 * i + 2]), b = v3(cur[3 * i], cur[3 * i + 1], cur[3 * i + 2]);
+        double d = s.geodesic(a, b);
+        if (!std::isnan(d)) msd += d * d;
+        if (d < cutoff) overlap += 1;
+    }
+    *msdOut = msd / N;
+    *overlapOut = overlap / N;
+}
+
+// ---- logSpacedIntegers (inc/simpleUtilities.h:5-41) ---------------------------------------
+// The first `count` save steps: the constructor's nextSave, then nextSave after each update().
+void orc_log_spaced(int firstSave, double exponent, int count, int* out) {
+    int nextSave = firstSave, logSaveIdx = 0;
+    const double base = std::pow(10.0, exponent);
+    if (nextSave != 0) {
+        int tempCur = 0;
+        while (tempCur < nextSave) { logSaveIdx += 1; tempCur = (int)std::round(std::pow(base, logSaveIdx)); }
+    }
+    for (int i = 0; i < count; ++i) {
+        out[i] = nextSave;
+        logSaveIdx += 1;
+        int curSave = (int)std::round(std::pow(base, logSaveIdx));
+        while (curSave == nextSave) { logSaveIdx += 1; curSave = (int)std::round(std::pow(base, logSaveIdx)); }
+        nextSave = curSave;
+    }
+}
+
 // ---- FIRE (src/updaters/energyMinimizerFIRE.cpp, velocityVerlet.cpp) ----------------------
 struct orc_fire {
     double deltaT = 0.01, deltaTMin = 0.0001, deltaTMax = 0.1, deltaTInc = 1.05, deltaTDec = 0.95;
