@@ -8,6 +8,7 @@ from .model import (  # noqa: F401
     Topology,
     brownianDynamics,
     energyMinimizerFIRE,
+    neighborList,
     noiseSource,
     random_cell_centres,
     random_vertex_directors,
@@ -20,7 +21,7 @@ from .trajectory import dynamicalFeatures, logSpacedIntegers, run_trajectory, ve
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
-    "energyMinimizerFIRE", "noiseSource", "random_cell_centres", "random_vertex_directors",
+    "energyMinimizerFIRE", "neighborList", "noiseSource", "random_cell_centres", "random_vertex_directors",
     "sphericalSelfPropelledParticle", "sphericalVertexModel",
     "sphericalVertexModelBatch", "warmStartNetwork", "dynamicalFeatures", "logSpacedIntegers", "run_trajectory",
     "vectorValueNetCDF",

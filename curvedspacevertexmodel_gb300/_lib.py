@@ -107,6 +107,13 @@ SIGNATURES = {
     "svm_brownian_step_host_noise": (i32, [vp, f64, f64, f64, dp]),
     "svm_model_set_dynamics_reference": (i32, [vp]),
     "svm_model_dynamics": (i32, [vp, f64, f64, C.POINTER(f64), C.POINTER(f64)]),
+    "svm_neighbor_list_create": (i32, [f64, f64, i32, i32, i32, vp, pvp]),
+    "svm_neighbor_list_destroy": (i32, [vp]),
+    "svm_neighbor_list_compute": (i32, [vp, vp, i32]),
+    "svm_neighbor_list_compute_model": (i32, [vp, vp]),
+    "svm_neighbor_list_get": (i32, [vp, C.POINTER(i32), _nullable(np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")),
+                                     _nullable(np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")), dp, dp,
+                                     C.c_long]),
     "svm_model_set_directors": (i32, [vp, dp]),
     "svm_model_get_directors": (i32, [vp, dp]),
     "svm_spp_step": (i32, [vp, f64, f64, f64, f64, i32, dp, u64]),

@@ -10,8 +10,10 @@
 //   k_cl_bin     bin each point, take a provisional slot with an atomic
 //   k_cl_order   rank each point among its bin's entries by index, write the final slot
 //   k_cl_nmax    Nmax = max(Nmax, largest occupancy), the grow-only width of the reference
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 #include "svm_internal.cuh"
 
@@ -110,9 +112,189 @@ int compute(svm_cell_list* cl, P pts, int np) {
     k_cl_nmax<<<1, 1, 0, cl->stream>>>(cl->scalars);
     return check_launch();
 }
+// neighborList (src/utilities/neighborList.cpp:6-18, 96-151; kernels neighborList.cu:108-357): per
+// point, over the adjacent bins of its (clamped) bin in the mask's order and each bin's points in
+// slot order, every other point whose minimum-image displacement (periodic box of side 2 radius,
+// periodicBoundaryConditions.h:124-132) is shorter than `range`; the first nmax are stored, the
+// count is kept whole (the host grows nmax and recomputes when a count exceeds it).  range2Hi is
+// an upper bound of range^2: a candidate with dd above it has sqrt(dd) > range, so its correctly
+// rounded root is >= range too and the root need not be taken (sqrt is monotone and range is a
+// double); every other candidate is decided by the reference's own test on the rounded root.
+template <typename P>
+__global__ void k_nl(P pts, int np, const unsigned* __restrict__ counts, const int* __restrict__ slots, int cap,
+                     int nside, double h, double radius, double range, double range2Hi,
+                     const int* __restrict__ mask, int K,
+                     int nmax, unsigned* __restrict__ npp, int* __restrict__ idx, double* __restrict__ vec,
+                     double* __restrict__ dist, int* __restrict__ maxCount) {
+    const int pp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pp >= np) return;
+    double t[3];
+    pts(pp, t[0], t[1], t[2]);
+    int c[3];
+    for (int d = 0; d < 3; ++d) c[d] = max(0, min(nside - 1, (int)floor((t[d] + radius) / h)));
+    int count = 0;
+    for (int cc = 0; cc < K; ++cc) {
+        int nb[3];
+        for (int d = 0; d < 3; ++d) {
+            nb[d] = (c[d] + mask[3 * cc + d]) % nside;
+            if (nb[d] < 0) nb[d] += nside;
+        }
+        const long cell = nb[0] + (long)nb[1] * nside + (long)nb[2] * nside * nside;
+        const int n = min((int)counts[cell], cap);
+        for (int p1 = 0; p1 < n; ++p1) {
+            const int j = slots[cell * cap + p1];
+            if (j == pp) continue;
+            double q[3], disp[3];
+            pts(j, q[0], q[1], q[2]);
+            for (int d = 0; d < 3; ++d) {
+                disp[d] = t[d] - q[d];
+                while (disp[d] < -radius) disp[d] += 2. * radius;
+                while (disp[d] > radius) disp[d] -= 2. * radius;
+            }
+            const double dd = disp[0] * disp[0] + disp[1] * disp[1] + disp[2] * disp[2];
+            if (dd > range2Hi) continue;  // sqrt(dd) > range: the rounded root is >= range as well
+            const double r = sqrt(dd);
+            if (r >= range) continue;
+            if (count < nmax) {
+                const long at = (long)pp * nmax + count;
+                idx[at] = j;
+                vec[3 * at] = disp[0]; vec[3 * at + 1] = disp[1]; vec[3 * at + 2] = disp[2];
+                dist[at] = r;
+            }
+            ++count;
+        }
+    }
+    npp[pp] = (unsigned)count;
+    atomicMax(maxCount, count);
+}
+}  // namespace
+
+struct svm_neighbor_list {
+    svm_cell_list* cl = nullptr;
+    double range = 1.0, radius = 1.0;
+    int nPoints = 0, nmax = 4, K = 0;   // Nmax starts at 4 (neighborList.cpp:17)
+    int* mask = nullptr;                // [3 K] adjacent-bin offsets
+    unsigned* npp = nullptr;            // [nPoints]
+    int* idx = nullptr;                 // [nPoints * nmax]
+    double* vec = nullptr;              // [nPoints * nmax * 3]
+    double* dist = nullptr;             // [nPoints * nmax]
+    int* maxCount = nullptr;
+};
+
+namespace {
+int nl_alloc(svm_neighbor_list* nl) {
+    cudaFree(nl->idx); cudaFree(nl->vec); cudaFree(nl->dist);
+    nl->idx = nullptr; nl->vec = nullptr; nl->dist = nullptr;
+    const size_t e = (size_t)nl->nPoints * nl->nmax;
+    if (cudaMalloc(&nl->idx, sizeof(int) * e) != cudaSuccess || cudaMalloc(&nl->vec, sizeof(double) * 3 * e) != cudaSuccess ||
+        cudaMalloc(&nl->dist, sizeof(double) * e) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    return SVM_OK;
+}
+
+template <typename P>
+int nl_compute(svm_neighbor_list* nl, P pts, int np) {
+    if (np != nl->nPoints) return SVM_ERR_ARG;
+    svm_cell_list* cl = nl->cl;
+    const size_t nb = (np + kB - 1) / kB;
+    for (int pass = 0; pass < 64; ++pass) {   // a second pass at most: the first finds the largest count
+        const size_t e = (size_t)np * nl->nmax;
+        cudaMemsetAsync(nl->idx, 0, sizeof(int) * e, cl->stream);   // resetNeighbors: zero past each count
+        cudaMemsetAsync(nl->vec, 0, sizeof(double) * 3 * e, cl->stream);
+        cudaMemsetAsync(nl->dist, 0, sizeof(double) * e, cl->stream);
+        cudaMemsetAsync(nl->maxCount, 0, sizeof(int), cl->stream);
+        k_nl<<<nb, kB, 0, cl->stream>>>(pts, np, cl->counts, cl->slots, cl->cap, cl->nside, cl->h, cl->radius, nl->range,
+                                        nl->range * nl->range * (1.0 + 0x1p-48), nl->mask, nl->K, nl->nmax, nl->npp, nl->idx, nl->vec, nl->dist, nl->maxCount);
+        if (check_launch()) return SVM_ERR_CUDA;
+        int mc = 0, sc[4];
+        if (cudaMemcpyAsync(&mc, nl->maxCount, sizeof(int), cudaMemcpyDeviceToHost, cl->stream) != cudaSuccess ||
+            cudaMemcpyAsync(sc, cl->scalars, sizeof(sc), cudaMemcpyDeviceToHost, cl->stream) != cudaSuccess ||
+            cudaStreamSynchronize(cl->stream) != cudaSuccess)
+            return SVM_ERR_CUDA;
+        if (sc[2] || sc[3]) return SVM_ERR_DEVICE;  // the cell list overflowed a bin or lost a point
+        if (mc <= nl->nmax) return SVM_OK;
+        nl->nmax = mc;  // grow-only, then recompute
+        if (nl_alloc(nl)) return SVM_ERR_CUDA;
+    }
+    return SVM_ERR_DEVICE;
+}
 }  // namespace
 
 extern "C" {
+
+int svm_neighbor_list_create(double range, double radius, int subGridReduction, int nPoints, int slotCapacity,
+                             void* stream, svm_neighbor_list** out) {
+    if (!(range > 0) || !(radius > 0) || subGridReduction < 1 || nPoints <= 0 || !out) return SVM_ERR_ARG;
+    svm_neighbor_list* nl = new svm_neighbor_list();
+    nl->range = range; nl->radius = radius; nl->nPoints = nPoints;
+    int rc = svm_cell_list_create(range * (1. / (double)subGridReduction), radius, nPoints, slotCapacity, stream, &nl->cl);
+    if (rc) { delete nl; return rc; }
+    // computeAdjacentCells (hyperrectangularCellList.cpp:219-262): offsets in iVecIterate order
+    // (x fastest) whose nearest corner lies within `width` bins
+    const int width = subGridReduction;
+    const double h = nl->cl->h;
+    std::vector<int> mask;
+    for (int z = -width; z <= width; ++z)
+        for (int y = -width; y <= width; ++y)
+            for (int x = -width; x <= width; ++x) {
+                const int g[3] = {x, y, z};
+                double rmin = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    const double t = h * (std::max(std::abs(g[d]) - 1., 0.0));
+                    rmin += t * t;
+                }
+                rmin = std::sqrt(rmin);
+                if (rmin < h * width + 1e-6) { mask.push_back(x); mask.push_back(y); mask.push_back(z); }
+            }
+    nl->K = (int)mask.size() / 3;
+    bool ok = cudaMalloc(&nl->mask, sizeof(int) * mask.size()) == cudaSuccess &&
+              cudaMalloc(&nl->npp, sizeof(unsigned) * nPoints) == cudaSuccess &&
+              cudaMalloc(&nl->maxCount, sizeof(int)) == cudaSuccess && nl_alloc(nl) == SVM_OK;
+    if (ok) ok = cudaMemcpy(nl->mask, mask.data(), sizeof(int) * mask.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) { svm_neighbor_list_destroy(nl); return SVM_ERR_CUDA; }
+    *out = nl;
+    return SVM_OK;
+}
+
+int svm_neighbor_list_destroy(svm_neighbor_list* nl) {
+    if (!nl) return SVM_ERR_ARG;
+    if (nl->cl) svm_cell_list_destroy(nl->cl);
+    void* ptrs[] = {nl->mask, nl->npp, nl->idx, nl->vec, nl->dist, nl->maxCount};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    delete nl;
+    return SVM_OK;
+}
+
+int svm_neighbor_list_compute(svm_neighbor_list* nl, const double* pts, int n) {
+    if (!nl || !pts) return SVM_ERR_ARG;
+    int rc = svm_cell_list_compute(nl->cl, pts, n);
+    return rc ? rc : nl_compute(nl, AosPoints{pts}, n);
+}
+
+int svm_neighbor_list_compute_model(svm_neighbor_list* nl, svm_model* m) {
+    if (!nl || !m) return SVM_ERR_ARG;
+    int rc = svm_cell_list_compute_model(nl->cl, m);
+    if (rc) return rc;
+    if (m->precision == SVM_PRECISION_MIXED) return nl_compute(nl, ModelPoints32{m->pos32[m->cur]}, m->nVertices);
+    return nl_compute(nl, ModelPoints{m->pos[m->cur]}, m->nVertices);
+}
+
+int svm_neighbor_list_get(svm_neighbor_list* nl, int* nmax, unsigned* npp, int* idx, double* vec, double* dist,
+                          long capacity) {
+    if (!nl) return SVM_ERR_ARG;
+    if (nmax) *nmax = nl->nmax;
+    const size_t e = (size_t)nl->nPoints * nl->nmax;
+    if ((idx || vec || dist) && (long)e > capacity) return SVM_ERR_ARG;
+    cudaStream_t s = nl->cl->stream;
+    if (npp && cudaMemcpyAsync(npp, nl->npp, sizeof(unsigned) * nl->nPoints, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    if (idx && cudaMemcpyAsync(idx, nl->idx, sizeof(int) * e, cudaMemcpyDeviceToHost, s) != cudaSuccess) return SVM_ERR_CUDA;
+    if (vec && cudaMemcpyAsync(vec, nl->vec, sizeof(double) * 3 * e, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    if (dist && cudaMemcpyAsync(dist, nl->dist, sizeof(double) * e, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    return cudaStreamSynchronize(s) == cudaSuccess ? SVM_OK : SVM_ERR_CUDA;
+}
 
 int svm_cell_list_create(double a, double radius, int nPoints, int cap, void* stream, svm_cell_list** out) {
     if (!(a > 0) || !(radius > 0) || nPoints <= 0 || cap < 2 || !out) return SVM_ERR_ARG;

@@ -682,6 +682,66 @@ class warmStartNetwork:
         call("svm_mlp_warm_start", self._h, model.handle)
 
 
+class neighborList:
+    """Metric neighbour lists of points on the device (src/utilities/neighborList.{h,cpp}): every
+    other point within `range` (minimum image in a periodic box of side 2 sphereRadius), through a
+    cell list of grid size range / subGridReduction.  The spherical model's own is
+    neighborList(1.0, R + 2.5) (sphericalModel.cpp:21)."""
+
+    def __init__(self, range_: float, sphereRadius: float, subGridReduction: int = 1, slotCapacity: int = 16):
+        self.maxRange = float(range_)
+        self.radius = float(sphereRadius)
+        self.subGridReduction = int(subGridReduction)
+        self.slotCapacity = int(slotCapacity)
+        self._h = None
+        self._n = 0
+
+    def _ensure(self, n: int):
+        if self._h is not None and self._n == n:
+            return
+        self.close()
+        h = C.c_void_p()
+        call("svm_neighbor_list_create", self.maxRange, self.radius, self.subGridReduction, int(n),
+             self.slotCapacity, None, C.byref(h))
+        self._h, self._n = h, int(n)
+
+    def computeNeighborLists(self, points, fetch: bool = True):
+        """`points`: a sphericalVertexModel (its vertex positions) or a torch CUDA tensor of shape
+        (n, 3), float64.  fetch=False leaves the lists on the device (Nmax is still read)."""
+        if isinstance(points, sphericalVertexModel):
+            self._ensure(points.nVertices)
+            call("svm_neighbor_list_compute_model", self._h, points.handle)
+        else:
+            n = int(points.shape[0])
+            self._ensure(n)
+            call("svm_neighbor_list_compute", self._h, C.c_void_p(points.data_ptr()), n)
+        nm = C.c_int()
+        if not fetch:
+            call("svm_neighbor_list_get", self._h, C.byref(nm), None, None, None, None, 0)
+            self.Nmax = nm.value
+            return
+        npp = np.empty(self._n, dtype=np.uint32)
+        call("svm_neighbor_list_get", self._h, C.byref(nm), npp, None, None, None, 0)
+        e = self._n * nm.value
+        idx = np.empty(e, dtype=np.int32)
+        vec = np.empty(3 * e)
+        dist = np.empty(e)
+        call("svm_neighbor_list_get", self._h, C.byref(nm), npp, idx, vec, dist, e)
+        self.Nmax = nm.value
+        self.neighborsPerParticle = npp
+        self.particleIndices = idx.reshape(self._n, self.Nmax)
+        self.neighborVectors = vec.reshape(self._n, self.Nmax, 3)
+        self.neighborDistances = dist.reshape(self._n, self.Nmax)
+
+    def close(self):
+        if self._h is not None:
+            _lib.lib().svm_neighbor_list_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 class Simulation:
     """Ordered updaters over one configuration (src/simulation/simulation.{h,cpp})."""
 

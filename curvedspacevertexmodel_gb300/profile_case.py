@@ -9,7 +9,9 @@ as the reference driver does), `equil` graph-replayed steps at the run parameter
 With --mixed the `steps` steps run in the mixed-precision form (kernels k32_*); with --replicas R
 a batch of R replicas runs instead (stabilisation, then `steps` steps at per-replica P0 and T);
 with --fire K the `steps` Brownian steps are followed by K FIRE iterations (energyMinimizerFIRE,
-the reference's default parameters, force tolerance 1e-12 so that all K run).
+the reference's default parameters, force tolerance 1e-12 so that all K run); with --neighbors K
+the vertices' neighbour list (range 1, radius R + 2.5, the model's own) is then computed K times
+and the mean time of a computation (device lists, Nmax read back) is printed.
 """
 from __future__ import annotations
 
@@ -32,6 +34,8 @@ def main():
                     help="instead: a batch of this many replicas, N log-uniform in [100, 5000] (seeded), "
                          "P0 U[3.6, 3.95], T logU[1e-4, 1e-1]")
     ap.add_argument("--fire", type=int, default=0, help="FIRE iterations after the Brownian steps")
+    ap.add_argument("--neighbors", type=int, default=0, help="neighbour-list computations after the steps")
+    ap.add_argument("--sub-grid", type=int, default=1, help="the neighbour list's subGridReduction")
     args = ap.parse_args()
     t0 = time.time()
     if args.replicas:
@@ -78,6 +82,15 @@ def main():
         fire.setMaximumIterations(args.fire)
         fire.setForceCutoff(1e-12)
         fire.minimize()
+    if args.neighbors:
+        nl = svm.neighborList(1.0, m.radius + 2.5, args.sub_grid)
+        nl.computeNeighborLists(m, fetch=False)  # sizes the lists
+        t1 = time.perf_counter()
+        for _ in range(args.neighbors):
+            nl.computeNeighborLists(m, fetch=False)
+        dt = (time.perf_counter() - t1) / args.neighbors
+        print(f"neighbour list: {m.nVertices} points, Nmax {nl.Nmax}, {dt * 1e3:.3f} ms per computation")
+        nl.close()
     m.computeGeometry()
     print(f"cells {args.cells} vertices {m.nVertices} energy/cell {m.computeEnergy() / args.cells:.6g} "
           f"status {m.deviceStatus()} wall {time.time() - t0:.1f} s")

@@ -287,6 +287,25 @@ int svm_cell_list_compute(svm_cell_list* cl, const double* pointsDevice, int n);
 int svm_cell_list_get(svm_cell_list* cl, int* nside, int* nmax, unsigned* counts, int* slots, long slotsCapacity);
 int svm_cell_list_bins(svm_cell_list* cl, int* binOfPoint);
 
+/* ---- neighbour list ------------------------------------------------------------------------
+ * neighborList (src/utilities/neighborList.{h,cpp}; the spherical model builds it with range 1 and
+ * radius R + 2.5, sphericalModel.cpp:21): a cell list of grid size range / subGridReduction over
+ * [-radius, radius]^3 (slotCapacity points per bin at most), then per point every other point at
+ * minimum-image distance below `range` in a periodic box of side 2 radius, listed in the order of
+ * the adjacent bins (computeAdjacentCells) and of each bin's slots.  Nmax starts at 4 and grows to
+ * the largest count (the list is recomputed then). */
+typedef struct svm_neighbor_list svm_neighbor_list;
+int svm_neighbor_list_create(double range, double radius, int subGridReduction, int nPoints, int slotCapacity,
+                             void* stream, svm_neighbor_list** out);
+int svm_neighbor_list_destroy(svm_neighbor_list* nl);
+/* Caller points (DEVICE double[3*n] AoS), or the model's current vertex positions. */
+int svm_neighbor_list_compute(svm_neighbor_list* nl, const double* pointsDevice, int n);
+int svm_neighbor_list_compute_model(svm_neighbor_list* nl, svm_model* m);
+/* Nmax; per point the neighbour count [n]; per (point, k < Nmax), k-major within a point: index,
+ * displacement (3 doubles) and distance, zero past the count (capacity >= n Nmax entries). */
+int svm_neighbor_list_get(svm_neighbor_list* nl, int* nmax, unsigned* npp, int* idx, double* vec, double* dist,
+                          long capacity);
+
 /* ---- batches of replicas -------------------------------------------------------------------
  * No counterpart in the reference, which runs one sphere per process (its seed loops,
  * minimization.cpp:98-132, run instances one after another).  A batch is one svm_model holding

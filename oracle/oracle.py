@@ -71,6 +71,8 @@ def orc_lib():
         _sig(lib, "orc_dynamics", None, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
              C.POINTER(C.c_double), C.POINTER(C.c_double))
         _sig(lib, "orc_log_spaced", None, C.c_int, C.c_double, C.c_int, _ip)
+        _sig(lib, "orc_neighbor_list", C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, _up, _ip, _dp,
+             _dp, C.c_long)
         _sig(lib, "orc_set_directors", None, vp, _dp)
         _sig(lib, "orc_get_directors", None, vp, _dp)
         _sig(lib, "orc_init_directors", None, vp, vp)
@@ -341,6 +343,8 @@ def ref_lib():
         _sig(lib, "ref_get_vertex_cells", None, vp, _ip)
         _sig(lib, "ref_get_vertex_neighbors", None, vp, _ip)
         _sig(lib, "ref_cell_list", C.c_int, vp, C.POINTER(C.c_int), _up, _ip, C.c_long)
+        _sig(lib, "ref_neighbor_list", C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.c_int, _up, _ip, _dp, _dp,
+             C.c_long)
         _ref = lib
     return _ref
 
@@ -467,3 +471,25 @@ def log_spaced(first_save, exponent, count):
     out = np.empty(count, dtype=np.int32)
     orc_lib().orc_log_spaced(int(first_save), float(exponent), int(count), out)
     return out
+
+
+def neighbor_list(points, range_, radius, sub_grid=1, reference=False):
+    """neighborList::computeCPU (src/utilities/neighborList.cpp:96-151): (Nmax, counts, indices,
+    displacements, distances) with the per-point arrays of width Nmax.  reference=True runs the
+    reference's own class from oracle/_ref instead of the restatement."""
+    p = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+    n = p.size // 3
+    cap = n * 8
+    while True:
+        npp = np.empty(n, dtype=np.uint32)
+        idx = np.empty(cap, dtype=np.int32)
+        vec = np.empty(3 * cap)
+        dist = np.empty(cap)
+        if reference:
+            nm = ref_lib().ref_neighbor_list(p, n, range_, radius, sub_grid, npp, idx, vec, dist, cap)
+        else:
+            nm = orc_lib().orc_neighbor_list(p, n, range_, radius, sub_grid, 4, npp, idx, vec, dist, cap)
+        if nm > 0:
+            e = n * nm
+            return nm, npp, idx[:e].reshape(n, nm), vec[:3 * e].reshape(n, nm, 3), dist[:e].reshape(n, nm)
+        cap = n * (-nm)

@@ -14,6 +14,7 @@
 #include "simulation.h"
 #include "noiseSource.h"
 #include "hyperrectangularCellList.h"
+#include "neighborList.h"
 
 struct ref_handle {
     noiseSource initNoise{true};
@@ -133,6 +134,37 @@ int ref_cell_list(ref_handle* h, int* nsideOut, unsigned* counts, int* idx, long
         counts[b] = e.data[b];
         for (int s = 0; s < Nmax; ++s)
             idx[(long)b * Nmax + s] = s < (int)e.data[b] ? pi.data[cl.cellListIndexer(s, b)] : -1;
+    }
+    return Nmax;
+}
+
+// neighborList(range, radius, subGrid).computeNeighborLists over caller points (neighborList.cpp:
+// 7-20, 96-151, CPU branch).  Returns Nmax, or -Nmax when `capacity` (entries) is too small.
+int ref_neighbor_list(const double* pts, int np, double range, double radius, int subGrid, unsigned* npp, int* idx,
+                      double* vec, double* dist, long capacity) {
+    GPUArray<dVec> points((unsigned int)np, true);
+    {
+        ArrayHandle<dVec> p(points, access_location::host, access_mode::overwrite);
+        for (int i = 0; i < np; ++i)
+            for (int d = 0; d < 3; ++d) p.data[i].x[d] = pts[3 * i + d];
+    }
+    neighborList nl(range, radius, subGrid);
+    nl.computeNeighborLists(points);
+    const int Nmax = nl.Nmax;
+    if ((long)np * Nmax > capacity) return -Nmax;
+    ArrayHandle<unsigned int> hn(nl.neighborsPerParticle, access_location::host, access_mode::read);
+    ArrayHandle<int> hi(nl.particleIndices, access_location::host, access_mode::read);
+    ArrayHandle<dVec> hv(nl.neighborVectors, access_location::host, access_mode::read);
+    ArrayHandle<scalar> hd(nl.neighborDistances, access_location::host, access_mode::read);
+    for (int pp = 0; pp < np; ++pp) {
+        npp[pp] = hn.data[pp];
+        for (int k = 0; k < Nmax; ++k) {
+            const int at = nl.neighborIndexer(k, pp);
+            const long o = (long)pp * Nmax + k;
+            idx[o] = hi.data[at];
+            dist[o] = hd.data[at];
+            for (int d = 0; d < 3; ++d) vec[3 * o + d] = hv.data[at].x[d];
+        }
     }
     return Nmax;
 }

@@ -785,4 +785,99 @@ int orc_cell_list(const double* pts, int np, double a, double radius, int* nmaxI
     return 0;
 }
 
+// neighborList (src/utilities/neighborList.cpp:6-18, 96-151): a cell list of grid size
+// range / subGridReduction over [-radius, radius]^3, adjacent cells within `width` =
+// subGridReduction (computeAdjacentCells, hyperrectangularCellList.cpp:219-262: the offsets in
+// iVecIterate order, x fastest, kept if the nearest corner is within width cells, wrapped
+// periodically), then per point, in cell-list slot order, every other point at minimum-image
+// distance (periodic box of side 2 radius, periodicBoundaryConditions.h:124-132) below `range`.
+// Nmax starts at 4 and grows to the largest count.  Outputs [Np] counts and [Np * Nmax] index,
+// displacement (3 doubles) and distance, zero past each count; returns Nmax.
+int orc_neighbor_list(const double* pts, int np, double range, double radius, int subGrid, int nmaxIn,
+                      unsigned* nppOut, int* idxOut, double* vecOut, double* distOut, long capacity) {
+    int nside; double h;
+    const double a = range * (1. / (double)subGrid);
+    orc_cell_list_dims(a, radius, &nside, &h);
+    const long total = (long)nside * nside * nside;
+    int cellNmax = 2;  // the cell list's own width, grown by its first pass
+    std::vector<int> bins(np);
+    std::vector<unsigned> counts(total);
+    orc_cell_list(pts, np, a, radius, &cellNmax, bins.data(), counts.data(), nullptr, 0);
+    std::vector<int> slots((size_t)total * cellNmax, -1);
+    orc_cell_list(pts, np, a, radius, &cellNmax, bins.data(), counts.data(), slots.data(), (long)total * cellNmax);
+    const int width = subGrid;
+    std::vector<int> mask;
+    for (int z = -width; z <= width; ++z)
+        for (int y = -width; y <= width; ++y)
+            for (int x = -width; x <= width; ++x) {
+                const int g[3] = {x, y, z};
+                double rmin = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    double t = h * (std::max(std::abs(g[d]) - 1., 0.0));
+                    rmin += t * t;
+                }
+                rmin = std::sqrt(rmin);
+                if (rmin < h * width + 1e-6) { mask.push_back(x); mask.push_back(y); mask.push_back(z); }
+            }
+    const int K = (int)mask.size() / 3;
+    int Nmax = nmaxIn;
+    bool recompute = true;
+    std::vector<unsigned> npp;
+    std::vector<int> idx;
+    std::vector<double> vec, dist;
+    while (recompute) {
+        recompute = false;
+        npp.assign(np, 0u);
+        idx.assign((size_t)np * Nmax, 0);
+        vec.assign((size_t)np * Nmax * 3, 0.0);
+        dist.assign((size_t)np * Nmax, 0.0);
+        int nmax = Nmax;
+        for (int pp = 0; pp < np; ++pp) {
+            const double* t = pts + 3 * pp;
+            int c[3];
+            for (int d = 0; d < 3; ++d) c[d] = std::max(0, std::min(nside - 1, (int)std::floor((t[d] + radius) / h)));
+            for (int cc = 0; cc < K; ++cc) {
+                int nb[3];
+                for (int d = 0; d < 3; ++d) {
+                    nb[d] = (c[d] + mask[3 * cc + d]) % nside;
+                    if (nb[d] < 0) nb[d] += nside;
+                }
+                const long cell = nb[0] + (long)nb[1] * nside + (long)nb[2] * nside * nside;
+                for (unsigned p1 = 0; p1 < counts[cell]; ++p1) {
+                    const int j = slots[(size_t)cell * cellNmax + p1];
+                    if (j == pp) continue;
+                    double disp[3];
+                    for (int d = 0; d < 3; ++d) {
+                        disp[d] = t[d] - pts[3 * j + d];
+                        while (disp[d] < -radius) disp[d] += 2. * radius;
+                        while (disp[d] > radius) disp[d] -= 2. * radius;
+                    }
+                    double dd = 0.0;
+                    dd += disp[0] * disp[0]; dd += disp[1] * disp[1]; dd += disp[2] * disp[2];
+                    const double r = std::sqrt(dd);
+                    if (r >= range) continue;
+                    const int off = (int)npp[pp];
+                    if (off < Nmax && !recompute) {
+                        const size_t at = (size_t)pp * Nmax + off;
+                        idx[at] = j;
+                        for (int d = 0; d < 3; ++d) vec[3 * at + d] = disp[d];
+                        dist[at] = r;
+                    } else {
+                        nmax = std::max(nmax, off + 1);
+                        Nmax = nmax;
+                        recompute = true;
+                    }
+                    npp[pp] += 1;
+                }
+            }
+        }
+    }
+    if ((long)np * Nmax > capacity) return -Nmax;
+    std::memcpy(nppOut, npp.data(), sizeof(unsigned) * np);
+    std::memcpy(idxOut, idx.data(), sizeof(int) * idx.size());
+    std::memcpy(vecOut, vec.data(), sizeof(double) * vec.size());
+    std::memcpy(distOut, dist.data(), sizeof(double) * dist.size());
+    return Nmax;
+}
+
 }  // extern "C"

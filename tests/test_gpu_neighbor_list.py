@@ -1,0 +1,70 @@
+"""Neighbour lists on the device (svm_neighbor_list_*) against the oracle's restatement of
+neighborList::computeCPU (src/utilities/neighborList.cpp:96-151): the width Nmax, every count,
+index, minimum-image displacement and distance, bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def svm(svm_lib):
+    if svm_lib.device_count() < 1:
+        pytest.fail("no CUDA device: the GPU tests need a GB300")
+    return svm_lib
+
+
+def _same(nl, ref):
+    nm, npp, idx, vec, dist = ref
+    assert nl.Nmax == nm
+    assert np.array_equal(nl.neighborsPerParticle, npp)
+    assert np.array_equal(nl.particleIndices, idx)
+    assert np.array_equal(nl.neighborVectors, vec)
+    assert np.array_equal(nl.neighborDistances, dist)
+
+
+@pytest.mark.parametrize("sub_grid", [1, 2])
+def test_model_vertices_match_oracle(svm, sub_grid):
+    m = svm.sphericalVertexModel(6000, svm.noiseSource())
+    R = m.radius
+    nl = svm.neighborList(1.0, R + 2.5, sub_grid)
+    nl.computeNeighborLists(m)
+    ref = oracle.neighbor_list(m.returnPositions(), 1.0, R + 2.5, sub_grid)
+    _same(nl, ref)
+    assert nl.Nmax > 4 and nl.neighborsPerParticle.min() >= 1
+    # a second call reuses the grown width
+    nl.computeNeighborLists(m)
+    _same(nl, ref)
+    nl.close()
+
+
+def test_device_points_in_a_periodic_box_match_oracle(svm):
+    """Points filling the box, so that the minimum image crosses its faces."""
+    import torch
+    rng = np.random.default_rng(12)
+    radius = 6.0
+    pts = rng.uniform(-radius, radius * (1 - 1e-12), (5000, 3))
+    pts[:40, 0] = radius * (1 - 1e-9)        # on the +x face ...
+    pts[40:80, 0] = -radius                  # ... and on the -x face: neighbours through the boundary
+    dev = torch.from_numpy(pts.copy()).cuda()
+    for sub_grid, rng_ in ((1, 0.7), (2, 0.7), (3, 1.3)):
+        nl = svm.neighborList(rng_, radius, sub_grid)
+        nl.computeNeighborLists(dev)
+        ref = oracle.neighbor_list(pts, rng_, radius, sub_grid)
+        _same(nl, ref)
+        wrapped = np.abs(nl.neighborVectors[:80, :, 0]).max()
+        assert wrapped < rng_  # the displacement is the minimum image, not the raw difference
+        nl.close()
+
+
+def test_mixed_precision_model_is_listed_from_its_float_positions(svm):
+    m = svm.sphericalVertexModel(3000, svm.noiseSource())
+    m.precision = "mixed"
+    R = m.radius
+    nl = svm.neighborList(1.0, R + 2.5, 1)
+    nl.computeNeighborLists(m)
+    ref = oracle.neighbor_list(m.returnPositions().astype(np.float32).astype(np.float64), 1.0, R + 2.5, 1)
+    _same(nl, ref)
+    nl.close()

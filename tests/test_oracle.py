@@ -214,3 +214,24 @@ def test_vector_form_forces_match_reference(oracle_mod, gold):
         fd = -(en[0] - en[1]) / 2e-6
         assert abs(f[w] @ e - fd) <= abs(fref[w] @ e - fd) + 1e-7 * fmax
     om.set_positions(pos)
+
+
+@ref_only
+def test_neighbor_list_against_reference(oracle_mod):
+    """orc_neighbor_list against the reference's neighborList::computeCPU: the model's vertices
+    with the model's parameters (range 1, radius R + 2.5), and points filling a periodic box so
+    that minimum images cross its faces; Nmax grows from 4 through the recompute loop."""
+    ref = oracle_mod.RefModel(400, 11)
+    R = ref.radius
+    cases = [(ref.positions(), 1.0, R + 2.5, 1), (ref.positions(), 1.0, R + 2.5, 2)]
+    rng = np.random.default_rng(3)
+    box = rng.uniform(-4.0, 4.0 * (1 - 1e-12), (1500, 3))
+    box[:30, 0] = 4.0 * (1 - 1e-9)
+    box[30:60, 0] = -4.0
+    cases += [(box, 0.7, 4.0, 1), (box, 0.7, 4.0, 2), (box, 1.3, 4.0, 3)]
+    for pts, rng_, radius, sub in cases:
+        a = oracle_mod.neighbor_list(pts, rng_, radius, sub)
+        b = oracle_mod.neighbor_list(pts, rng_, radius, sub, reference=True)
+        assert a[0] == b[0] and a[0] > 4, (rng_, sub)
+        for x, y in zip(a[1:], b[1:]):
+            assert np.array_equal(x, y), (rng_, sub)
