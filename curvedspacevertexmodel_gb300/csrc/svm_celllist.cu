@@ -54,15 +54,20 @@ template <typename P>
 __global__ void k_cl_bin(P pts, int np, double r, double h, int n, int cap, int* __restrict__ binOf,
                          unsigned* __restrict__ counts, int* __restrict__ tmp, int* __restrict__ scalars) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= np) return;
-    double x, y, z;
-    pts(i, x, y, z);
-    const int b = bin_of(x, y, z, r, h, n, scalars + 3);
-    binOf[i] = b;
-    const unsigned s = atomicAdd(counts + b, 1u);
-    if ((int)s < cap) tmp[(long)b * cap + s] = i;
-    else atomicExch(scalars + 2, 1);
-    atomicMax(scalars, (int)s + 1);
+    int occ = 0;
+    if (i < np) {
+        double x, y, z;
+        pts(i, x, y, z);
+        const int b = bin_of(x, y, z, r, h, n, scalars + 3);
+        binOf[i] = b;
+        const unsigned s = atomicAdd(counts + b, 1u);
+        if ((int)s < cap) tmp[(long)b * cap + s] = i;
+        else atomicExch(scalars + 2, 1);
+        occ = (int)s + 1;
+    }
+    // one atomic per warp: a per-point atomic on this one word serialises in L2
+    occ = __reduce_max_sync(0xffffffffu, occ);
+    if ((threadIdx.x & 31) == 0 && occ > 0) atomicMax(scalars, occ);
 }
 
 __global__ void k_cl_order(const int* __restrict__ binOf, const unsigned* __restrict__ counts,
@@ -112,60 +117,192 @@ int compute(svm_cell_list* cl, P pts, int np) {
     k_cl_nmax<<<1, 1, 0, cl->stream>>>(cl->scalars);
     return check_launch();
 }
+
+// A bin took more points than it has slots: give every bin `cap` slots, as the reference's cell
+// list widens its Nmax and bins again (hyperrectangularCellList.cpp:165-214).  The counts of the
+// overflowing call stay valid for the next call's incremental clear.
+int cl_grow(svm_cell_list* cl, int cap) {
+    if (cudaStreamSynchronize(cl->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    cudaFree(cl->tmp); cudaFree(cl->slots);
+    cl->tmp = nullptr; cl->slots = nullptr;
+    if (cudaMalloc(&cl->tmp, sizeof(int) * cl->total * cap) != cudaSuccess ||
+        cudaMalloc(&cl->slots, sizeof(int) * cl->total * cap) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    cl->cap = cap;
+    return SVM_OK;
+}
 // neighborList (src/utilities/neighborList.cpp:6-18, 96-151; kernels neighborList.cu:108-357): per
 // point, over the adjacent bins of its (clamped) bin in the mask's order and each bin's points in
 // slot order, every other point whose minimum-image displacement (periodic box of side 2 radius,
 // periodicBoundaryConditions.h:124-132) is shorter than `range`; the first nmax are stored, the
-// count is kept whole (the host grows nmax and recomputes when a count exceeds it).  range2Hi is
-// an upper bound of range^2: a candidate with dd above it has sqrt(dd) > range, so its correctly
-// rounded root is >= range too and the root need not be taken (sqrt is monotone and range is a
-// double); every other candidate is decided by the reference's own test on the rounded root.
+// rest of each row is zero, and the count is kept whole (the host grows nmax and recomputes when a
+// count exceeds it).
+//
+// FP64 issues at a sixty-fourth of the FP32 rate here, so a candidate is first classified in FP32
+// and only neighbours (and the rare borderline candidate) see FP64:
+//   phase 1, a thread per point: scan the candidates with FP32 copies of the positions.  With E
+//     a bound on |d32 - d64| per component (coordinates within the grid, |x| <= radius, rounded
+//     to FP32 and subtracted: E = radius 2^-21 covers both roundings with a factor of two), a
+//     candidate whose |d32| components all stay below radius - 2E cannot wrap in FP64, and then
+//       dd32 > thrHi (> ((range + 2E)(1 + 2^-20))^2)  => |d64| > range      => not a neighbour
+//       dd32 < thrLo (< ((range - 2E)(1 - 2^-20))^2)  => |d64| < range      => a neighbour
+//     (dd32's own rounding is below 3 2^-24 relative, inside the 2^-20 factors).  Any other
+//     candidate takes the reference's FP64 test in place.  Neighbours are queued in order in
+//     shared memory (kNlQueue per thread; the scan resumes where it stopped when a queue fills).
+//   phase 2, the warp: the queued neighbours of its 32 points are dealt over the lanes, and each
+//     lane computes one neighbour's displacement, squared length and root in FP64 exactly as the
+//     reference does, and stores them at the owner's next row position.
+// The minimum-image loops run at most kWrapIters times: points inside the grid need one, and a
+// point outside it is an error the host reports (the cell list's flag).
+constexpr int kNlQueue = 16;
+constexpr int kWrapIters = 8;
+constexpr unsigned kNlWrapped = 0x80000000u;  // queue flag: the displacement wrapped
+
+struct NlParams {
+    int np, cap, nside, K, nmax;
+    double h, radius, range, range2Hi;
+    float wrapLim, thrLo, thrHi;
+};
+
+__device__ __forceinline__ bool min_image(double& d, double radius) {
+    bool w = false;
+    for (int i = 0; i < kWrapIters && d < -radius; ++i) { d += 2. * radius; w = true; }
+    for (int i = 0; i < kWrapIters && d > radius; ++i) { d -= 2. * radius; w = true; }
+    return w;
+}
+
 template <typename P>
-__global__ void k_nl(P pts, int np, const unsigned* __restrict__ counts, const int* __restrict__ slots, int cap,
-                     int nside, double h, double radius, double range, double range2Hi,
-                     const int* __restrict__ mask, int K,
-                     int nmax, unsigned* __restrict__ npp, int* __restrict__ idx, double* __restrict__ vec,
-                     double* __restrict__ dist, int* __restrict__ maxCount) {
-    const int pp = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pp >= np) return;
-    double t[3];
-    pts(pp, t[0], t[1], t[2]);
-    int c[3];
-    for (int d = 0; d < 3; ++d) c[d] = max(0, min(nside - 1, (int)floor((t[d] + radius) / h)));
-    int count = 0;
-    for (int cc = 0; cc < K; ++cc) {
+__global__ void k_nl_pack(P pts, int np, float4* __restrict__ p32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    double x, y, z;
+    pts(i, x, y, z);
+    p32[i] = make_float4((float)x, (float)y, (float)z, 0.f);
+}
+
+template <typename P>
+__global__ void __launch_bounds__(kB, 6) k_nl(P pts, const float4* __restrict__ p32, NlParams prm,
+                                          const unsigned* __restrict__ counts, const int* __restrict__ slots,
+                                          const int* __restrict__ mask, unsigned* __restrict__ npp,
+                                          int* __restrict__ idx, double* __restrict__ vec,
+                                          double* __restrict__ dist, int* __restrict__ maxCount) {
+    __shared__ unsigned queue[kNlQueue * kB];
+    const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+    const int pp = blockIdx.x * kB + threadIdx.x;
+    const bool active = pp < prm.np;
+    float t32[3] = {0.f, 0.f, 0.f};
+    int c[3] = {0, 0, 0};
+    if (active) {
+        double t[3];
+        pts(pp, t[0], t[1], t[2]);
+        const float4 f = p32[pp];
+        t32[0] = f.x; t32[1] = f.y; t32[2] = f.z;
+        for (int d = 0; d < 3; ++d) c[d] = max(0, min(prm.nside - 1, (int)floor((t[d] + prm.radius) / prm.h)));
+    }
+    auto cell_at = [&](int k) {
         int nb[3];
         for (int d = 0; d < 3; ++d) {
-            nb[d] = (c[d] + mask[3 * cc + d]) % nside;
-            if (nb[d] < 0) nb[d] += nside;
+            nb[d] = (c[d] + mask[3 * k + d]) % prm.nside;
+            if (nb[d] < 0) nb[d] += prm.nside;
         }
-        const long cell = nb[0] + (long)nb[1] * nside + (long)nb[2] * nside * nside;
-        const int n = min((int)counts[cell], cap);
-        for (int p1 = 0; p1 < n; ++p1) {
-            const int j = slots[cell * cap + p1];
+        return nb[0] + (long)nb[1] * prm.nside + (long)nb[2] * prm.nside * prm.nside;
+    };
+    // the next bin's count is loaded one bin ahead, off the scan's dependent-load chain
+    int cc = 0, p1 = 0, n = 0, count = 0, stored = 0;
+    long cell = 0, cellNext = 0;
+    unsigned nNext = 0;
+    if (active) { cellNext = cell_at(0); nNext = counts[cellNext]; }
+    bool more = active;
+    while (__any_sync(0xffffffffu, more)) {
+        int nq = 0;
+        // ---- phase 1: queue up to kNlQueue neighbours of this thread's point, in scan order
+        while (more && nq < kNlQueue) {
+            if (p1 >= n) {
+                if (cc >= prm.K) { more = false; break; }
+                cell = cellNext;
+                n = min((int)nNext, prm.cap);
+                p1 = 0;
+                if (++cc < prm.K) { cellNext = cell_at(cc); nNext = counts[cellNext]; }
+                continue;
+            }
+            const int j = slots[cell * prm.cap + p1];
+            ++p1;
             if (j == pp) continue;
-            double q[3], disp[3];
-            pts(j, q[0], q[1], q[2]);
-            for (int d = 0; d < 3; ++d) {
-                disp[d] = t[d] - q[d];
-                while (disp[d] < -radius) disp[d] += 2. * radius;
-                while (disp[d] > radius) disp[d] -= 2. * radius;
+            const float4 q = p32[j];
+            const float d0 = t32[0] - q.x, d1 = t32[1] - q.y, d2 = t32[2] - q.z;
+            int verdict = 0;  // 1 neighbour, -1 not, 0 decide in FP64
+            if (fabsf(d0) <= prm.wrapLim && fabsf(d1) <= prm.wrapLim && fabsf(d2) <= prm.wrapLim) {
+                const float dd32 = d0 * d0 + d1 * d1 + d2 * d2;
+                verdict = dd32 > prm.thrHi ? -1 : (dd32 < prm.thrLo ? 1 : 0);
             }
-            const double dd = disp[0] * disp[0] + disp[1] * disp[1] + disp[2] * disp[2];
-            if (dd > range2Hi) continue;  // sqrt(dd) > range: the rounded root is >= range as well
-            const double r = sqrt(dd);
-            if (r >= range) continue;
-            if (count < nmax) {
-                const long at = (long)pp * nmax + count;
-                idx[at] = j;
-                vec[3 * at] = disp[0]; vec[3 * at + 1] = disp[1]; vec[3 * at + 2] = disp[2];
-                dist[at] = r;
+            unsigned entry = (unsigned)j;
+            if (verdict == 0) {  // the reference's test, in FP64 (rare: the point is reloaded)
+                double t[3], qd[3], disp[3];
+                pts(pp, t[0], t[1], t[2]);
+                pts(j, qd[0], qd[1], qd[2]);
+                bool w = false;
+                for (int d = 0; d < 3; ++d) {
+                    disp[d] = t[d] - qd[d];
+                    w |= min_image(disp[d], prm.radius);
+                }
+                const double dd = disp[0] * disp[0] + disp[1] * disp[1] + disp[2] * disp[2];
+                verdict = (dd > prm.range2Hi || sqrt(dd) >= prm.range) ? -1 : 1;
+                if (w) entry |= kNlWrapped;
             }
+            if (verdict < 0) continue;
+            if (count < prm.nmax) queue[nq++ * kB + threadIdx.x] = entry;
             ++count;
         }
+        // ---- phase 2: the warp's queued neighbours over its lanes, in FP64
+        int incl = nq;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int excl = incl - nq, total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int base = 0; base < total; base += 32) {
+            const int g = base + lane;
+            int owner = 0;  // the last lane whose queue starts at or before g
+            for (int step = 16; step > 0; step >>= 1) {
+                const int e = __shfl_sync(0xffffffffu, excl, owner + step);
+                if (e <= g) owner += step;
+            }
+            const int k = g - __shfl_sync(0xffffffffu, excl, owner);
+            const int row = __shfl_sync(0xffffffffu, stored, owner) + k;
+            if (g < total) {
+                const unsigned entry = queue[k * kB + wbase + owner];
+                const int j = (int)(entry & ~kNlWrapped);
+                const int po = blockIdx.x * kB + wbase + owner;
+                double a[3], b[3], disp[3];
+                pts(po, a[0], a[1], a[2]);
+                pts(j, b[0], b[1], b[2]);
+                for (int d = 0; d < 3; ++d) disp[d] = a[d] - b[d];
+                if (entry & kNlWrapped)
+                    for (int d = 0; d < 3; ++d) min_image(disp[d], prm.radius);
+                const double dd = disp[0] * disp[0] + disp[1] * disp[1] + disp[2] * disp[2];
+                const long at = (long)po * prm.nmax + row;
+                idx[at] = j;
+                vec[3 * at] = disp[0]; vec[3 * at + 1] = disp[1]; vec[3 * at + 2] = disp[2];
+                dist[at] = sqrt(dd);
+            }
+        }
+        stored += nq;
     }
-    npp[pp] = (unsigned)count;
-    atomicMax(maxCount, count);
+    // ---- the rest of each row is zero (resetNeighbors), written a row at a time by the warp
+    for (int o = 0; o < 32; ++o) {
+        const int s = __shfl_sync(0xffffffffu, stored, o);
+        const int po = blockIdx.x * kB + wbase + o;
+        if (po >= prm.np) break;
+        for (int k = s + lane; k < prm.nmax; k += 32) {
+            const long at = (long)po * prm.nmax + k;
+            idx[at] = 0;
+            vec[3 * at] = 0.; vec[3 * at + 1] = 0.; vec[3 * at + 2] = 0.;
+            dist[at] = 0.;
+        }
+    }
+    if (active) npp[pp] = (unsigned)count;
+    count = __reduce_max_sync(0xffffffffu, count);  // one atomic per warp on the shared word
+    if (lane == 0 && count > 0) atomicMax(maxCount, count);
 }
 }  // namespace
 
@@ -179,6 +316,7 @@ struct svm_neighbor_list {
     double* vec = nullptr;              // [nPoints * nmax * 3]
     double* dist = nullptr;             // [nPoints * nmax]
     int* maxCount = nullptr;
+    float4* p32 = nullptr;              // [nPoints] FP32 copies for the candidate scan
 };
 
 namespace {
@@ -192,26 +330,43 @@ int nl_alloc(svm_neighbor_list* nl) {
     return SVM_OK;
 }
 
+// The scan's FP32 thresholds for points within [-radius, radius]^3, rounded outward.
+void nl_thresholds(NlParams& p) {
+    const double E = p.radius * 0x1p-21;
+    auto down = [](double v) { float f = (float)v; if ((double)f > v) f = std::nextafter(f, -INFINITY); return f; };
+    auto up = [](double v) { float f = (float)v; if ((double)f < v) f = std::nextafter(f, INFINITY); return f; };
+    p.wrapLim = p.radius > 2 * E ? down(p.radius - 2 * E) : -1.f;
+    const double hi = (p.range + 2 * E) * (1 + 0x1p-20), lo = (p.range - 2 * E) * (1 - 0x1p-20);
+    p.thrHi = up(hi * hi);
+    p.thrLo = lo > 0 ? down(lo * lo) : -1.f;
+}
+
 template <typename P>
 int nl_compute(svm_neighbor_list* nl, P pts, int np) {
     if (np != nl->nPoints) return SVM_ERR_ARG;
     svm_cell_list* cl = nl->cl;
     const size_t nb = (np + kB - 1) / kB;
-    for (int pass = 0; pass < 64; ++pass) {   // a second pass at most: the first finds the largest count
-        const size_t e = (size_t)np * nl->nmax;
-        cudaMemsetAsync(nl->idx, 0, sizeof(int) * e, cl->stream);   // resetNeighbors: zero past each count
-        cudaMemsetAsync(nl->vec, 0, sizeof(double) * 3 * e, cl->stream);
-        cudaMemsetAsync(nl->dist, 0, sizeof(double) * e, cl->stream);
+    k_nl_pack<<<nb, kB, 0, cl->stream>>>(pts, np, nl->p32);
+    for (int pass = 0; pass < 64; ++pass) {   // a third pass at most: slots widened, then nmax grown
+        NlParams prm;
+        prm.np = np; prm.cap = cl->cap; prm.nside = cl->nside; prm.K = nl->K; prm.nmax = nl->nmax;
+        prm.h = cl->h; prm.radius = cl->radius; prm.range = nl->range;
+        prm.range2Hi = nl->range * nl->range * (1.0 + 0x1p-48);
+        nl_thresholds(prm);
         cudaMemsetAsync(nl->maxCount, 0, sizeof(int), cl->stream);
-        k_nl<<<nb, kB, 0, cl->stream>>>(pts, np, cl->counts, cl->slots, cl->cap, cl->nside, cl->h, cl->radius, nl->range,
-                                        nl->range * nl->range * (1.0 + 0x1p-48), nl->mask, nl->K, nl->nmax, nl->npp, nl->idx, nl->vec, nl->dist, nl->maxCount);
+        k_nl<<<nb, kB, 0, cl->stream>>>(pts, nl->p32, prm, cl->counts, cl->slots, nl->mask, nl->npp, nl->idx, nl->vec,
+                                        nl->dist, nl->maxCount);
         if (check_launch()) return SVM_ERR_CUDA;
         int mc = 0, sc[4];
         if (cudaMemcpyAsync(&mc, nl->maxCount, sizeof(int), cudaMemcpyDeviceToHost, cl->stream) != cudaSuccess ||
             cudaMemcpyAsync(sc, cl->scalars, sizeof(sc), cudaMemcpyDeviceToHost, cl->stream) != cudaSuccess ||
             cudaStreamSynchronize(cl->stream) != cudaSuccess)
             return SVM_ERR_CUDA;
-        if (sc[2] || sc[3]) return SVM_ERR_DEVICE;  // the cell list overflowed a bin or lost a point
+        if (sc[3]) return SVM_ERR_DEVICE;  // a point lay outside the grid (or was not finite)
+        if (sc[2]) {                       // a bin overflowed its slots: widen them, bin again
+            if (cl_grow(cl, sc[0]) || compute(cl, pts, np)) return SVM_ERR_CUDA;
+            continue;
+        }
         if (mc <= nl->nmax) return SVM_OK;
         nl->nmax = mc;  // grow-only, then recompute
         if (nl_alloc(nl)) return SVM_ERR_CUDA;
@@ -249,7 +404,8 @@ int svm_neighbor_list_create(double range, double radius, int subGridReduction, 
     nl->K = (int)mask.size() / 3;
     bool ok = cudaMalloc(&nl->mask, sizeof(int) * mask.size()) == cudaSuccess &&
               cudaMalloc(&nl->npp, sizeof(unsigned) * nPoints) == cudaSuccess &&
-              cudaMalloc(&nl->maxCount, sizeof(int)) == cudaSuccess && nl_alloc(nl) == SVM_OK;
+              cudaMalloc(&nl->maxCount, sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&nl->p32, sizeof(float4) * nPoints) == cudaSuccess && nl_alloc(nl) == SVM_OK;
     if (ok) ok = cudaMemcpy(nl->mask, mask.data(), sizeof(int) * mask.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     if (!ok) { svm_neighbor_list_destroy(nl); return SVM_ERR_CUDA; }
     *out = nl;
@@ -259,7 +415,7 @@ int svm_neighbor_list_create(double range, double radius, int subGridReduction, 
 int svm_neighbor_list_destroy(svm_neighbor_list* nl) {
     if (!nl) return SVM_ERR_ARG;
     if (nl->cl) svm_cell_list_destroy(nl->cl);
-    void* ptrs[] = {nl->mask, nl->npp, nl->idx, nl->vec, nl->dist, nl->maxCount};
+    void* ptrs[] = {nl->mask, nl->npp, nl->idx, nl->vec, nl->dist, nl->maxCount, nl->p32};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete nl;
     return SVM_OK;
