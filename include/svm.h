@@ -290,10 +290,13 @@ int svm_cell_list_bins(svm_cell_list* cl, int* binOfPoint);
 /* ---- neighbour list ------------------------------------------------------------------------
  * neighborList (src/utilities/neighborList.{h,cpp}; the spherical model builds it with range 1 and
  * radius R + 2.5, sphericalModel.cpp:21): a cell list of grid size range / subGridReduction over
- * [-radius, radius]^3 (slotCapacity points per bin at most), then per point every other point at
+ * [-radius, radius]^3 (slotCapacity slots per bin to start with; a bin that overflows them widens
+ * every bin, as the reference's cell list grows its Nmax), then per point every other point at
  * minimum-image distance below `range` in a periodic box of side 2 radius, listed in the order of
  * the adjacent bins (computeAdjacentCells) and of each bin's slots.  Nmax starts at 4 and grows to
- * the largest count (the list is recomputed then). */
+ * the largest count (the list is recomputed then).  Points must lie in [-radius, radius)^3: one
+ * outside (or not finite) returns SVM_ERR_DEVICE.  Replaces neighborList::computeNeighborLists
+ * (neighborList.h:17-28) and its launcher gpu_compute_neighbor_list (neighborList.cuh). */
 typedef struct svm_neighbor_list svm_neighbor_list;
 int svm_neighbor_list_create(double range, double radius, int subGridReduction, int nPoints, int slotCapacity,
                              void* stream, svm_neighbor_list** out);
