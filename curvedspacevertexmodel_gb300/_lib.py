@@ -61,6 +61,7 @@ SIGNATURES = {
     "svm_random_cell_centres": (i32, [i32, i32, dp]),
     "svm_random_vertex_directors": (i32, [i32, i32, dp, i32, dp]),
     "svm_topology_from_points": (i32, [dp, i32, pvp]),
+    "svm_topology_from_points_gpu": (i32, [dp, i32, vp, pvp]),
     "svm_topology_from_triangles": (i32, [dp, i32, ip, i32, pvp]),
     "svm_topology_sizes": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
     "svm_topology_get": (i32, [vp, dp, ip, i32, up, ip, ip]),

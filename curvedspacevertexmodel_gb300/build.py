@@ -30,8 +30,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # where the area fallback is taken every step, which the CPU-rounding build does not), so every
 # product and sum rounds as the CPU does.
 FMA_SOURCES: set = set()
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-I" + INCLUDE, "-I" + CSRC]
+# The host code of the .cu files goes to gcc through nvcc: -ffp-contract=off keeps it from fusing
+# a*b+c on aarch64 (gcc's default there), where the host-side sums (e.g. a centre's radius for the
+# vertex positions) would otherwise round differently from the same expressions in the .cpp files.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
 
@@ -97,7 +100,7 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
     exe = os.path.join(PKG, "sphericalVertex_gpu")
     src = os.path.join(host, "sphericalVertex_gpu.cpp")
     if _needs(exe, [src, os.path.join(host, "svm.hpp"), LIB]):
-        run([shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + host, src, "-o", exe,
+        run([shutil.which("g++") or "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, "-I" + host, src, "-o", exe,
              "-L" + PKG, "-lsvm", "-Wl,-rpath,$ORIGIN"])
     return LIB
 

@@ -375,6 +375,24 @@ int nl_compute(svm_neighbor_list* nl, P pts, int np) {
 }
 }  // namespace
 
+namespace svm {
+int cell_list_bin(svm_cell_list* cl, const double* pts, int n, CellGrid* view) {
+    if (!cl || !pts || !view || n != cl->nPoints) return SVM_ERR_ARG;
+    for (int pass = 0; pass < 8; ++pass) {
+        if (compute(cl, AosPoints{pts}, n)) return SVM_ERR_CUDA;
+        int sc[4];
+        if (cudaMemcpyAsync(sc, cl->scalars, sizeof(sc), cudaMemcpyDeviceToHost, cl->stream) != cudaSuccess ||
+            cudaStreamSynchronize(cl->stream) != cudaSuccess)
+            return SVM_ERR_CUDA;
+        if (sc[3]) return SVM_ERR_DEVICE;
+        if (sc[2]) { if (cl_grow(cl, sc[0])) return SVM_ERR_CUDA; continue; }
+        *view = CellGrid{cl->counts, cl->slots, cl->cap, cl->nside, cl->h, cl->radius};
+        return SVM_OK;
+    }
+    return SVM_ERR_DEVICE;
+}
+}  // namespace svm
+
 extern "C" {
 
 int svm_neighbor_list_create(double range, double radius, int subGridReduction, int nPoints, int slotCapacity,

@@ -48,3 +48,6 @@ bool topologyFromTriangles(const double* points, int n, const std::vector<int>& 
                            Topology& topo);
 
 }  // namespace svm
+
+// The C ABI's topology handle (svm_topology_*), filled by the host hull or the device hull.
+struct svm_topology { svm::Topology t; };

@@ -413,6 +413,17 @@ int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
 int launch_t1_apply(svm_model* m, int bump);
 int check_launch();
+// A binned view of device points (svm_celllist.cu): per-bin counts and slots (ascending point
+// index), grid side nside and bin side h over [-radius, radius]^3.
+struct CellGrid {
+    const unsigned* counts;
+    const int* slots;
+    int cap, nside;
+    double h, radius;
+};
+// Bins the points (AoS double[3n] on the device), widening the slots until no bin overflows;
+// synchronises.  SVM_ERR_DEVICE when a point lies outside the grid.
+int cell_list_bin(svm_cell_list* cl, const double* pointsDevice, int n, CellGrid* view);
 void fire_detach(svm_fire* F);          // svm_fire.cu: the model is going away
 int model_alloc(int nCells, int nVertices, int Wc, const double* radius, int nRep, void* stream, svm_model** out);
 // replicas (svm_batch.cu)

@@ -1880,8 +1880,6 @@ int svm_device_count(int* count) {
     return n > 0 ? SVM_OK : SVM_ERR_NO_DEVICE;
 }
 
-struct svm_topology { svm::Topology t; };
-
 int svm_topology_from_points(const double* pts, int n, svm_topology** out) {
     if (!pts || n < 4 || !out) return SVM_ERR_ARG;
     std::vector<int> tris;

@@ -50,7 +50,7 @@ class sphericalVertexModel {
         std::vector<double> centres(3 * (size_t)n);
         check(svm_random_cell_centres(noise.RNGSeed, n, centres.data()), "svm_random_cell_centres");
         svm_topology* t = nullptr;
-        check(svm_topology_from_points(centres.data(), n, &t), "svm_topology_from_points");
+        check(svm_topology_from_points_gpu(centres.data(), n, nullptr, &t), "svm_topology_from_points_gpu");
         int nc = 0, nv = 0, maxRing = 0;
         svm_topology_sizes(t, &nc, &nv, &maxRing);
         nVertices = nv;
@@ -173,7 +173,7 @@ class sphericalVertexModelBatch : private detail::BatchTopoHolder, public spheri
             std::vector<double> centres(3 * (size_t)n[r]);
             check(svm_random_cell_centres(seeds[r], n[r], centres.data()), "svm_random_cell_centres");
             svm_topology* t = nullptr;
-            check(svm_topology_from_points(centres.data(), n[r], &t), "svm_topology_from_points");
+            check(svm_topology_from_points_gpu(centres.data(), n[r], nullptr, &t), "svm_topology_from_points_gpu");
             int nc = 0, nv = 0, mr = 0;
             svm_topology_sizes(t, &nc, &nv, &mr);
             One o{std::vector<double>(3 * (size_t)nv), std::vector<int>((size_t)nc * mr), std::vector<int>(3 * (size_t)nv),

@@ -36,11 +36,15 @@ class Topology:
         t.radius = float(np.linalg.norm(t.vertexPositions[0]))
         return t
 
-    def __init__(self, centres: np.ndarray, triangles: np.ndarray | None = None):
+    def __init__(self, centres: np.ndarray, triangles: np.ndarray | None = None, device: bool = False):
+        """The hull of `centres` on the host (svm_topology_from_points), on the device
+        (device=True, svm_topology_from_points_gpu: the same arrays), or the given triangles."""
         pts = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1)
         n = pts.size // 3
         h = C.c_void_p()
-        if triangles is None:
+        if triangles is None and device:
+            call("svm_topology_from_points_gpu", pts, n, None, C.byref(h))
+        elif triangles is None:
             call("svm_topology_from_points", pts, n, C.byref(h))
         else:
             tri = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1)
@@ -110,7 +114,7 @@ class sphericalVertexModel:
         self.noise = noise or noiseSource(True)
         if topology is None:
             centres = random_cell_centres(self.noise.RNGSeed, self.nCells)
-            topology = Topology(centres)
+            topology = Topology(centres, device=True)
         self.topology = topology
         self.nVertices = topology.nVertices
         self.radius = math.sqrt(self.nCells / (4.0 * PI)) if radius is None else float(radius)
@@ -340,7 +344,7 @@ class sphericalVertexModelBatch(sphericalVertexModel):
         nCells = [int(n) for n in nCells]
         R = len(nCells)
         if topologies is None:
-            topologies = [Topology(random_cell_centres(int(sd), n)) for n, sd in zip(nCells, seeds)]
+            topologies = [Topology(random_cell_centres(int(sd), n), device=True) for n, sd in zip(nCells, seeds)]
         self.topologies = topologies
         self.nReplicas = R
         self.radii = np.array([math.sqrt(n / (4.0 * PI)) for n in nCells])

@@ -74,6 +74,11 @@ int svm_random_vertex_directors(int seed, int nCells, const double* vertexPos, i
  * normalised facet centroid, CCW vertex->cell / vertex->vertex slots, clockwise cell rings. */
 typedef struct svm_topology svm_topology;
 int svm_topology_from_points(const double* cellCentres, int nCells, svm_topology** out);
+/* The same topology computed on the device (cell centres: HOST double[3*nCells]): per-centre
+ * stars of the hull by gift wrapping over cell-list candidates, certified by their circumcaps,
+ * checked for consistency, then numbered and assembled exactly as svm_topology_from_points does.
+ * Replaces convexHullCGALInterface::sphericalConvexHullForVertexModel (convexHullCGAL.cpp:82-186). */
+int svm_topology_from_points_gpu(const double* cellCentres, int nCells, void* stream, svm_topology** out);
 /* Same contract from caller-supplied hull triangles (CCW seen from outside, int[3*nTri]). */
 int svm_topology_from_triangles(const double* cellCentres, int nCells, const int* triangles, int nTriangles,
                                 svm_topology** out);
