@@ -108,12 +108,27 @@ __device__ bool cap_within(const double* p, const double* q, const double* s, do
     return diameter * (1.0 + 1e-9) < reach;
 }
 
+// The plane of (p, q, s) for the pivot's FP32 sign test: n = b x c with b = q - p, c = s - p in
+// FP32, and the coefficients of the filter's permanent (|b1 c2| + |b2 c1|, ...).
+struct Plane32 { float n[3], k[3]; };
+__device__ __forceinline__ Plane32 plane32(const float* b, const float* c) {
+    Plane32 t;
+    t.n[0] = b[1] * c[2] - b[2] * c[1]; t.n[1] = b[2] * c[0] - b[0] * c[2]; t.n[2] = b[0] * c[1] - b[1] * c[0];
+    t.k[0] = fabsf(b[1] * c[2]) + fabsf(b[2] * c[1]);
+    t.k[1] = fabsf(b[2] * c[0]) + fabsf(b[0] * c[2]);
+    t.k[2] = fabsf(b[0] * c[1]) + fabsf(b[1] * c[0]);
+    return t;
+}
+
 __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P, int n, CellGrid g,
                                                   int* __restrict__ deg, int* __restrict__ star,
                                                   int* __restrict__ err) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
+    // candidates and their offsets from p, fl32(x - p) of the FP64 difference (relative error
+    // within 2^-24 (1 + 2^-29) per component)
     int cand[kMaxCand];
+    float dv[kMaxCand][3];
     int st[kMaxDeg];
     double pp[3];
     load3(P, p, pp);
@@ -126,8 +141,9 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
             lo[d] = max(0, c[d] - w); hi[d] = min(g.nside - 1, c[d] + w);
             whole &= lo[d] == 0 && hi[d] == g.nside - 1;
         }
-        int nc = 0;
+        int nc = 0, iq0 = -1;
         bool overflow = false;
+        double best = 0.0;
         for (int z = lo[2]; z <= hi[2]; ++z)
             for (int y = lo[1]; y <= hi[1]; ++y)
                 for (int x = lo[0]; x <= hi[0]; ++x) {
@@ -136,42 +152,49 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
                     for (int k = 0; k < m; ++k) {
                         const int j = g.slots[cell * g.cap + k];
                         if (j == p) continue;
-                        if (nc < kMaxCand) cand[nc++] = j;
-                        else overflow = true;
+                        if (nc >= kMaxCand) { overflow = true; continue; }
+                        double xx[3];
+                        load3(P, j, xx);
+                        const double dx = xx[0] - pp[0], dy = xx[1] - pp[1], dz = xx[2] - pp[2];
+                        const double d2 = dx * dx + dy * dy + dz * dz;  // the nearest, lowest index on ties
+                        if (iq0 < 0 || d2 < best || (d2 == best && j < cand[iq0])) { best = d2; iq0 = nc; }
+                        cand[nc] = j;
+                        dv[nc][0] = (float)dx; dv[nc][1] = (float)dy; dv[nc][2] = (float)dz;
+                        ++nc;
                     }
                 }
         if (overflow) break;
         if (nc < 3) { if (whole) break; continue; }
-        // the nearest candidate (lowest index on ties)
-        int q0 = -1;
-        double best = 0.0;
-        for (int i = 0; i < nc; ++i) {
-            double x[3];
-            load3(P, cand[i], x);
-            const double dx = x[0] - pp[0], dy = x[1] - pp[1], dz = x[2] - pp[2];
-            const double d2 = dx * dx + dy * dy + dz * dz;
-            if (q0 < 0 || d2 < best || (d2 == best && cand[i] < q0)) { best = d2; q0 = cand[i]; }
-        }
-        // gift wrapping around p
-        int d = 0, q = q0;
+        // gift wrapping around p from the edge to the nearest candidate.  The pivot's sign test
+        // runs in FP32 with the plane hoisted out of the candidate loop: with every input within
+        // 2^-24 relative, |det32 - det| <= 8 2^-24 perm, so |det32| > 1e-5 perm32 fixes the sign;
+        // anything closer (or so small that FP32 could underflow) takes the FP64 test.
+        int d = 0, iq = iq0;
         bool ok = true;
         do {
             if (d >= kMaxDeg) { ok = false; break; }
-            st[d++] = q;
-            double qq[3];
-            load3(P, q, qq);
-            int s = -1;
-            double ss[3];
+            st[d++] = cand[iq];
+            const float b[3] = {dv[iq][0], dv[iq][1], dv[iq][2]};
+            int is = -1;
+            Plane32 pl;
             for (int i = 0; i < nc; ++i) {
-                const int x = cand[i];
-                if (x == q) continue;
-                double xx[3];
-                load3(P, x, xx);
-                if (s < 0 || orient(pp, qq, ss, xx) > 0.0) { s = x; ss[0] = xx[0]; ss[1] = xx[1]; ss[2] = xx[2]; }
+                if (i == iq) continue;
+                if (is < 0) { is = i; pl = plane32(b, dv[i]); continue; }
+                const float det = pl.n[0] * dv[i][0] + pl.n[1] * dv[i][1] + pl.n[2] * dv[i][2];
+                const float perm = pl.k[0] * fabsf(dv[i][0]) + pl.k[1] * fabsf(dv[i][1]) + pl.k[2] * fabsf(dv[i][2]);
+                bool above;
+                if (perm > 1e-30f && fabsf(det) > 1e-5f * perm) {
+                    above = det > 0.f;
+                } else {
+                    double qq[3], ss[3], xx[3];
+                    load3(P, cand[iq], qq); load3(P, cand[is], ss); load3(P, cand[i], xx);
+                    above = orient(pp, qq, ss, xx) > 0.0;
+                }
+                if (above) { is = i; pl = plane32(b, dv[i]); }
             }
-            if (s < 0) { ok = false; break; }
-            q = s;
-        } while (q != q0);
+            if (is < 0) { ok = false; break; }
+            iq = is;
+        } while (iq != iq0);
         if (ok && d < 3) ok = false;
         if (ok && !whole) {
             const double reach = w * g.h;
