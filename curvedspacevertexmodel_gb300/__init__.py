@@ -13,6 +13,7 @@ from .model import (  # noqa: F401
     random_cell_centres,
     random_vertex_directors,
     sphericalSelfPropelledParticle,
+    sphericalVectorialVicsek,
     sphericalVertexModel,
     sphericalVertexModelBatch,
     warmStartNetwork,
@@ -22,7 +23,7 @@ from .trajectory import dynamicalFeatures, logSpacedIntegers, run_trajectory, ve
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
     "energyMinimizerFIRE", "neighborList", "noiseSource", "random_cell_centres", "random_vertex_directors",
-    "sphericalSelfPropelledParticle", "sphericalVertexModel",
+    "sphericalSelfPropelledParticle", "sphericalVectorialVicsek", "sphericalVertexModel",
     "sphericalVertexModelBatch", "warmStartNetwork", "dynamicalFeatures", "logSpacedIntegers", "run_trajectory",
     "vectorValueNetCDF",
 ]

@@ -118,6 +118,7 @@ SIGNATURES = {
     "svm_model_set_directors": (i32, [vp, dp]),
     "svm_model_get_directors": (i32, [vp, dp]),
     "svm_spp_step": (i32, [vp, f64, f64, f64, f64, i32, dp, u64]),
+    "svm_vicsek_step": (i32, [vp, f64, f64, f64, f64, f64, i32, dp, u64]),
     "svm_brownian_step_io": (i32, [vp, f64, f64, f64, u64, dp, dp, C.POINTER(f64)]),
     "svm_brownian_run": (i32, [vp, f64, f64, f64, u64, i32]),
     "svm_fire_create": (i32, [vp, f64, f64, f64, f64, f64, f64, i32, f64, f64, i32, pvp]),

@@ -35,10 +35,12 @@ extern "C" int svm_random_cell_centres(int seed, int n, double* out) {
     return SVM_OK;
 }
 
-// The vertex model's random directors (sphericalVertexModel.cpp:58-70): the model's noise source
-// continues after the cell centres and the cell model's own director draws (sphericalModel.cpp:
-// 37-63, 4 nCells uniforms), two uniforms per vertex give a random unit vector, projected onto the
-// tangent plane at the vertex and normalised (sphericalDomain.h:173-177).
+// The vertex model's random directors, made as sphericalVertexModel.cpp:58-70 makes them: two
+// uniforms per vertex give a random unit vector, projected onto the tangent plane at the vertex and
+// normalised (sphericalDomain.h:173-177).  The draws continue the seeded stream after the cell
+// centres and the cell model's own director draws (sphericalModel.cpp:37-63, 4 nCells uniforms);
+// the reference uses the model's own default noise source instead, which random_device seeds
+// (noiseSource.h:21-30), so only the distribution is the reference's.
 extern "C" int svm_random_vertex_directors(int seed, int nCells, const double* vertexPos, int nV, double* out) {
     if (nCells < 4 || nV < 1 || !vertexPos || !out) return SVM_ERR_ARG;
     std::mt19937 gen(13377);

@@ -322,6 +322,7 @@ struct svm_model {
     double4_32a* vsph = nullptr;
     double* vnorm = nullptr;           // |p| per vertex, from the last corner pass (FP64 form)
     double4_32a* dir = nullptr;        // directors (self-propelled updater; single spheres only)
+    double4_32a* dirTarget = nullptr;  // the Vicsek updater's target directors (allocated on first use)
     double4_32a* cellRef = nullptr;    // reference cell positions of the dynamical observables
     double4_32a* edgeC = nullptr;      // per owned edge slot 3v+j (v < u): p_v x p_u and its norm
     double* edgeArc = nullptr;         // and the arc (FP64 corner pass; single spheres only)

@@ -1657,6 +1657,66 @@ __global__ void k_spp_dirs(const double4_32a* __restrict__ pos, double4_32a* __r
                    __dadd_rn(__dadd_rn(__dmul_rn(c, n.z), __dmul_rn(sn, cp.z)), __dmul_rn(w, p.z))});
 }
 
+// ---- vectorial Vicsek alignment (sphericalVectorialVicsek::integrateEOMCPU,
+// src/updaters/sphericalVectorialVicsek.cpp:5-60) on the vertex model's directors ------------------
+// After the self-propelled move and its T1 flips, from the directors before this update: a random
+// unit vector (u, w: phi = 2 pi u, theta = acos(2 w - 1)) projected onto the tangent plane at the
+// vertex and normalised; the target (n_v + the three vertex neighbours' n) / 4 + eta point,
+// projected and normalised.  u, w injected (r[2v], r[2v + 1]) or from Philox counter word 4.
+template <int kNoise>
+__global__ void k_vicsek_target(const double4_32a* __restrict__ pos, const double4_32a* __restrict__ dir,
+                                const int4* __restrict__ vnbr, double4_32a* __restrict__ target,
+                                const double* __restrict__ r, uint64_t seed,
+                                const unsigned long long* __restrict__ stepCounter, double eta, int nV) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    double u, w;
+    if (kNoise == SVM_NOISE_BUFFER) {
+        u = r[2 * v]; w = r[2 * v + 1];
+    } else {
+        const unsigned long long step = *stepCounter;
+        const uint4 q = philox4x32_10(make_uint4((unsigned)v, (unsigned)step, (unsigned)(step >> 32), 4u),
+                                      make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+        u = u53(q.x, q.y); w = u53(q.z, q.w);
+    }
+    const D3 p = ld3(pos, v);
+    const double phi = __dmul_rn(2.0 * 3.141592653589793, u), theta = acos(__dsub_rn(__dmul_rn(2.0, w), 1.0));
+    const double st = sin(theta);
+    D3 sp{__dmul_rn(st, cos(phi)), __dmul_rn(st, sin(phi)), cos(theta)};
+    const double ps = __ddiv_rn(dot3(sp, p), dot3(p, p));
+    sp = D3{__dsub_rn(sp.x, __dmul_rn(ps, p.x)), __dsub_rn(sp.y, __dmul_rn(ps, p.y)), __dsub_rn(sp.z, __dmul_rn(ps, p.z))};
+    const double is = 1.0 / sqrt(dot3(sp, sp));
+    sp = D3{__dmul_rn(sp.x, is), __dmul_rn(sp.y, is), __dmul_rn(sp.z, is)};
+    const int4 nb = vnbr[v];
+    D3 t = ld3(dir, v);
+    const int nbs[3] = {nb.x, nb.y, nb.z};
+    for (int k = 0; k < 3; ++k) {
+        const D3 o = ld3(dir, nbs[k]);
+        t = D3{__dadd_rn(t.x, o.x), __dadd_rn(t.y, o.y), __dadd_rn(t.z, o.z)};
+    }
+    const double mi = 1.0 / 4.0;  // self plus three neighbours
+    t = D3{__dadd_rn(__dmul_rn(t.x, mi), __dmul_rn(sp.x, eta)), __dadd_rn(__dmul_rn(t.y, mi), __dmul_rn(sp.y, eta)),
+           __dadd_rn(__dmul_rn(t.z, mi), __dmul_rn(sp.z, eta))};
+    const double ts = __ddiv_rn(dot3(t, p), dot3(p, p));
+    t = D3{__dsub_rn(t.x, __dmul_rn(ts, p.x)), __dsub_rn(t.y, __dmul_rn(ts, p.y)), __dsub_rn(t.z, __dmul_rn(ts, p.z))};
+    const double it = 1.0 / sqrt(dot3(t, t));
+    st3(target, v, D3{__dmul_rn(t.x, it), __dmul_rn(t.y, it), __dmul_rn(t.z, it)});
+}
+// n += (dt / tau)(target - n), projected onto the tangent plane and normalised.
+__global__ void k_vicsek_update(const double4_32a* __restrict__ pos, double4_32a* __restrict__ dir,
+                                const double4_32a* __restrict__ target, double rate, int nV) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const D3 p = ld3(pos, v), t = ld3(target, v);
+    D3 n = ld3(dir, v);
+    n = D3{__dadd_rn(n.x, __dmul_rn(rate, __dsub_rn(t.x, n.x))), __dadd_rn(n.y, __dmul_rn(rate, __dsub_rn(t.y, n.y))),
+           __dadd_rn(n.z, __dmul_rn(rate, __dsub_rn(t.z, n.z)))};
+    const double s = __ddiv_rn(dot3(n, p), dot3(p, p));
+    n = D3{__dsub_rn(n.x, __dmul_rn(s, p.x)), __dsub_rn(n.y, __dmul_rn(s, p.y)), __dsub_rn(n.z, __dmul_rn(s, p.z))};
+    const double inv = 1.0 / sqrt(dot3(n, n));
+    st3(dir, v, D3{__dmul_rn(n.x, inv), __dmul_rn(n.y, inv), __dmul_rn(n.z, inv)});
+}
+
 // ---- launch helpers --------------------------------------------------------------------------
 static ApplyArgs apply_args(svm_model* m, int bump) {
     ApplyArgs A;
@@ -2043,7 +2103,7 @@ int svm_model_destroy(svm_model* m) {
     if (!m) return SVM_ERR_ARG;
     if (m->stream) cudaStreamSynchronize(m->stream);
     for (svm_fire* F : m->fires) svm::fire_detach(F);
-    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->dir, m->cellRef, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
+    void* ptrs[] = {m->pos[0], m->pos[1], m->vsph, m->vnorm, m->dir, m->dirTarget, m->cellRef, m->edgeC, m->edgeArc, m->vcell, m->vnbr, m->vlast, m->vnext, m->vrpos, m->ring,
                     m->ringCount, m->corner, m->cellPos, m->cellSph, m->ap, m->pref, m->force, m->vel, m->noiseBuf,
                     m->dispBuf, m->partials, m->ticket, m->scalars, m->fallbackFlag, m->status, m->stepCounter,
                     m->t1.bits, m->t1.summary, m->t1.count, m->t1.flipLog, m->t1.flipCount, m->t1.touched,
@@ -2586,6 +2646,33 @@ int svm_spp_step(svm_model* m, double dt, double mu, double v0, double tau, int 
     else
         k_spp_dirs<SVM_NOISE_PHILOX><<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
             m->pos[m->cur], m->dir, nullptr, seed, m->stepCounter, amp, m->nVertices);
+    return svm::check_launch();
+}
+
+int svm_vicsek_step(svm_model* m, double dt, double mu, double v0, double eta, double tau, int noiseMode,
+                    const double* uniforms, uint64_t seed) {
+    if (!m || !m->dir || m->nRep > 1 || m->precision == SVM_PRECISION_MIXED || !(tau != 0.0)) return SVM_ERR_ARG;
+    if (noiseMode == SVM_NOISE_BUFFER && !uniforms) return SVM_ERR_ARG;
+    if (!m->dirTarget) SVM_CUDA(cudaMalloc(&m->dirTarget, m->nVertices * sizeof(double4_32a)));
+    if (noiseMode == SVM_NOISE_BUFFER)
+        SVM_CUDA(cudaMemcpyAsync(m->noiseBuf, uniforms, sizeof(double) * 2 * m->nVertices, cudaMemcpyHostToDevice,
+                                 m->stream));
+    int rc = svm::launch_geometry(m);
+    if (rc || (rc = svm::launch_force_fp64(m))) return rc;
+    k_spp_move<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->dir, m->force, dt, mu,
+                                                                            v0, m->nVertices, m->R);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    m->cornersValid = false;
+    if ((rc = svm::launch_corners(m, !m->restricted)) || (rc = svm::launch_t1_apply(m, 1))) return rc;
+    if (noiseMode == SVM_NOISE_BUFFER)
+        k_vicsek_target<SVM_NOISE_BUFFER><<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
+            m->pos[m->cur], m->dir, m->vnbr, m->dirTarget, m->noiseBuf, seed, m->stepCounter, eta, m->nVertices);
+    else
+        k_vicsek_target<SVM_NOISE_PHILOX><<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(
+            m->pos[m->cur], m->dir, m->vnbr, m->dirTarget, nullptr, seed, m->stepCounter, eta, m->nVertices);
+    if (svm::check_launch()) return SVM_ERR_CUDA;
+    k_vicsek_update<<<svm::blocksFor(m->nVertices), svm::kBlock, 0, m->stream>>>(m->pos[m->cur], m->dir, m->dirTarget,
+                                                                                 dt / tau, m->nVertices);
     return svm::check_launch();
 }
 

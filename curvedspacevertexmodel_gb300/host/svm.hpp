@@ -70,7 +70,7 @@ class sphericalVertexModel {
         setT1Threshold(0.1);  // sphericalVertexModel.cpp:13
         setPreferredParameters(a0, p0);
         setScalarModelParameter(1.0);
-        std::vector<double> dirs(3 * (size_t)nv);  // sphericalVertexModel.cpp:58-70
+        std::vector<double> dirs(3 * (size_t)nv);  // made as sphericalVertexModel.cpp:58-70, seeded
         check(svm_random_vertex_directors(noise.RNGSeed, n, vp.data(), nv, dirs.data()), "svm_random_vertex_directors");
         check(svm_model_set_directors(h, dirs.data()), "svm_model_set_directors");
         computeGeometry();

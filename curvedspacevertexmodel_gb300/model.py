@@ -77,8 +77,11 @@ def random_cell_centres(seed: int, n: int) -> np.ndarray:
 
 
 def random_vertex_directors(seed: int, n_cells: int, vertex_positions: np.ndarray) -> np.ndarray:
-    """The reference vertex model's initial directors for these vertex positions (the seeded
-    stream continued after the cell centres; sphericalVertexModel.cpp:58-70)."""
+    """Initial directors for these vertex positions: the construction of sphericalVertexModel.cpp:
+    58-70 (a uniform random unit vector projected onto the tangent plane and normalised), drawn
+    from the seeded stream after the cell centres and the cell model's directors.  The reference
+    draws them from the model's own default noise source, which random_device seeds
+    (noiseSource.h:21-30), so its directors do not repeat between runs; these do."""
     p = np.ascontiguousarray(vertex_positions, dtype=np.float64).reshape(-1)
     out = np.empty_like(p)
     call("svm_random_vertex_directors", int(seed), int(n_cells), p, p.size // 3, out)
@@ -487,6 +490,37 @@ class sphericalSelfPropelledParticle:
     def run(self, nSteps: int):
         for _ in range(int(nSteps)):
             self.integrateEquationOfMotion()
+
+
+class sphericalVectorialVicsek(sphericalSelfPropelledParticle):
+    """Vicsek alignment of the vertices' directors (src/updaters/sphericalVectorialVicsek.{h,cpp},
+    parameters of vectorialVicsek.h:11-44, defaults mu 1, Eta 1, tau 1, v0 0.01): the self-propelled
+    move, then each director relaxes at rate dt / tau towards the normalised tangent average of
+    itself and its three vertex neighbours plus Eta times a random tangent unit vector.  The
+    reference runs it on the CPU only; here the step runs on the device."""
+
+    def __init__(self, reproducible: bool = True):
+        super().__init__(reproducible)
+        self.v0 = 0.01
+        self.Eta = 1.0
+
+    def setEta(self, eta: float):
+        self.Eta = float(eta)
+
+    def injectNoise(self, uw: np.ndarray | None):
+        """Uniform draws in [0, 1), (u, w) for each vertex in vertex order, for the next step only."""
+        self._injected = None if uw is None else np.ascontiguousarray(uw, dtype=np.float64).reshape(-1)
+
+    def integrateEquationOfMotion(self):
+        m = self.model
+        seed = self.noise.RNGSeed if self.noise.RNGSeed >= 0 else 1337
+        if self._injected is not None:
+            call("svm_vicsek_step", m.handle, self.deltaT, self.mu, self.v0, self.Eta, self.tau,
+                 _lib.SVM_NOISE_BUFFER, self._injected, seed)
+            self._injected = None
+        else:
+            call("svm_vicsek_step", m.handle, self.deltaT, self.mu, self.v0, self.Eta, self.tau,
+                 _lib.SVM_NOISE_PHILOX, None, seed)
 
 
 class brownianDynamics:

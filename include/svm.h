@@ -63,9 +63,11 @@ int svm_device_count(int* count);
  * then scaled to R = sqrt(n / 4 pi) (sphericalVertexModel.cpp:12).  seed < 0 keeps the default
  * engine seed 13377 (src/utilities/noiseSource.h:24).  out: double[3n]. */
 int svm_random_cell_centres(int seed, int n, double* out);
-/* The reference vertex model's initial directors (one unit tangent vector per vertex, drawn from
- * the same seeded stream after the cell centres; sphericalVertexModel.cpp:58-70) for the given
- * vertex positions: out[3 nV]. */
+/* Initial directors for the given vertex positions (one unit tangent vector per vertex, made as
+ * sphericalVertexModel.cpp:58-70 makes them) drawn from the seeded stream after the cell centres
+ * and the cell model's directors: out[3 nV].  The reference draws them from the model's own
+ * default noise source, seeded by random_device (noiseSource.h:21-30), so its directors do not
+ * repeat between runs; these do, with the same distribution. */
 int svm_random_vertex_directors(int seed, int nCells, const double* vertexPos, int nV, double* out);
 
 /* ---- initial topology (host) ------------------------------------------------------------
@@ -196,6 +198,16 @@ int svm_model_get_directors(svm_model* m, double* dirs);
  * (host), SVM_NOISE_PHILOX draws them in-kernel from (seed, step counter, vertex). */
 int svm_spp_step(svm_model* m, double dt, double mu, double v0, double tau, int noiseMode, const double* uniforms,
                  uint64_t seed);
+/* One step of sphericalVectorialVicsek (src/updaters/sphericalVectorialVicsek.cpp:5-60) on the
+ * vertex model, whose neighbours are each vertex's three vertex neighbours: forces, the
+ * self-propelled move dt (v0 n + mu F) with its T1 flips, then per vertex the target
+ * (n + neighbours' n) / 4 + eta xi (xi a random unit vector projected onto the tangent plane and
+ * normalised), projected and normalised, and n += (dt / tau)(target - n), projected and
+ * normalised.  noiseMode SVM_NOISE_BUFFER: `uniforms` = HOST double[2 nV], (u, w) per vertex in
+ * [0, 1) as the reference draws them; SVM_NOISE_PHILOX: in-kernel draws (seed, step).  FP64 form,
+ * single spheres. */
+int svm_vicsek_step(svm_model* m, double dt, double mu, double v0, double eta, double tau, int noiseMode,
+                    const double* uniforms, uint64_t seed);
 /* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
  * z, unused) per vertex in the FP64 form, float4 in the mixed form.  Valid until the next step,
  * precision switch or svm_model_destroy. */

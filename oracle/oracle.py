@@ -77,6 +77,8 @@ def orc_lib():
         _sig(lib, "orc_get_directors", None, vp, _dp)
         _sig(lib, "orc_init_directors", None, vp, vp)
         _sig(lib, "orc_spp_step_noise", None, vp, _dp, C.c_double, C.c_double, C.c_double, C.c_double)
+        _sig(lib, "orc_vicsek_step_noise", None, vp, _dp, C.c_double, C.c_double, C.c_double, C.c_double,
+             C.c_double)
         _sig(lib, "orc_noise_uniforms", None, vp, C.c_double, C.c_double, _dp, C.c_long)
         _sig(lib, "orc_last_excess_area", C.c_double, vp)
         _sig(lib, "orc_fallback_count", C.c_int, vp)
@@ -182,6 +184,10 @@ class OracleModel:
 
     def spp_step_noise(self, r, dt, mu, v0, tau):
         self.lib.orc_spp_step_noise(self.h, np.ascontiguousarray(r, dtype=np.float64).reshape(-1), dt, mu, v0, tau)
+
+    def vicsek_step_noise(self, uw, dt, mu, v0, eta, tau):
+        self.lib.orc_vicsek_step_noise(self.h, np.ascontiguousarray(uw, dtype=np.float64).reshape(-1), dt, mu, v0,
+                                       eta, tau)
 
     def set_directors(self, d):
         self.lib.orc_set_directors(self.h, np.ascontiguousarray(d, dtype=np.float64).reshape(-1))
@@ -336,7 +342,9 @@ def ref_lib():
         _sig(lib, "ref_num_vertices", C.c_int, vp)
         _sig(lib, "ref_ring_width", C.c_int, vp)
         _sig(lib, "ref_radius", C.c_double, vp)
-        for n in ("positions", "forces", "velocities", "cell_positions", "area_perimeter"):
+        _sig(lib, "ref_active_setup", None, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+             C.c_double)
+        for n in ("positions", "forces", "velocities", "cell_positions", "area_perimeter", "directors"):
             _sig(lib, "ref_get_" + n, None, vp, _dp)
         _sig(lib, "ref_set_positions", None, vp, _dp)
         _sig(lib, "ref_get_rings", C.c_int, vp, _ip, C.c_int, _up)
@@ -374,6 +382,13 @@ class RefModel:
 
     def steps(self, n):
         self.lib.ref_steps(self.h, n)
+
+    def active_setup(self, kind, seed, dt, mu, v0, eta, tau):
+        """kind 0: sphericalSelfPropelledParticle, 1: sphericalVectorialVicsek (its noise seeded)."""
+        self.lib.ref_active_setup(self.h, kind, seed, dt, mu, v0, eta, tau)
+
+    def directors(self):
+        return self._vec("directors", self.nVertices)
 
     def set_restricted(self, r):
         self.lib.ref_set_restricted(self.h, int(bool(r)))

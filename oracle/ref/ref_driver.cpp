@@ -15,6 +15,8 @@
 #include "noiseSource.h"
 #include "hyperrectangularCellList.h"
 #include "neighborList.h"
+#include "sphericalSelfPropelledParticle.h"
+#include "sphericalVectorialVicsek.h"
 
 struct ref_handle {
     noiseSource initNoise{true};
@@ -22,6 +24,7 @@ struct ref_handle {
     std::shared_ptr<brownianDynamics> bd;
     std::shared_ptr<energyMinimizerFIRE> fire;
     std::shared_ptr<Simulation> sim;
+    std::shared_ptr<vectorialVicsek> active;   // the self-propelled or Vicsek updater
 };
 
 extern "C" {
@@ -49,6 +52,30 @@ void ref_bd_setup(ref_handle* h, int bdSeed, double T, double dt, double mu) {
     if (bdSeed >= 0) h->bd->noise.setReproducibleSeed(bdSeed);
     h->bd->setT(T);
     h->bd->mu = mu;
+}
+
+// An active updater on the model, as mainwindow.cpp:184-214 wires the self-propelled one:
+// kind 0 sphericalSelfPropelledParticle, 1 sphericalVectorialVicsek; the updater's own noise
+// seeded with `seed`.
+void ref_active_setup(ref_handle* h, int kind, int seed, double dt, double mu, double v0, double eta, double tau) {
+    if (kind == 0) h->active = std::make_shared<sphericalSelfPropelledParticle>();
+    else h->active = std::make_shared<sphericalVectorialVicsek>();
+    h->sim = std::make_shared<Simulation>();
+    h->sim->setConfiguration(h->model);
+    h->sim->addUpdater(h->active, h->model);
+    h->sim->setIntegrationTimestep(dt);
+    h->sim->setCPUOperation(true);
+    h->sim->setReproducible(true);
+    h->active->noise.setReproducibleSeed(seed);
+    h->active->setMu(mu);
+    h->active->setV0(v0);
+    h->active->setEta(eta);
+    h->active->setTau(tau);
+}
+void ref_get_directors(ref_handle* h, double* out) {
+    ArrayHandle<dVec> a(h->model->returnDirectors(), access_location::host, access_mode::read);
+    for (int i = 0; i < h->model->getNumberOfParticles(); ++i)
+        for (int d = 0; d < 3; ++d) out[3 * i + d] = a.data[i].x[d];
 }
 
 // minimization.cpp:251-262

@@ -17,6 +17,7 @@
 #include "brownianDynamics.cuh"
 #include "energyMinimizerFIRE.cuh"
 #include "velocityVerlet.cuh"
+#include "vectorialVicsek.cuh"
 
 [[noreturn]] static void offPath(const char* name) {
     std::fprintf(stderr, "reference CPU build: GPU launcher %s reached\n", name);
@@ -24,6 +25,9 @@
 }
 
 bool gpu_move_particles_on_sphere(dVec*, dVec*, sphericalDomain&, scalar, int) { offPath(__func__); }
+bool gpu_selfPropelledParticleDisplacement(dVec*, dVec*, dVec*, scalar, scalar, scalar, int) { offPath(__func__); }
+bool gpu_vectorVicsek_target_directors(dVec*, dVec*, unsigned int*, int*, curandState*, Index2D&, scalar, int) { offPath(__func__); }
+bool gpu_vectorVicsek_update_directors(dVec*, dVec*, scalar, scalar, int) { offPath(__func__); }
 bool gpu_spherical_vertex_model_geometry(dVec*, dVec*, int*, int*, unsigned int*, dVec*, dVec*, dVec*, unsigned int*, scalar2*, Index2D, Index2D, sphericalDomain&, int) { offPath(__func__); }
 bool gpu_quadratic_spherical_cellular_force(dVec*, dVec*, dVec*, int*, unsigned int*, dVec*, dVec*, dVec*, unsigned int*, scalar2*, scalar2*, Index2D, scalar, sphericalDomain&, int) { offPath(__func__); }
 bool gpu_vm_test_edges_for_T1(dVec*, int*, int*, int*, unsigned int*, int*, sphericalDomain&, scalar, int, int, int*, Index2D&) { offPath(__func__); }

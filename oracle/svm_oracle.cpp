@@ -571,8 +571,9 @@ void orc_get_directors(orc_model* m, double* out) {
     for (int i = 0; i < m->N; ++i)
         for (int d = 0; d < 3; ++d) out[3 * i + d] = m->dir[i].x[d];
 }
-// The vertex model's random directors (sphericalVertexModel.cpp:58-70), drawn from the noise source
-// that made the cell centres, after them.
+// The vertex model's random directors, made as sphericalVertexModel.cpp:58-70 makes them, drawn from
+// the noise source that made the cell centres, after them (the reference draws them from the
+// model's own random_device-seeded source; the library's seeded choice is restated here).
 void orc_init_directors(orc_model* m, orc_noise* nz) {
     for (int i = 0; i < m->N; ++i) {
         double u2 = orc_noise_uniform(nz, 0., 1.), v2 = orc_noise_uniform(nz, 0., 1.);
@@ -599,6 +600,46 @@ void orc_spp_step_noise(orc_model* m, const double* r, double dt, double mu, dou
         V3 nd = m->dir[i];
         rodrigues(nd, m->pos[i], theta);
         m->dir[i] = nd;
+    }
+}
+// sphericalVectorialVicsek::integrateEOMCPU (src/updaters/sphericalVectorialVicsek.cpp:5-60) on the
+// vertex model, whose neighbours (numberOfNeighbors, neighbors) are the three vertex neighbours:
+// forces; disp = dt (v0 n + mu F); move (with T1 unless restricted); then, from the directors before
+// the update, per vertex a random unit vector (u, w: phi = 2 pi u, theta = acos(2w - 1)) projected
+// onto the tangent plane at the vertex's new position and normalised, the target
+// (n + neighbours' n) * (1/4) + point * eta projected and normalised; then each director
+// n += (dt/tau)(target - n), projected onto the tangent plane and normalised.  uw: the caller's
+// 2 Nv uniform draws in [0, 1), (u, w) per vertex in vertex order.
+void orc_vicsek_step_noise(orc_model* m, const double* uw, double dt, double mu, double v0, double eta, double tau) {
+    orc_compute_forces(m);
+    std::vector<double> disp(3 * (size_t)m->N);
+    for (int i = 0; i < m->N; ++i)
+        for (int d = 0; d < 3; ++d) disp[3 * i + d] = dt * (v0 * m->dir[i].x[d] + mu * m->forces[i].x[d]);
+    orc_move(m, disp.data(), 1.0);
+    std::vector<V3> target(m->N);
+    for (int i = 0; i < m->N; ++i) {
+        const V3& p = m->pos[i];
+        const double u = uw[2 * i], w = uw[2 * i + 1];
+        const double phi = 2.0 * kPI * u, theta = std::acos(2.0 * w - 1);
+        V3 sp = v3(1.0 * std::sin(theta) * std::cos(phi), 1.0 * std::sin(theta) * std::sin(phi), 1.0 * std::cos(theta));
+        const double s = dot(sp, p) / dot(p, p);
+        sp = sub(sp, scale(s, p));
+        sp = scale(1.0 / norm(sp), sp);
+        V3 nd = m->dir[i];
+        int cnt = 3;
+        for (int jj = 0; jj < cnt; ++jj) nd = add(nd, m->dir[m->vn[3 * i + jj]]);
+        cnt += 1;
+        const double mi = 1.0 / cnt;
+        nd = add(scale(mi, nd), scale(eta, sp));
+        projectNormalize(nd, p);
+        target[i] = nd;
+    }
+    for (int i = 0; i < m->N; ++i) {
+        const V3& p = m->pos[i];
+        V3 n = add(m->dir[i], scale(dt / tau, sub(target[i], m->dir[i])));
+        const double s = dot(n, p) / dot(p, p);
+        n = sub(n, scale(s, p));
+        m->dir[i] = scale(1.0 / norm(n), n);
     }
 }
 // Uniform draws getRealUniform(lo, hi) (noiseSource.cpp:18-27), count of them.

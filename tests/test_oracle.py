@@ -235,3 +235,37 @@ def test_neighbor_list_against_reference(oracle_mod):
         assert a[0] == b[0] and a[0] > 4, (rng_, sub)
         for x, y in zip(a[1:], b[1:]):
             assert np.array_equal(x, y), (rng_, sub)
+
+
+@ref_only
+@pytest.mark.parametrize("kind", [0, 1])
+def test_active_updaters_against_reference(oracle_mod, kind):
+    """orc_spp_step_noise (kind 0) and orc_vicsek_step_noise (kind 1) against the reference's
+    sphericalSelfPropelledParticle and sphericalVectorialVicsek driving its vertex model: the
+    oracle fed the same mt19937 uniforms the reference's updater draws, 300 steps with T1 flips,
+    positions and directors equal bit for bit after every step."""
+    n, seed = 120, 7
+    ref = oracle_mod.RefModel(n, seed, 1.0, 3.8, 1.0, 0.04)
+    topo = ref.topology()
+    m = oracle_mod.OracleModel(topo["pos"], topo["rings"], topo["counts"], topo["vcells"], topo["vnbrs"], topo["radius"])
+    m.set_preferred(1.0, 3.8)
+    m.set_t1_threshold(0.04)
+    d0 = ref.directors()  # the reference's come from a random_device-seeded source: start from them
+    p = ref.positions()
+    assert np.abs(np.sum(d0 * p, axis=1)).max() < 1e-12 and np.abs(np.linalg.norm(d0, axis=1) - 1).max() < 1e-14
+    m.set_directors(d0)
+    dt, mu, v0, eta, tau = 0.01, 1.0, 0.3, 0.5, 0.7
+    ref.active_setup(kind, 55, dt, mu, v0, eta, tau)
+    draws = oracle_mod.OracleNoise(55)
+    nv = ref.nVertices
+    flips = 0
+    for step in range(300):
+        ref.steps(1)
+        if kind == 0:
+            m.spp_step_noise(draws.uniforms(nv, -0.5, 0.5), dt, mu, v0, tau)
+        else:
+            m.vicsek_step_noise(draws.uniforms(2 * nv, 0.0, 1.0), dt, mu, v0, eta, tau)
+        flips += len(m.flips())
+        assert np.array_equal(ref.positions(), m.positions()), step
+        assert np.array_equal(ref.directors(), m.directors()), step
+    assert flips > 0

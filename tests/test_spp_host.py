@@ -1,5 +1,5 @@
 """Host side of the self-propelled updater: the model's initial directors follow the reference
-vertex model's seeded stream (sphericalVertexModel.cpp:58-70) bit for bit against the oracle, and
+construction of sphericalVertexModel.cpp:58-70 on the seeded stream bit for bit against the oracle, and
 are unit tangent vectors."""
 import numpy as np
 
