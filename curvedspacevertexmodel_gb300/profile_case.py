@@ -11,7 +11,10 @@ a batch of R replicas runs instead (stabilisation, then `steps` steps at per-rep
 with --fire K the `steps` Brownian steps are followed by K FIRE iterations (energyMinimizerFIRE,
 the reference's default parameters, force tolerance 1e-12 so that all K run); with --neighbors K
 the vertices' neighbour list (range 1, radius R + 2.5, the model's own) is then computed K times
-and the mean time of a computation (device lists, Nmax read back) is printed.
+and the mean time of a computation (device lists, Nmax read back) is printed; with --active K,
+K self-propelled steps (v0 0.1, tau 1, in-kernel draws) and then K Vicsek steps (Eta 0.5) are
+timed, and with --dynamics K, K evaluations of the MSD and overlap against the starting cell
+positions (each reading its two numbers back).
 """
 from __future__ import annotations
 
@@ -36,6 +39,8 @@ def main():
     ap.add_argument("--fire", type=int, default=0, help="FIRE iterations after the Brownian steps")
     ap.add_argument("--neighbors", type=int, default=0, help="neighbour-list computations after the steps")
     ap.add_argument("--sub-grid", type=int, default=1, help="the neighbour list's subGridReduction")
+    ap.add_argument("--active", type=int, default=0, help="timed self-propelled and Vicsek steps")
+    ap.add_argument("--dynamics", type=int, default=0, help="timed MSD + overlap evaluations")
     args = ap.parse_args()
     t0 = time.time()
     if args.replicas:
@@ -82,6 +87,29 @@ def main():
         fire.setMaximumIterations(args.fire)
         fire.setForceCutoff(1e-12)
         fire.minimize()
+    if args.dynamics:
+        dyn = svm.dynamicalFeatures(m)
+        dyn._both(0.5)
+        t1 = time.perf_counter()
+        for _ in range(args.dynamics):
+            msd, ov = dyn._both(0.5)
+        dt = (time.perf_counter() - t1) / args.dynamics
+        print(f"dynamics: {m.nCells} cells, msd {msd:.4g} overlap {ov:.4g}, {dt * 1e3:.3f} ms per evaluation")
+    if args.active:
+        for name, upd in (("self-propelled", svm.sphericalSelfPropelledParticle()),
+                          ("Vicsek", svm.sphericalVectorialVicsek())):
+            upd.setModel(m)
+            upd.setDeltaT(0.01)
+            upd.setV0(0.1)
+            if name == "Vicsek":
+                upd.setEta(0.5)
+            upd.integrateEquationOfMotion()
+            m.deviceStatus()
+            t1 = time.perf_counter()
+            upd.run(args.active)
+            st = m.deviceStatus()
+            dt = (time.perf_counter() - t1) / args.active
+            print(f"{name} step: {m.nVertices} vertices, {dt * 1e3:.3f} ms per step, status {st}")
     if args.neighbors:
         nl = svm.neighborList(1.0, m.radius + 2.5, args.sub_grid)
         nl.computeNeighborLists(m, fetch=False)  # sizes the lists
