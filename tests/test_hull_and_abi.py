@@ -158,6 +158,20 @@ def test_abi_rejects_bad_arguments_without_a_device(svm):
     assert L.svm_model_set_t1_blocks(None, 0) == ERR_ARG
     assert L.svm_brownian_step_io(None, 0.0, 0.01, 1.0, 1, None, None, None) == ERR_ARG
     assert L.svm_energy_noalloc(None, None, 1.0, 10, None, None) == ERR_ARG
+    three = np.zeros(9)
+    assert L.svm_topology_from_points_gpu(three, 3, None, C.byref(h)) == ERR_ARG  # N < 4
+    for bad in ((0.0, 5.0, 1, 10, 16), (1.0, -1.0, 1, 10, 16), (1.0, 5.0, 0, 10, 16), (1.0, 5.0, 1, 0, 16)):
+        rng_, rad, sub, npts, cap = bad
+        assert L.svm_neighbor_list_create(C.c_double(rng_), C.c_double(rad), sub, npts, cap, None,
+                                          C.byref(h)) == ERR_ARG, bad
+    for fn in ("svm_neighbor_list_destroy",):
+        assert getattr(L, fn)(None) == ERR_ARG, fn
+    assert L.svm_neighbor_list_compute(None, None, 10) == ERR_ARG
+    assert L.svm_neighbor_list_compute_model(None, None) == ERR_ARG
+    assert L.svm_vicsek_step(None, C.c_double(0.01), C.c_double(1.0), C.c_double(0.1), C.c_double(0.5),
+                             C.c_double(1.0), 1, None, C.c_uint64(1)) == ERR_ARG
+    assert L.svm_spp_step(None, C.c_double(0.01), C.c_double(1.0), C.c_double(0.1), C.c_double(1.0), 1, None,
+                          C.c_uint64(1)) == ERR_ARG
     cnt = C.c_int()
     assert L.svm_mlp_parameter_count(C.byref(cnt)) == 0 and cnt.value == 24 * 64 + 64 + 64 * 64 + 64 + 2 * 64 + 2
     assert L.svm_status_string(ERR_ARG) and L.svm_status_string(999)
