@@ -16,7 +16,8 @@
 //                 hemisphere) lies within 2 rho of p, rho the triangle's circumradius, so when
 //                 2 rho < w h every point that could lie in the cap was a candidate and the
 //                 triangle is a hull facet.  A star with an uncertified triangle is computed
-//                 again with w + 1.  A closed cycle of hull facets around p is p's whole star.
+//                 again with w + 1 (in a second launch over the centres that need it).  A closed
+//                 cycle of hull facets around p is p's whole star.
 //   k_hull_check  every triangle of a star appears, rotated, in the stars of its other two corners
 //                 (the stars form one triangulated sphere), and counts the triangles whose
 //                 smallest corner is the star's own point.
@@ -120,11 +121,17 @@ __device__ __forceinline__ Plane32 plane32(const float* b, const float* c) {
     return t;
 }
 
-__global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P, int n, CellGrid g,
+// Centres list[0..count) (all centres when list is null) with searches of wFirst..wLast bins.  A
+// centre whose stars all fail certification in that range is queued in retry (when given) for a
+// second launch with the wider searches, so that warps of the first launch do not wait on them.
+__global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P, const int* __restrict__ list,
+                                                  int count, int wFirst, int wLast, CellGrid g,
                                                   int* __restrict__ deg, int* __restrict__ star,
+                                                  int* __restrict__ retry, int* __restrict__ retryCount,
                                                   int* __restrict__ err) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int p = list ? list[t] : t;
     // candidates and their offsets from p, fl32(x - p) of the FP64 difference (relative error
     // within 2^-24 (1 + 2^-29) per component)
     int cand[kMaxCand];
@@ -134,7 +141,8 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
     load3(P, p, pp);
     int c[3];
     for (int d = 0; d < 3; ++d) c[d] = max(0, min(g.nside - 1, (int)floor((pp[d] + g.radius) / g.h)));
-    for (int w = 1; w <= kMaxW; ++w) {
+    bool hard = false;  // a failure no wider search can repair
+    for (int w = wFirst; w <= wLast; ++w) {
         int lo[3], hi[3];
         bool whole = true;
         for (int d = 0; d < 3; ++d) {
@@ -143,7 +151,7 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
         }
         int nc = 0, iq0 = -1;
         bool overflow = false;
-        double best = 0.0;
+        float b1 = INFINITY, b2 = INFINITY;
         for (int z = lo[2]; z <= hi[2]; ++z)
             for (int y = lo[1]; y <= hi[1]; ++y)
                 for (int x = lo[0]; x <= hi[0]; ++x) {
@@ -155,16 +163,30 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
                         if (nc >= kMaxCand) { overflow = true; continue; }
                         double xx[3];
                         load3(P, j, xx);
-                        const double dx = xx[0] - pp[0], dy = xx[1] - pp[1], dz = xx[2] - pp[2];
-                        const double d2 = dx * dx + dy * dy + dz * dz;  // the nearest, lowest index on ties
-                        if (iq0 < 0 || d2 < best || (d2 == best && j < cand[iq0])) { best = d2; iq0 = nc; }
                         cand[nc] = j;
-                        dv[nc][0] = (float)dx; dv[nc][1] = (float)dy; dv[nc][2] = (float)dz;
+                        dv[nc][0] = (float)(xx[0] - pp[0]);
+                        dv[nc][1] = (float)(xx[1] - pp[1]);
+                        dv[nc][2] = (float)(xx[2] - pp[2]);
+                        // the nearest in FP32 (squared length within 5 2^-24 relative of the exact one)
+                        const float d2 = dv[nc][0] * dv[nc][0] + dv[nc][1] * dv[nc][1] + dv[nc][2] * dv[nc][2];
+                        if (d2 < b1) { b2 = b1; b1 = d2; iq0 = nc; }
+                        else if (d2 < b2) b2 = d2;
                         ++nc;
                     }
                 }
-        if (overflow) break;
-        if (nc < 3) { if (whole) break; continue; }
+        if (overflow) { hard = true; break; }
+        if (nc < 3) { if (whole) { hard = true; break; } continue; }
+        if (!(b2 > b1 * (1.0f + 1e-5f))) {  // a near tie: the FP64 squared lengths, lowest index on ties
+            double best = 0.0;
+            iq0 = -1;
+            for (int i = 0; i < nc; ++i) {
+                double xx[3];
+                load3(P, cand[i], xx);
+                const double dx = xx[0] - pp[0], dy = xx[1] - pp[1], dz = xx[2] - pp[2];
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                if (iq0 < 0 || d2 < best || (d2 == best && cand[i] < cand[iq0])) { best = d2; iq0 = i; }
+            }
+        }
         // gift wrapping around p from the edge to the nearest candidate.  The pivot's sign test
         // runs in FP32 with the plane hoisted out of the candidate loop: with every input within
         // 2^-24 relative, |det32 - det| <= 8 2^-24 perm, so |det32| > 1e-5 perm32 fixes the sign;
@@ -210,9 +232,10 @@ __global__ void __launch_bounds__(kHB) k_hull_star(const double* __restrict__ P,
             for (int i = 0; i < d; ++i) star[(long)p * kMaxDeg + i] = st[i];
             return;
         }
-        if (whole) break;
+        if (whole) { hard = true; break; }
     }
     deg[p] = 0;
+    if (retry && !hard) { retry[atomicAdd(retryCount, 1)] = p; return; }
     atomicOr(err, 1);
 }
 
@@ -380,10 +403,11 @@ extern "C" int svm_topology_from_points_gpu(const double* pts, int n, void* stre
     int* deg = buf.get<int>(n);
     int* star = buf.get<int>((size_t)n * kMaxDeg);
     int* own = buf.get<int>((size_t)n + 1);
-    int* err = buf.get<int>(1);
-    if (!P || !deg || !star || !own || !err) return SVM_ERR_CUDA;
+    int* err = buf.get<int>(2);          // [0] error bits, [1] centres queued for the wider search
+    int* retry = buf.get<int>(n);
+    if (!P || !deg || !star || !own || !err || !retry) return SVM_ERR_CUDA;
     if (cudaMemcpyAsync(P, pts, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess || cudaMemsetAsync(own + n, 0, sizeof(int), s) != cudaSuccess ||
+        cudaMemsetAsync(err, 0, 2 * sizeof(int), s) != cudaSuccess || cudaMemsetAsync(own + n, 0, sizeof(int), s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)  // the cell list bins on a stream of its own
         return SVM_ERR_CUDA;
     // bins of side 2.5 mean spacings (a unit-density sphere has ~70 candidates at w = 1)
@@ -399,7 +423,15 @@ extern "C" int svm_topology_from_points_gpu(const double* pts, int n, void* stre
     CellGrid g;
     rc = cell_list_bin(cl, P, n, &g);
     if (!rc) {
-        k_hull_star<<<(n + kHB - 1) / kHB, kHB, 0, s>>>(P, n, g, deg, star, err);
+        k_hull_star<<<(n + kHB - 1) / kHB, kHB, 0, s>>>(P, nullptr, n, 1, 1, g, deg, star, retry, err + 1, err);
+        rc = check_launch();
+    }
+    int nRetry = 0;
+    if (!rc) rc = (cudaMemcpyAsync(&nRetry, err + 1, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                   cudaStreamSynchronize(s) == cudaSuccess) ? SVM_OK : SVM_ERR_CUDA;
+    if (!rc && nRetry > 0) {
+        k_hull_star<<<(nRetry + kHB - 1) / kHB, kHB, 0, s>>>(P, retry, nRetry, 2, kMaxW, g, deg, star, nullptr,
+                                                            nullptr, err);
         rc = check_launch();
     }
     if (!rc) {
