@@ -279,6 +279,76 @@ class sphericalSelfPropelledParticle : public updater {
     noiseSource noise;
 };
 
+// sphericalVectorialVicsek (src/updaters/sphericalVectorialVicsek.{h,cpp}; defaults of
+// vectorialVicsek.h:11): the self-propelled move, then each director relaxes at rate dt / tau towards
+// the tangent average of itself and its three vertex neighbours plus Eta times a random tangent
+// unit vector.
+class sphericalVectorialVicsek : public updater {
+  public:
+    explicit sphericalVectorialVicsek(bool rep = true) { reproducible = rep; noise.setReproducible(rep); }
+    void setMu(scalar m) { mu = m; }
+    void setV0(scalar v) { v0 = v; }
+    void setEta(scalar e) { Eta = e; }
+    void setTau(scalar t) { tau = t; }
+    void performUpdate() override { integrateEquationOfMotion(); }
+    void integrateEquationOfMotion() {
+        const uint64_t seed = noise.RNGSeed >= 0 ? (uint64_t)noise.RNGSeed : 1337u;
+        check(svm_vicsek_step(model->h(), deltaT, mu, v0, Eta, tau, SVM_NOISE_PHILOX, nullptr, seed), "vicsek step");
+    }
+    scalar mu = 1.0, v0 = 0.01, Eta = 1.0, tau = 1.0;
+    noiseSource noise;
+};
+
+// neighborList (src/utilities/neighborList.h:8-75): metric neighbours within maxRange of each point
+// (minimum image in a periodic box of side 2 radius), rows of Nmax entries, zero past each count.
+class neighborList {
+  public:
+    neighborList(scalar range, scalar sphereRadius, int subGridReduction = 1, int slotCapacity = 16)
+        : maxRange(range), radius(sphereRadius), sub(subGridReduction), cap(slotCapacity) {}
+    ~neighborList() { if (nl) svm_neighbor_list_destroy(nl); }
+    neighborList(const neighborList&) = delete;
+    neighborList& operator=(const neighborList&) = delete;
+    // the model's current vertex positions
+    void computeNeighborLists(sphericalVertexModel& m) {
+        ensure(m.getNumberOfParticles());
+        check(svm_neighbor_list_compute_model(nl, m.h()), "computeNeighborLists");
+        fetch();
+    }
+    // caller points already on the device (AoS double[3 n])
+    void computeNeighborLists(const double* pointsDevice, int n) {
+        ensure(n);
+        check(svm_neighbor_list_compute(nl, pointsDevice, n), "computeNeighborLists");
+        fetch();
+    }
+    scalar maxRange, radius;
+    int Nmax = 4;
+    std::vector<unsigned> neighborsPerParticle;
+    std::vector<int> particleIndices;       // [n * Nmax], row per point
+    std::vector<double> neighborVectors;    // [n * Nmax * 3]
+    std::vector<double> neighborDistances;  // [n * Nmax]
+
+  private:
+    void ensure(int n) {
+        if (nl && n == nPoints) return;
+        if (nl) svm_neighbor_list_destroy(nl);
+        nl = nullptr;
+        check(svm_neighbor_list_create(maxRange, radius, sub, n, cap, nullptr, &nl), "neighborList");
+        nPoints = n;
+    }
+    void fetch() {
+        check(svm_neighbor_list_get(nl, &Nmax, nullptr, nullptr, nullptr, nullptr, 0), "get");
+        const size_t e = (size_t)nPoints * Nmax;
+        neighborsPerParticle.resize(nPoints);
+        particleIndices.resize(e);
+        neighborVectors.resize(3 * e);
+        neighborDistances.resize(e);
+        check(svm_neighbor_list_get(nl, &Nmax, neighborsPerParticle.data(), particleIndices.data(),
+                                    neighborVectors.data(), neighborDistances.data(), (long)e), "get");
+    }
+    int sub, cap, nPoints = 0;
+    svm_neighbor_list* nl = nullptr;
+};
+
 // energyMinimizerFIRE (src/updaters/energyMinimizerFIRE.h:27-68)
 class energyMinimizerFIRE : public updater {
   public:
