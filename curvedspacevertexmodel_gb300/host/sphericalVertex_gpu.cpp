@@ -44,8 +44,44 @@ static int run_batch(int argc, char** argv) {
     return 0;
 }
 
+// "active N steps seed": the Vicsek updater on the model through the C++ classes, then the model's
+// neighbour list (range 1, radius R + 2.5, as sphericalModel.cpp:21 sets it up).
+static int run_active(int argc, char** argv) {
+    const int N = argc > 2 ? std::atoi(argv[2]) : 200;
+    const int iterations = argc > 3 ? std::atoi(argv[3]) : 100;
+    const int seed = argc > 4 ? std::atoi(argv[4]) : 1137;
+    try {
+        noiseSource noise(true);
+        noise.setReproducibleSeed(seed);
+        auto model = std::make_shared<sphericalVertexModel>(N, noise, 1.0, 3.8, true, false);
+        model->setT1Threshold(0.04);
+        auto V = std::make_shared<sphericalVectorialVicsek>(true);
+        V->noise.setReproducibleSeed(seed + 3);
+        V->setModel(model);
+        V->setDeltaT(0.01);
+        V->setV0(0.1);
+        V->setEta(0.4);
+        V->setTau(0.5);
+        for (int i = 0; i < iterations; ++i) V->performUpdate();
+        model->computeGeometry();
+        const double e = model->computeEnergy();
+        neighborList nl(1.0, model->radius + 2.5);
+        nl.computeNeighborLists(*model);
+        long pairs = 0, indexSum = 0;
+        for (unsigned c : nl.neighborsPerParticle) pairs += c;
+        for (int j : nl.particleIndices) indexSum += j;
+        std::printf("{\"vertices\": %d, \"energy\": %.17g, \"Nmax\": %d, \"pairs\": %ld, \"index_sum\": %ld}\n",
+                    model->getNumberOfParticles(), e, nl.Nmax, pairs, indexSum);
+    } catch (const std::exception& ex) {
+        std::fprintf(stderr, "error: %s\n", ex.what());
+        return 1;
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc > 1 && std::string(argv[1]) == "batch") return run_batch(argc, argv);
+    if (argc > 1 && std::string(argv[1]) == "active") return run_active(argc, argv);
     const int N = argc > 1 ? std::atoi(argv[1]) : 200;
     const int iterations = argc > 2 ? std::atoi(argv[2]) : 100;
     const double T = argc > 3 ? std::atof(argv[3]) : 0.01;

@@ -64,3 +64,35 @@ def test_cpp_batch_matches_python_batch(svm):
     b.computeGeometry()
     assert cpp["vertices"] == b.nVertices
     assert cpp["energies"] == list(b.replicaEnergies())
+
+
+def test_cpp_vicsek_and_neighbour_list_match_python_classes(svm):
+    """The Vicsek updater and the neighbour list through the C++ classes and through the Python
+    classes: the same energy after 60 steps and the same lists, bit for bit."""
+    import numpy as np
+    exe = os.path.join(os.path.dirname(svm.__file__), "sphericalVertex_gpu")
+    N, steps, seed = 300, 60, 41
+    out = subprocess.run([exe, "active", str(N), str(steps), str(seed)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    cpp = json.loads(out.stdout.strip().splitlines()[-1])
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(seed)
+    m = svm.sphericalVertexModel(N, noise, 1.0, 3.8)
+    m.setT1Threshold(0.04)
+    v = svm.sphericalVectorialVicsek()
+    v.noise.setReproducibleSeed(seed + 3)
+    v.setModel(m)
+    v.setDeltaT(0.01)
+    v.setV0(0.1)
+    v.setEta(0.4)
+    v.setTau(0.5)
+    v.run(steps)
+    m.computeGeometry()
+    nl = svm.neighborList(1.0, m.radius + 2.5)
+    nl.computeNeighborLists(m)
+    assert cpp["vertices"] == m.nVertices
+    assert cpp["energy"] == m.computeEnergy()
+    assert cpp["Nmax"] == nl.Nmax
+    assert cpp["pairs"] == int(nl.neighborsPerParticle.sum())
+    assert cpp["index_sum"] == int(nl.particleIndices.astype(np.int64).sum())
+    nl.close()
