@@ -83,3 +83,16 @@ def test_crowded_bins_widen_the_cell_list(svm):
     _same(nl, ref)
     assert nl.Nmax >= 49
     nl.close()
+
+
+def test_small_edge_cases(svm):
+    """One point, a close pair, a pair across the periodic faces, a pair exactly at the range."""
+    import torch
+    small = [np.array([[0.5, -0.25, 1.0]]), np.array([[0.1, 0.2, 0.3], [0.15, 0.2, 0.3]]),
+             np.array([[3.99, 0.0, 0.0], [-3.99, 0.0, 0.0]]), np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]])]
+    for pts in small:
+        for sub in (1, 2):
+            nl = svm.neighborList(0.5, 4.0, sub)
+            nl.computeNeighborLists(torch.from_numpy(pts.copy()).cuda())
+            _same(nl, oracle.neighbor_list(pts, 0.5, 4.0, sub))
+            nl.close()

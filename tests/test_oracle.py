@@ -235,6 +235,16 @@ def test_neighbor_list_against_reference(oracle_mod):
         assert a[0] == b[0] and a[0] > 4, (rng_, sub)
         for x, y in zip(a[1:], b[1:]):
             assert np.array_equal(x, y), (rng_, sub)
+    # edge cases: one point, a close pair, a pair across the periodic faces, a pair exactly at range
+    small = [np.array([[0.5, -0.25, 1.0]]), np.array([[0.1, 0.2, 0.3], [0.15, 0.2, 0.3]]),
+             np.array([[3.99, 0.0, 0.0], [-3.99, 0.0, 0.0]]), np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]])]
+    for pts in small:
+        for sub in (1, 2):
+            a = oracle_mod.neighbor_list(pts, 0.5, 4.0, sub)
+            b = oracle_mod.neighbor_list(pts, 0.5, 4.0, sub, reference=True)
+            assert a[0] == b[0] == 4
+            for x, y in zip(a[1:], b[1:]):
+                assert np.array_equal(x, y), pts
 
 
 @ref_only
