@@ -175,3 +175,19 @@ def test_abi_rejects_bad_arguments_without_a_device(svm):
     cnt = C.c_int()
     assert L.svm_mlp_parameter_count(C.byref(cnt)) == 0 and cnt.value == 24 * 64 + 64 + 64 * 64 + 64 + 2 * 64 + 2
     assert L.svm_status_string(ERR_ARG) and L.svm_status_string(999)
+
+
+def test_device_paths_fail_loudly_without_a_device(svm):
+    """With no GPU the device entry points return an error that the Python classes raise; nothing
+    falls back to host code (the host hull stays a separate, explicit entry point)."""
+    if svm.device_count() > 0:
+        pytest.skip("a device is present")
+    pts = svm.random_cell_centres(3, 50)
+    with pytest.raises(svm.SVMError):
+        svm.Topology(pts, device=True)
+    with pytest.raises(svm.SVMError):
+        svm.sphericalVertexModel(50, svm.noiseSource())
+    nl = svm.neighborList(1.0, 5.0)
+    with pytest.raises(svm.SVMError):
+        nl._ensure(10)
+    assert svm.Topology(pts).nVertices == 96  # the explicit host builder
