@@ -750,6 +750,9 @@ class neighborList:
             self._ensure(points.nVertices)
             call("svm_neighbor_list_compute_model", self._h, points.handle)
         else:
+            if (not getattr(points, "is_cuda", False) or str(points.dtype) != "torch.float64"
+                    or points.dim() != 2 or points.shape[1] != 3 or not points.is_contiguous()):
+                raise ValueError("points: a contiguous float64 CUDA tensor of shape (n, 3), or a model")
             n = int(points.shape[0])
             self._ensure(n)
             call("svm_neighbor_list_compute", self._h, C.c_void_p(points.data_ptr()), n)

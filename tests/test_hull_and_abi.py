@@ -191,3 +191,12 @@ def test_device_paths_fail_loudly_without_a_device(svm):
     with pytest.raises(svm.SVMError):
         nl._ensure(10)
     assert svm.Topology(pts).nVertices == 96  # the explicit host builder
+
+
+def test_neighbor_list_rejects_host_or_misshapen_points(svm):
+    import torch
+    nl = svm.neighborList(1.0, 5.0)
+    for bad in (torch.zeros(10, 3, dtype=torch.float64), torch.zeros(10, 3, dtype=torch.float32),
+                torch.zeros(10, 2, dtype=torch.float64), np.zeros((10, 3))):
+        with pytest.raises(ValueError):
+            nl.computeNeighborLists(bad)
