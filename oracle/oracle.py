@@ -344,6 +344,8 @@ def ref_lib():
         _sig(lib, "ref_radius", C.c_double, vp)
         _sig(lib, "ref_active_setup", None, vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
              C.c_double)
+        _sig(lib, "ref_dynamics", None, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
+             C.POINTER(C.c_double), C.POINTER(C.c_double))
         for n in ("positions", "forces", "velocities", "cell_positions", "area_perimeter", "directors"):
             _sig(lib, "ref_get_" + n, None, vp, _dp)
         _sig(lib, "ref_set_positions", None, vp, _dp)
@@ -472,12 +474,16 @@ class RefModel:
                     vnbrs=self.vertex_neighbors(), radius=self.radius)
 
 
-def dynamics(initial, current, radius, fraction=1.0, cutoff=0.5):
-    """computeMSD and computeOverlapFunction (src/analysis/dynamicalFeatures.cpp:17-53)."""
+def dynamics(initial, current, radius, fraction=1.0, cutoff=0.5, reference=False):
+    """computeMSD and computeOverlapFunction (src/analysis/dynamicalFeatures.cpp:17-53);
+    reference=True runs the reference's own class from oracle/_ref."""
     a = np.ascontiguousarray(initial, dtype=np.float64).reshape(-1)
     b = np.ascontiguousarray(current, dtype=np.float64).reshape(-1)
     msd, ov = C.c_double(), C.c_double()
-    orc_lib().orc_dynamics(a, b, a.size // 3, fraction, radius, cutoff, C.byref(msd), C.byref(ov))
+    if reference:
+        ref_lib().ref_dynamics(a, b, a.size // 3, fraction, radius, cutoff, C.byref(msd), C.byref(ov))
+    else:
+        orc_lib().orc_dynamics(a, b, a.size // 3, fraction, radius, cutoff, C.byref(msd), C.byref(ov))
     return msd.value, ov.value
 
 

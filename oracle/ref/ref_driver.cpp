@@ -17,6 +17,7 @@
 #include "neighborList.h"
 #include "sphericalSelfPropelledParticle.h"
 #include "sphericalVectorialVicsek.h"
+#include "dynamicalFeatures.h"
 
 struct ref_handle {
     noiseSource initNoise{true};
@@ -76,6 +77,22 @@ void ref_get_directors(ref_handle* h, double* out) {
     ArrayHandle<dVec> a(h->model->returnDirectors(), access_location::host, access_mode::read);
     for (int i = 0; i < h->model->getNumberOfParticles(); ++i)
         for (int d = 0; d < 3; ++d) out[3 * i + d] = a.data[i].x[d];
+}
+
+// dynamicalFeatures(initial, sphere, fraction).computeMSD / computeOverlapFunction
+// (src/analysis/dynamicalFeatures.cpp:6-53) on caller positions.
+void ref_dynamics(const double* init, const double* cur, int n, double fraction, double radius, double cutoff,
+                  double* msd, double* overlap) {
+    GPUArray<dVec> a((unsigned int)n, true), b((unsigned int)n, true);
+    {
+        ArrayHandle<dVec> ha(a, access_location::host, access_mode::overwrite);
+        ArrayHandle<dVec> hb(b, access_location::host, access_mode::overwrite);
+        for (int i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) { ha.data[i].x[d] = init[3 * i + d]; hb.data[i].x[d] = cur[3 * i + d]; }
+    }
+    dynamicalFeatures df(a, std::make_shared<sphericalDomain>(radius), fraction);
+    *msd = df.computeMSD(b);
+    *overlap = df.computeOverlapFunction(b, cutoff);
 }
 
 // minimization.cpp:251-262

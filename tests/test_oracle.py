@@ -279,3 +279,22 @@ def test_active_updaters_against_reference(oracle_mod, kind):
         assert np.array_equal(ref.positions(), m.positions()), step
         assert np.array_equal(ref.directors(), m.directors()), step
     assert flips > 0
+
+
+@ref_only
+def test_dynamics_against_reference(oracle_mod):
+    """orc_dynamics against the reference's dynamicalFeatures (MSD with NaN distances skipped,
+    overlap below a cutoff, the first floor(N f) points): equal bit for bit, including a point
+    whose geodesic distance is NaN (acos of a rounding above 1)."""
+    rng = np.random.default_rng(8)
+    n, R = 3000, 15.45
+    a = rng.normal(size=(n, 3))
+    a *= R / np.linalg.norm(a, axis=1, keepdims=True)
+    b = a + rng.normal(scale=0.3, size=(n, 3))
+    b *= R / np.linalg.norm(b, axis=1, keepdims=True)
+    b[5] = a[5] * (1 + 1e-16)   # a rounding-level copy
+    for fraction in (1.0, 0.37, 0.999):
+        for cutoff in (0.5, 0.2, 2.0):
+            o = oracle_mod.dynamics(a, b, R, fraction, cutoff)
+            r = oracle_mod.dynamics(a, b, R, fraction, cutoff, reference=True)
+            assert o == r, (fraction, cutoff)
