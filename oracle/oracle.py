@@ -346,6 +346,8 @@ def ref_lib():
              C.c_double)
         _sig(lib, "ref_dynamics", None, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
              C.POINTER(C.c_double), C.POINTER(C.c_double))
+        _sig(lib, "ref_log_spaced", None, C.c_int, C.c_double, C.c_int,
+             np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"))
         for n in ("positions", "forces", "velocities", "cell_positions", "area_perimeter", "directors"):
             _sig(lib, "ref_get_" + n, None, vp, _dp)
         _sig(lib, "ref_set_positions", None, vp, _dp)
@@ -487,8 +489,13 @@ def dynamics(initial, current, radius, fraction=1.0, cutoff=0.5, reference=False
     return msd.value, ov.value
 
 
-def log_spaced(first_save, exponent, count):
-    """The first `count` save steps of logSpacedIntegers (inc/simpleUtilities.h:5-41)."""
+def log_spaced(first_save, exponent, count, reference=False):
+    """The first `count` save steps of logSpacedIntegers (inc/simpleUtilities.h:5-41);
+    reference=True runs the reference's own class from oracle/_ref."""
+    if reference:
+        out = np.empty(count, dtype=np.int64)
+        ref_lib().ref_log_spaced(int(first_save), float(exponent), int(count), out)
+        return out
     out = np.empty(count, dtype=np.int32)
     orc_lib().orc_log_spaced(int(first_save), float(exponent), int(count), out)
     return out

@@ -18,6 +18,7 @@
 #include "sphericalSelfPropelledParticle.h"
 #include "sphericalVectorialVicsek.h"
 #include "dynamicalFeatures.h"
+#include "simpleUtilities.h"
 
 struct ref_handle {
     noiseSource initNoise{true};
@@ -93,6 +94,12 @@ void ref_dynamics(const double* init, const double* cur, int n, double fraction,
     dynamicalFeatures df(a, std::make_shared<sphericalDomain>(radius), fraction);
     *msd = df.computeMSD(b);
     *overlap = df.computeOverlapFunction(b, cutoff);
+}
+
+// The first `count` save steps of logSpacedIntegers(firstSave, exponent) (inc/simpleUtilities.h:5-41).
+void ref_log_spaced(int firstSave, double exponent, int count, long* out) {
+    logSpacedIntegers lsi(firstSave, exponent);
+    for (int i = 0; i < count; ++i) { out[i] = lsi.nextSave; lsi.update(); }
 }
 
 // minimization.cpp:251-262

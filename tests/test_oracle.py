@@ -298,3 +298,11 @@ def test_dynamics_against_reference(oracle_mod):
             o = oracle_mod.dynamics(a, b, R, fraction, cutoff)
             r = oracle_mod.dynamics(a, b, R, fraction, cutoff, reference=True)
             assert o == r, (fraction, cutoff)
+
+
+@ref_only
+@pytest.mark.parametrize("first,exponent,count", [(0, 0.05, 150), (0, 0.1, 80), (37, 0.05, 150), (1000, 0.02, 150)])
+def test_log_spaced_against_reference(oracle_mod, first, exponent, count):
+    """orc_log_spaced against the reference's logSpacedIntegers, schedule for schedule."""
+    assert np.array_equal(oracle_mod.log_spaced(first, exponent, count),
+                          oracle_mod.log_spaced(first, exponent, count, reference=True))
