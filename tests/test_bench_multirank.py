@@ -66,3 +66,12 @@ def test_missing_rank_ends_with_an_error():
     assert p.exitcode not in (0, None)
     if p.is_alive():
         p.kill()
+
+
+def test_fp64_roofline_arithmetic():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    r = bench.fp64_roofline(0.6, 199996)
+    assert abs(r["peak"] - 629.28) < 1e-9
+    assert abs(r["achieved"] - 1420 * 199996 / 0.6e-3 / 1e9) < 1e-9
+    assert 0.7 < r["frac"] < 0.8
