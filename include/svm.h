@@ -79,7 +79,10 @@ int svm_topology_from_points(const double* cellCentres, int nCells, svm_topology
 /* The same topology computed on the device (cell centres: HOST double[3*nCells]): per-centre
  * stars of the hull by gift wrapping over cell-list candidates, certified by their circumcaps,
  * checked for consistency, then numbered and assembled exactly as svm_topology_from_points does.
- * Replaces convexHullCGALInterface::sphericalConvexHullForVertexModel (convexHullCGAL.cpp:82-186). */
+ * Replaces convexHullCGALInterface::sphericalConvexHullForVertexModel (convexHullCGAL.cpp:82-186).
+ * SVM_ERR_HULL when the stars do not close into one triangulated sphere, or when a centre would need
+ * more than 512 candidates (a local density roughly 7x the mean): svm_topology_from_points then
+ * builds the same topology on the host. */
 int svm_topology_from_points_gpu(const double* cellCentres, int nCells, void* stream, svm_topology** out);
 /* Same contract from caller-supplied hull triangles (CCW seen from outside, int[3*nTri]). */
 int svm_topology_from_triangles(const double* cellCentres, int nCells, const int* triangles, int nTriangles,
@@ -205,7 +208,7 @@ int svm_spp_step(svm_model* m, double dt, double mu, double v0, double tau, int 
  * normalised), projected and normalised, and n += (dt / tau)(target - n), projected and
  * normalised.  noiseMode SVM_NOISE_BUFFER: `uniforms` = HOST double[2 nV], (u, w) per vertex in
  * [0, 1) as the reference draws them; SVM_NOISE_PHILOX: in-kernel draws (seed, step).  FP64 form,
- * single spheres. */
+ * single spheres; tau must be non-zero (SVM_ERR_ARG). */
 int svm_vicsek_step(svm_model* m, double dt, double mu, double v0, double eta, double tau, int noiseMode,
                     const double* uniforms, uint64_t seed);
 /* Device pointer of the current positions for callers that keep data on the GPU: double4 (x, y,
