@@ -14,6 +14,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 #include "svm_internal.cuh"
 #include "svm_force.cuh"
@@ -1820,13 +1821,19 @@ int launch_geometry(svm_model* m) {
 // 3000 vertices (from 20000 vertices on, at most the co-resident count), or the count set by
 // svm_model_set_t1_blocks.
 static int t1_coop_blocks(svm_model* m) {
-    static int maxCoop = 0;  // co-resident blocks of k_t1_parallel<true> on this device
+    // co-resident blocks of k_t1_parallel<true>, per device (computed on the model's device, which
+    // is current while its calls run); atomics, as host threads may drive models concurrently
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> maxCoopOf[kMaxDevices];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int maxCoop = dev >= 0 && dev < kMaxDevices ? maxCoopOf[dev].load(std::memory_order_relaxed) : 0;
     if (maxCoop == 0) {
-        int dev = 0, sms = 0, perSm = 0;
-        cudaGetDevice(&dev);
+        int sms = 0, perSm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_t1_parallel<true>, kCoopThreads, 0);
         maxCoop = std::max(1, sms * perSm);
+        if (dev >= 0 && dev < kMaxDevices) maxCoopOf[dev].store(maxCoop, std::memory_order_relaxed);
     }
     int n = m->t1Blocks;
     if (n == 0) n = m->nVertices < 20000 ? 1 : std::max(8, std::min(152, m->nVertices / 3000));

@@ -133,6 +133,17 @@ def load(path: str) -> warmStartNetwork:
     return net
 
 
+def fallback_reason(e_start, e_after_warm_start, max_force_after=None, tolerance=1e-9):
+    """Why plain FIRE from the unperturbed start must replace the warm-started run, or None: the
+    warm start raised the energy, or FIRE from it missed the force tolerance within its iteration
+    budget.  Written so that a NaN energy or force (a diverged warm start) takes the fallback."""
+    if not (e_after_warm_start <= e_start):
+        return "warm start raised the energy"
+    if max_force_after is not None and not (max_force_after < tolerance):
+        return "iteration budget exceeded"
+    return None
+
+
 def compare(net: warmStartNetwork, n: int, p0: float, seed: int, budget: float = 1.25, max_iterations: int = 100000,
             scales=(0.5, 0.25, 0.125)):
     """Plain FIRE and warm-started FIRE from the same start state (wall seconds and iterations).
@@ -165,14 +176,11 @@ def compare(net: warmStartNetwork, n: int, p0: float, seed: int, budget: float =
         net.setOutputScale(base * f_best)
         net.warmStart(m)
         net.setOutputScale(base)
-    fallback = None
-    if e_warm0 > e0:
-        fallback = "warm start raised the energy"
-    else:
+    fallback = fallback_reason(e0, e_warm0)
+    if fallback is None:
         cap = int(budget * it_p) if budget else max_iterations
         it_w, t_w, f_w = minimize(m, max_iterations=cap)
-        if f_w >= 1e-9:
-            fallback = "iteration budget exceeded"
+        fallback = fallback_reason(e0, e_warm0, f_w)
     if fallback:
         m.loadState(start)
         it_w, t_fb, f_w = minimize(m, max_iterations=max_iterations)

@@ -68,7 +68,8 @@ def test_same_state_evaluation_matches_fp64(svm, state20k):
     assert np.median(resid) < 1e-15 and resid.max() < 4 * ulp_angle * m.radius ** 2
     per = np.abs(ap32[:, 1] - ap64[:, 1]) / ap64[:, 1]
     assert per.max() < RTOL_PERIMETER
-    assert abs(e32 - e64) / e64 < 1e-5
+    # the goal's bar for the mixed form: energy within 1e-6 relative of FP64 (measured ~2e-8)
+    assert abs(e32 - e64) / e64 < 1e-6
     assert rel_err(cp32, cp64, m.radius) < 1e-6
     fmax = np.max(np.linalg.norm(f64, axis=1))
     rings, counts = m.rings()

@@ -28,3 +28,16 @@ def test_bf16_rounding():
     # 1 + 2^-8 is a tie between 1 and 1 + 2^-7: to even (1); 1 + 3 2^-8 ties up to 1 + 2^-6
     assert list(r[:5]) == [1.0, 1.0, 1.0 + 2 ** -7, 1.0 + 2 ** -6, -2.5]
     assert abs(r[5] - 3.140625) < 1e-12
+
+
+def test_warm_start_fallback_decision_takes_nan():
+    """A diverged warm start (NaN energy or NaN force) falls back to plain FIRE, as do a raised
+    energy and a missed force tolerance; a warm start that lowered the energy and converged does not."""
+    from curvedspacevertexmodel_gb300.warm_start import fallback_reason
+    nan = float("nan")
+    assert fallback_reason(10.0, nan) == "warm start raised the energy"
+    assert fallback_reason(10.0, 11.0) == "warm start raised the energy"
+    assert fallback_reason(10.0, 9.0) is None
+    assert fallback_reason(10.0, 9.0, nan) == "iteration budget exceeded"
+    assert fallback_reason(10.0, 9.0, 2e-9) == "iteration budget exceeded"
+    assert fallback_reason(10.0, 9.0, 5e-10) is None
