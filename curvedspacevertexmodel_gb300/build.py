@@ -5,6 +5,11 @@
 Each translation unit is compiled in parallel with nvcc (-gencode arch=compute_103a,code=sm_103a)
 and the objects are linked into curvedspacevertexmodel_gb300/libsvm.so.  Objects go to
 curvedspacevertexmodel_gb300/_build/.
+
+A second library, libsvm_pacos.so, is the same code with the FP64 geometry's arccosine replaced by
+the portable one (csrc/svm_acos.h, -DSVM_PORTABLE_ACOS): the translation units that evaluate acos
+are compiled once more with that macro and linked with the other objects.  Selected with
+SVM_LIBRARY, it reproduces the CPU restatement's portable mode bit for bit.
 """
 from __future__ import annotations
 
@@ -18,6 +23,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libsvm.so")
+LIB_PACOS = os.path.join(PKG, "libsvm_pacos.so")
+# translation units whose kernels evaluate acos (through svm_acos in svm_internal.cuh)
+PACOS_SOURCES = ("svm_model.cu", "svm_mixed.cu")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -73,6 +81,13 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
         if _needs(obj, [src] + headers):
             flags = [("-fmad=true" if f in FMA_SOURCES and flg == "-fmad=false" else flg) for flg in NVCC_FLAGS]
             jobs.append([nvcc, *ARCH, *flags, *extra_nvcc, "-c", src, "-o", obj])
+    pacos_objs = list(objs)
+    for f in PACOS_SOURCES:
+        src = os.path.join(CSRC, f)
+        obj = os.path.join(BUILD, f + ".pacos.o")
+        pacos_objs[objs.index(os.path.join(BUILD, f + ".o"))] = obj
+        if _needs(obj, [src] + headers):
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra_nvcc, "-DSVM_PORTABLE_ACOS", "-c", src, "-o", obj])
     for f in cpp:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")
@@ -89,12 +104,16 @@ def build(verbose: bool = False, extra_nvcc=()) -> str:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return r.stderr
 
+    jobs.sort(key=lambda cmd: -os.path.getsize(cmd[cmd.index("-c") + 1]))  # longest compiles first
     with cf.ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 4))) as ex:
         for msg in ex.map(run, jobs):
             if verbose and msg:
                 print(msg)
     if jobs or not os.path.exists(LIB):
         run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    cpp_objs = [o for o in objs if o.endswith(".cpp.o")]
+    if jobs or not os.path.exists(LIB_PACOS):
+        run([nvcc, *ARCH, "-shared", "-o", LIB_PACOS, *pacos_objs, *cpp_objs, "-lcudart"])
     # the C++ host layer's example driver (links libsvm.so)
     host = os.path.join(PKG, "host")
     exe = os.path.join(PKG, "sphericalVertex_gpu")

@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <vector>
 #include "../../include/svm.h"
+#include "svm_acos.h"
 
 namespace svm {
 
@@ -28,6 +29,18 @@ constexpr double kPI = 3.141592653589793115997963468544185161590576171875;
 constexpr double kPILo = 1.2246467991473532e-16;
 
 struct D3 { double x, y, z; };
+
+// The arccosine of the FP64 geometry (arcs, included angles, triangle areas, T1 length tests).
+// The default build uses CUDA's acos; a build with -DSVM_PORTABLE_ACOS uses svm_portable::acos,
+// the same operations as the CPU restatement's portable mode, which makes GPU and CPU trajectories
+// comparable bit for bit.
+__device__ __forceinline__ double svm_acos(double x) {
+#ifdef SVM_PORTABLE_ACOS
+    return svm_portable::acos(x);
+#else
+    return acos(x);
+#endif
+}
 
 __device__ __forceinline__ D3 ld3(const double4_32a* p, int i) {
     double4_32a t = p[i];
@@ -76,14 +89,14 @@ __device__ __forceinline__ D3 sphere_move(D3 p, D3 v, double R) {
 __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
     double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
-    return R * acos(num / den);
+    return R * svm_acos(num / den);
 }
 // |p| as geodesic and sph_coords evaluate it (same operations, so the same value)
 __device__ __forceinline__ double pos_norm(D3 p) { return sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
 // geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
 __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
     const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
-    return R * acos(num / (n1 * n2));
+    return R * svm_acos(num / (n1 * n2));
 }
 // The T1 length test geodesic(p1, p2) < t, i.e. R acos(c) < t with c = p1.p2 / (|p1||p2|).  acos
 // is decreasing, so away from c = cos(t / R) the answer is c > cos(t / R); the formula itself is
@@ -128,7 +141,7 @@ __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, d
     const double c = num / den;
     if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
     if (c < cosLo) return false;
-    return R * acos(c) < t;
+    return R * svm_acos(c) < t;
 }
 // Arc length in the mixed-precision form: 2 R asin(|q - p| / 2R) in FP32 from the raw chord
 // (exact for nearby FP32 points), well conditioned for the short arcs of the model (the acos form
@@ -141,7 +154,7 @@ __device__ __forceinline__ float arc32(float4 p, float4 q, float R) {
 __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
-    double a = acos(-dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1))));
+    double a = svm_acos(-dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1))));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -159,7 +172,7 @@ __device__ __forceinline__ double included_angle_pre(D3 Cx, D3 Cl, double nx, do
     const double det = dot3(pl, Cx);
     double c = dot3(Cx, Cl) / (nx * nl);
     if (clamp) c = fmin(1.0, fmax(-1.0, c));
-    double a = acos(c);
+    double a = svm_acos(c);
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -174,7 +187,7 @@ __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
     double c = -dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1)));
-    double a = acos(fmin(1.0, fmax(-1.0, c)));
+    double a = svm_acos(fmin(1.0, fmax(-1.0, c)));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -190,9 +203,9 @@ __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
 __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R) {
     double d12 = dot3(p1, p2), d13 = dot3(p1, p3), d23 = dot3(p2, p3);
     double area = -kPI;
-    area += acos((d23 - d12 * d13) / (sqrt(1 - d12 * d12) * sqrt(1 - d13 * d13)));
-    area += acos((d12 - d13 * d23) / (sqrt(1 - d13 * d13) * sqrt(1 - d23 * d23)));
-    area += acos((d13 - d12 * d23) / (sqrt(1 - d12 * d12) * sqrt(1 - d23 * d23)));
+    area += svm_acos((d23 - d12 * d13) / (sqrt(1 - d12 * d12) * sqrt(1 - d13 * d13)));
+    area += svm_acos((d12 - d13 * d23) / (sqrt(1 - d13 * d13) * sqrt(1 - d23 * d23)));
+    area += svm_acos((d13 - d12 * d23) / (sqrt(1 - d12 * d12) * sqrt(1 - d23 * d23)));
     return area * (R * R);
 }
 

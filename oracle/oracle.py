@@ -97,8 +97,30 @@ def orc_lib():
         _sig(lib, "orc_fire_state", None, vp, _dp)
         _sig(lib, "orc_cell_list_dims", C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double))
         _sig(lib, "orc_cell_list", C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int), _ip, _up, _ip, C.c_long)
+        _sig(lib, "orc_set_portable_acos", None, C.c_int)
+        _sig(lib, "orc_set_acos_mode", None, C.c_int, C.c_ulonglong)
+        _sig(lib, "orc_acos_portable", None, _dp, _dp, C.c_long)
         _orc = lib
     return _orc
+
+
+def set_portable_acos(on: bool) -> None:
+    """Geometry arccosine of every oracle model in this process: the C library's (the reference's
+    std::acos; the default) or the portable one shared with the device's portable build."""
+    orc_lib().orc_set_portable_acos(1 if on else 0)
+
+
+def set_acos_mode(mode: int, seed: int = 0) -> None:
+    """0: the C library's acos; 1: the portable one; 2: the C library's with a seeded one-ulp
+    perturbation of one result in four (another faithful arccosine)."""
+    orc_lib().orc_set_acos_mode(int(mode), int(seed))
+
+
+def acos_portable(x) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+    out = np.empty_like(x)
+    orc_lib().orc_acos_portable(x, out, x.size)
+    return out
 
 
 class OracleNoise:

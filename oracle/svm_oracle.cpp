@@ -21,7 +21,37 @@
 #include <vector>
 #include <algorithm>
 
+#include "svm_acos.h"   // the portable arccosine shared with the device build (product csrc/)
+
 namespace {
+
+// The arccosine of the geometry: the C library's (as the reference calls std::acos), or, when
+// switched on by orc_set_portable_acos, svm_portable::acos -- the function the device library's
+// -DSVM_PORTABLE_ACOS build evaluates with the same operations, so that GPU and CPU trajectories
+// can be compared bit for bit.
+//
+// Mode 2 (orc_set_acos_mode) is another faithful arccosine: the C library's with one result in four
+// moved by one ulp, up or down, chosen by a hash of the argument's bits and a seed -- a fixed
+// function of the argument, like any library's.  An ensemble of such variants measures how far
+// the reference's own trajectory moves when only the last bits of acos change.
+int gAcosMode = 0;
+unsigned long long gAcosSeed = 0;
+inline unsigned long long mix64(unsigned long long z) {   // splitmix64 finaliser (Steele et al. 2014)
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+inline double racos(double x) {
+    if (gAcosMode == 0) return std::acos(x);
+    if (gAcosMode == 1) return svm_portable::acos(x);
+    const double y = std::acos(x);
+    unsigned long long b;
+    std::memcpy(&b, &x, sizeof b);
+    const unsigned long long h = mix64(b ^ gAcosSeed);
+    if ((h & 3ull) != 0 || !(y > 0.0)) return y;
+    return std::nextafter(y, (h >> 2) & 1ull ? 4.0 : 0.0);
+}
 
 const double kPI = 3.141592653589793115997963468544185161590576171875;  // inc/std_include.h:47
 
@@ -72,7 +102,7 @@ struct Sphere {
         double num = p1.x[0] * p2.x[0] + p1.x[1] * p2.x[1] + p1.x[2] * p2.x[2];
         double den = std::sqrt(p1.x[0] * p1.x[0] + p1.x[1] * p1.x[1] + p1.x[2] * p1.x[2]) *
                      std::sqrt(p2.x[0] * p2.x[0] + p2.x[1] * p2.x[1] + p2.x[2] * p2.x[2]);
-        return radius * std::acos(num / den);
+        return radius * racos(num / den);
     }
     // includedAngle (sphericalDomain.h:114-133)
     static double includedAngle(const V3& p1, const V3& p2, const V3& p3) {
@@ -80,7 +110,7 @@ struct Sphere {
         double det = p1.x[0] * (p2.x[1] * p3.x[2] - p2.x[2] * p3.x[1]) +
                      p1.x[1] * (p2.x[2] * p3.x[0] - p2.x[0] * p3.x[2]) +
                      p1.x[2] * (p2.x[0] * p3.x[1] - p2.x[1] * p3.x[0]);
-        double a = std::acos(-dot(ci, cim1) / (norm(ci) * norm(cim1)));
+        double a = racos(-dot(ci, cim1) / (norm(ci) * norm(cim1)));
         if (det > 0) a *= -1;
         if (a < 0) a += 2. * kPI;
         return a;
@@ -91,9 +121,9 @@ struct Sphere {
         putVirtual(p1); putVirtual(p2); putVirtual(p3);
         double d12 = dot(p1, p2), d13 = dot(p1, p3), d23 = dot(p2, p3);
         double area = -kPI;
-        area += std::acos((d23 - d12 * d13) / (std::sqrt(1 - d12 * d12) * std::sqrt(1 - d13 * d13)));
-        area += std::acos((d12 - d13 * d23) / (std::sqrt(1 - d13 * d13) * std::sqrt(1 - d23 * d23)));
-        area += std::acos((d13 - d12 * d23) / (std::sqrt(1 - d12 * d12) * std::sqrt(1 - d23 * d23)));
+        area += racos((d23 - d12 * d13) / (std::sqrt(1 - d12 * d12) * std::sqrt(1 - d13 * d13)));
+        area += racos((d12 - d13 * d23) / (std::sqrt(1 - d13 * d13) * std::sqrt(1 - d23 * d23)));
+        area += racos((d13 - d12 * d23) / (std::sqrt(1 - d12 * d12) * std::sqrt(1 - d23 * d23)));
         area *= (radius * radius);
         return area;
     }
@@ -194,6 +224,18 @@ struct orc_model {
 };
 
 extern "C" {
+
+// Selects the arccosine of the geometry: 0 the C library's (the reference's), 1 the portable one,
+// 2 the C library's with a seeded one-ulp perturbation of one result in four.
+void orc_set_acos_mode(int mode, unsigned long long seed) {
+    gAcosMode = mode;
+    gAcosSeed = seed;
+}
+void orc_set_portable_acos(int on) { orc_set_acos_mode(on ? 1 : 0, 0); }
+// svm_portable::acos over an array (checks of the portable function itself).
+void orc_acos_portable(const double* x, double* out, long n) {
+    for (long i = 0; i < n; ++i) out[i] = svm_portable::acos(x[i]);
+}
 
 orc_model* orc_create(int nCells, int nVertices, int W, const double* pos, const int* cellNeighbors,
                       const unsigned* cellCount, const int* vcn, const int* vn, double radius) {

@@ -4,18 +4,22 @@ exactly."""
 import numpy as np
 import pytest
 
-from gpu_helpers import gpu_model, load_gold, oracle_model, params, rel_err, same_rings, stabilised
+from gpu_helpers import gpu_model, load_gold, oracle_model, params, rel_err, same_rings, stabilised, traj_tol
 
 pytestmark = pytest.mark.gpu
 
 # Trajectories.  One step agrees with the CPU to ~1e-15 (RTOL_STEP).  Over many noisy steps the
-# reference's own closed-form gradients divide by 1 - s^2 ~ theta^2 for collapsing edges
-# (theta ~ 1e-4 rad before a T1), amplifying the last-bit differences between glibc's and CUDA's
-# acos (neither is correctly rounded; glibc's misrounds ~4e-4 of arguments) by up to ~1e8.  The
-# measured separation after 1000 steps of the N=200 configuration is 8e-10 (positions),
-# 3e-10 (areas/perimeters) and 3e-11 (energy), with the T1 flip set identical at every step.
+# reference's closed-form gradients divide by 1 - s^2 ~ theta^2 for collapsing edges (theta ~ 1e-4
+# rad before a T1), amplifying last-bit differences of acos by up to ~1e8.  CUDA's acos and glibc's
+# differ in the last bit (neither is correctly rounded: glibc's misrounds ~10% of arguments, by up to
+# 0.81 ulp), so no device acos reproduces glibc's bits and the trajectories separate: after 1000
+# steps of the N=200 configuration by 8e-10 (positions), 3e-10 (areas/perimeters), 3e-11 (energy),
+# with the T1 flip set identical at every step.  The reference itself moves as far when only the
+# last bits of its acos change (gpu_helpers.ACOS_SPREAD: the largest deviation over twelve faithful
+# arccosines), so the tolerance after 10, 100 and 1000 steps is twice that spread (traj_tol); with
+# one arccosine on both sides the GPU and CPU paths are equal bit for bit
+# (test_gpu_portable_acos.py).
 RTOL_STEP = 1e-12
-RTOL_TRAJ = 1e-8
 # One evaluation of the geometry differs from the CPU only by rounding (acos, FMA).
 RTOL_EVAL = 1e-12
 # Forces are closed forms with 1 - s^2 (s = cosine of a short arc) in their denominators; their
@@ -48,8 +52,9 @@ def test_geometry_forces_energy_match_golden(svm, gold):
 def test_brownian_1000_steps_match_oracle_and_golden(svm, gold, oracle_mod):
     """Config 1: N=200, T=0.01, dt=0.01, T1 threshold 0.04, the reference's mt19937 noise stream
     injected into both sides: the ordered T1 flip list identical at every step, connectivity
-    identical, positions/areas/perimeters/energy within RTOL_STEP after one step and RTOL_TRAJ
-    after 10, 100 and 1000 steps."""
+    identical, positions/areas/perimeters/energy within RTOL_STEP after one step and within
+    traj_tol (twice the reference's own spread under faithful changes of acos) after 10, 100 and
+    1000 steps."""
     p = params(gold)
     gm = gpu_model(svm, gold)
     om = oracle_model(oracle_mod, gold)
@@ -71,21 +76,22 @@ def test_brownian_1000_steps_match_oracle_and_golden(svm, gold, oracle_mod):
         assert np.array_equal(f_gpu, f_orc), f"T1 flips differ at step {step}: {f_gpu} vs {f_orc}"
         total_flips += len(f_orc)
         if step in (1, 10, 100, 1000):
-            tol = RTOL_STEP if step == 1 else RTOL_TRAJ
+            tol = {q: RTOL_STEP if step == 1 else traj_tol(step, q) for q in ("pos", "ap", "energy")}
             assert same_rings(gm, om), step
             assert np.array_equal(gm.vertexCellNeighbors(), om.vertex_cells()), step
             assert np.array_equal(gm.vertexNeighbors(), om.vertex_neighbors()), step
             R = float(gold["init_radius"])
-            assert rel_err(gm.returnPositions(), om.positions(), R) < tol, step
+            assert rel_err(gm.returnPositions(), om.positions(), R) < tol["pos"], step
             gm.computeGeometry()
             om.compute_geometry()
-            assert rel_err(gm.areaPerimeter(), om.area_perimeter()) < tol, step
+            ap_g, ap_o = gm.areaPerimeter(), om.area_perimeter()
+            assert np.max(np.abs(ap_g - ap_o) / np.abs(ap_o)) < tol["ap"], step
             e_g, e_o = gm.computeEnergy(), om.energy()
-            assert abs(e_g - e_o) / e_o < tol, step
+            assert abs(e_g - e_o) / e_o < tol["energy"], step
             # and the fixtures made from the reference itself
             g = f"s{step}_"
-            assert rel_err(gm.returnPositions(), gold[g + "pos"], R) < tol, step
-            assert abs(e_g - float(gold[g + "energy"])) / float(gold[g + "energy"]) < tol, step
+            assert rel_err(gm.returnPositions(), gold[g + "pos"], R) < tol["pos"], step
+            assert abs(e_g - float(gold[g + "energy"])) / float(gold[g + "energy"]) < tol["energy"], step
     assert total_flips == len(gold["flips"]) and total_flips > 100
     assert gm.deviceStatus() == 0
 

@@ -306,3 +306,34 @@ def test_log_spaced_against_reference(oracle_mod, first, exponent, count):
     """orc_log_spaced against the reference's logSpacedIntegers, schedule for schedule."""
     assert np.array_equal(oracle_mod.log_spaced(first, exponent, count),
                           oracle_mod.log_spaced(first, exponent, count, reference=True))
+
+
+def test_reference_trajectory_spread_under_faithful_acos(oracle_mod):
+    """The reference's N = 200 trajectory (the restatement, bit-exact with the reference build)
+    under twelve other faithful arccosines: one step stays at the last bit, and the largest
+    deviations from the golden fixture after 10, 100 and 1000 steps are ACOS_SPREAD, which sets the
+    GPU trajectory tolerances (gpu_helpers.traj_tol)."""
+    from gpu_helpers import ACOS_SPREAD, ACOS_SPREAD_VARIANTS, load_gold, oracle_model, params, trajectory_deviation
+    g = load_gold()
+    p = params(g)
+    R = float(g["init_radius"])
+    env = {s: dict(pos=0.0, ap=0.0, energy=0.0) for s in ACOS_SPREAD}
+    try:
+        for mode, seed in ACOS_SPREAD_VARIANTS:
+            oracle_mod.set_acos_mode(mode, seed)
+            om = oracle_model(oracle_mod, g)
+            noise = oracle_mod.OracleNoise(p["bd_seed"])
+            for step in range(1, 1001):
+                om.brownian_step_noise(noise.normals(3 * 396), p["T"], p["dt"], p["mu"])
+                if step == 1:
+                    assert np.max(np.abs(om.positions() - g["s1_pos"])) / R < 1e-15
+                if step in env:
+                    om.compute_geometry()
+                    d = trajectory_deviation(om.positions(), om.area_perimeter(), om.energy(), g, step)
+                    for q in d:
+                        env[step][q] = max(env[step][q], d[q])
+    finally:
+        oracle_mod.set_acos_mode(0, 0)
+    for step, d in env.items():
+        for q, v in d.items():
+            assert abs(v / ACOS_SPREAD[step][q] - 1) < 1e-3, (step, q, v)
