@@ -7,6 +7,7 @@ from .model import (  # noqa: F401
     Simulation,
     Topology,
     brownianDynamics,
+    dotProducts,
     energyMinimizerFIRE,
     neighborList,
     noiseSource,
@@ -16,14 +17,15 @@ from .model import (  # noqa: F401
     sphericalVectorialVicsek,
     sphericalVertexModel,
     sphericalVertexModelBatch,
+    velocityVerlet,
     warmStartNetwork,
 )
 from .trajectory import dynamicalFeatures, logSpacedIntegers, run_trajectory, vectorValueNetCDF  # noqa: F401
 
 __all__ = [
     "LIBPATH", "SVMError", "device_count", "lib", "PI", "Simulation", "Topology", "brownianDynamics",
-    "energyMinimizerFIRE", "neighborList", "noiseSource", "random_cell_centres", "random_vertex_directors",
+    "dotProducts", "energyMinimizerFIRE", "neighborList", "noiseSource", "random_cell_centres", "random_vertex_directors",
     "sphericalSelfPropelledParticle", "sphericalVectorialVicsek", "sphericalVertexModel",
-    "sphericalVertexModelBatch", "warmStartNetwork", "dynamicalFeatures", "logSpacedIntegers", "run_trajectory",
+    "sphericalVertexModelBatch", "velocityVerlet", "warmStartNetwork", "dynamicalFeatures", "logSpacedIntegers", "run_trajectory",
     "vectorValueNetCDF",
 ]

@@ -125,6 +125,10 @@ SIGNATURES = {
     "svm_fire_destroy": (i32, [vp]),
     "svm_fire_minimize": (i32, [vp, i32, C.POINTER(i32), C.POINTER(f64)]),
     "svm_fire_state": (i32, [vp, dp]),
+    "svm_fire_step": (i32, [vp]),
+    "svm_velocity_verlet_step": (i32, [vp, f64, i32]),
+    "svm_vv_half": (i32, [vp, f64]),
+    "svm_reduce_dots": (i32, [vp, dp]),
     "svm_fire_set_max_iterations": (i32, [vp, i32]),
     "svm_cell_list_create": (i32, [f64, f64, i32, i32, vp, pvp]),
     "svm_cell_list_destroy": (i32, [vp]),

@@ -12,6 +12,7 @@
 //                  (power test, dt / alpha adaptation, stopping test)
 // The host launches captured batches of iterations and reads only the `done` flag between them.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <vector>
 #include "svm_internal.cuh"
@@ -83,6 +84,24 @@ __device__ __forceinline__ D3 fire_velocity(const FireState& S, D3 v, D3 f) {
               __dadd_rn(__dmul_rn(a1, v.z), __dmul_rn(as, f.z))};
 }
 
+// velocityVerlet::integrateEOMCPU's first loop for one vertex (velocityVerlet.cpp:14-20: unit
+// masses, the model's masses being 1): disp = dt v + (dt^2 / 2) F, v += (dt / 2) F, then the move
+// onto the sphere (moveParticles).  Products rounded before the sums, as on the CPU.
+__device__ __forceinline__ void vv_drift(double4_32a* __restrict__ pos, double4_32a* __restrict__ vel, int i, D3 v,
+                                         D3 f, double dt, double R) {
+    const double hv = (0.5 / 1.0) * dt, h2 = 0.5 * dt * dt;
+    const D3 d{__dadd_rn(__dmul_rn(dt, v.x), __dmul_rn(h2, f.x)), __dadd_rn(__dmul_rn(dt, v.y), __dmul_rn(h2, f.y)),
+               __dadd_rn(__dmul_rn(dt, v.z), __dmul_rn(h2, f.z))};
+    v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
+    st3(vel, i, v);
+    st3(pos, i, move_exact_f(ld3(pos, i), d, R));
+}
+// gpu_update_velocity (velocityVerlet.cu): v += (dt / 2) F / m with unit masses.
+__device__ __forceinline__ D3 vv_kick(D3 v, D3 f, double dt) {
+    const double hv = (0.5 / 1.0) * dt;
+    return D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
+}
+
 __global__ void k_fire_vv1(const FireState* __restrict__ Sp, double4_32a* __restrict__ pos,
                            double4_32a* __restrict__ vel, const double4_32a* __restrict__ force, int nV, double R) {
     const FireState S = *Sp;
@@ -92,12 +111,86 @@ __global__ void k_fire_vv1(const FireState* __restrict__ Sp, double4_32a* __rest
     const D3 f = ld3(force, i);
     D3 v = ld3(vel, i);
     if (S.pending) v = fire_velocity(S, v, f);
-    const double dt = S.dt, hv = (0.5 / 1.0) * dt, h2 = 0.5 * dt * dt;
-    const D3 d{__dadd_rn(__dmul_rn(dt, v.x), __dmul_rn(h2, f.x)), __dadd_rn(__dmul_rn(dt, v.y), __dmul_rn(h2, f.y)),
-               __dadd_rn(__dmul_rn(dt, v.z), __dmul_rn(h2, f.z))};
-    v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
-    st3(vel, i, v);
-    st3(pos, i, move_exact_f(ld3(pos, i), d, R));
+    vv_drift(pos, vel, i, v, f, S.dt, R);
+}
+
+// The standalone velocity-Verlet drift: vv_drift with the caller's dt.
+__global__ void k_vv_drift(double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                           const double4_32a* __restrict__ force, int nV, double dt, double R) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    vv_drift(pos, vel, i, ld3(vel, i), ld3(force, i), dt, R);
+}
+__global__ void k_vv_half(double4_32a* __restrict__ vel, const double4_32a* __restrict__ force, int nV, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    st3(vel, i, vv_kick(ld3(vel, i), ld3(force, i), dt));
+}
+
+// F.v, F.F and v.v of one vertex, each a dot product accumulated in component order.
+__device__ __forceinline__ void fire_dots(D3 f, D3 v, double& P, double& FF, double& VV) {
+    P = __dadd_rn(__dadd_rn(__dmul_rn(f.x, v.x), __dmul_rn(f.y, v.y)), __dmul_rn(f.z, v.z));
+    FF = __dadd_rn(__dadd_rn(__dmul_rn(f.x, f.x), __dmul_rn(f.y, f.y)), __dmul_rn(f.z, f.z));
+    VV = __dadd_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), __dmul_rn(v.z, v.z));
+}
+
+// The block partials of (F.v, F.F, v.v, max F.F), then, in the last block to finish, their sums in a
+// fixed order.  kControl: the last block runs fireStepCPU's control on them (energyMinimizerFIRE.cpp:
+// 138-172: scaling, power test, dt / alpha adaptation; the velocity update is left pending for the
+// next vertex kernel); kCount: also minimize's iteration count and stopping test (cpp:187-191).
+// Without kControl the four totals go to out4.  Every thread of the block calls it.
+template <bool kControl, bool kCount>
+__device__ void fire_reduce_tail(FireState* __restrict__ Sp, double P, double FF, double VV, int nV,
+                                 double* __restrict__ partials, unsigned* __restrict__ ticket, double* __restrict__ out4,
+                                 double* sh, bool& amLast) {
+    const double bP = bsum(P, sh), bF = bsum(FF, sh), bV = bsum(VV, sh), bM = bmax(FF, sh);
+    if (threadIdx.x == 0) {
+        double* q = partials + 4 * blockIdx.x;
+        q[0] = bP; q[1] = bF; q[2] = bV; q[3] = bM;
+        __threadfence();
+        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!amLast) return;
+    double sP = 0.0, sF = 0.0, sV = 0.0, sM = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        sP += __ldcg(partials + 4 * b); sF += __ldcg(partials + 4 * b + 1);
+        sV += __ldcg(partials + 4 * b + 2); sM = fmax(sM, __ldcg(partials + 4 * b + 3));
+    }
+    const double tP = bsum(sP, sh), tF = bsum(sF, sh), tV = bsum(sV, sh), tM = bmax(sM, sh);
+    if (threadIdx.x != 0) return;
+    *ticket = 0u;
+    if (!kControl) {
+        out4[0] = tP; out4[1] = tF; out4[2] = tV; out4[3] = tM;
+        return;
+    }
+    FireState S = *Sp;
+    S.power = tP; S.forceNorm = tF; S.velNorm = tV; S.maxF2 = tM;
+    S.rmsOverN = sqrt(tF) / (double)nV;
+    S.maxForce = sqrt(tM);
+    S.scaling = tF > 0. ? sqrt(tV / tF) : 0.0;
+    S.alphaUsed = S.alpha;
+    S.zeroV = tP > 0 ? 0 : 1;
+    if (tP > 0) {
+        if (S.nSince > S.nMin) {
+            S.dt = fmin(S.dt * S.dtInc, S.dtMax);
+            S.alpha = S.alpha * S.alphaDec;
+            S.alpha = fmax(S.alpha, S.alphaMin);
+        }
+        S.nSince += 1;
+    } else {
+        S.nSince = 0;
+        S.dt = S.dt * S.dtDec;
+        S.dt = fmax(S.dt, S.dtMin);
+        S.alpha = S.alphaStart;
+    }
+    S.pending = 1;
+    if (kCount) {
+        S.iterations += 1;
+        const double crit = S.criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
+        if (S.iterations >= S.maxIterations || !(crit > S.cutoff)) S.done = 1;
+    }
+    *Sp = S;
 }
 
 // Clears the pending flag after the first vertex kernel of an iteration has consumed it.
@@ -123,57 +216,29 @@ __global__ void __launch_bounds__(3 * kSlotVerts) k_fire_force(ForceArgs A, Fire
     if (threadIdx.x < kSlotVerts && i < nV) {
         const D3 f = fv;
         st3(force, i, f);
-        const double hv = (0.5 / 1.0) * dt;
-        D3 v = ld3(vel, i);
-        v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
+        const D3 v = vv_kick(ld3(vel, i), f, dt);
         st3(vel, i, v);
-        P = __dadd_rn(__dadd_rn(__dmul_rn(f.x, v.x), __dmul_rn(f.y, v.y)), __dmul_rn(f.z, v.z));
-        FF = __dadd_rn(__dadd_rn(__dmul_rn(f.x, f.x), __dmul_rn(f.y, f.y)), __dmul_rn(f.z, f.z));
-        VV = __dadd_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), __dmul_rn(v.z, v.z));
+        fire_dots(f, v, P, FF, VV);
     }
-    const double bP = bsum(P, sh), bF = bsum(FF, sh), bV = bsum(VV, sh), bM = bmax(FF, sh);
-    if (threadIdx.x == 0) {
-        double* q = partials + 4 * blockIdx.x;
-        q[0] = bP; q[1] = bF; q[2] = bV; q[3] = bM;
-        __threadfence();
-        amLast = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!amLast) return;
-    double sP = 0.0, sF = 0.0, sV = 0.0, sM = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-        sP += __ldcg(partials + 4 * b); sF += __ldcg(partials + 4 * b + 1);
-        sV += __ldcg(partials + 4 * b + 2); sM = fmax(sM, __ldcg(partials + 4 * b + 3));
-    }
-    const double tP = bsum(sP, sh), tF = bsum(sF, sh), tV = bsum(sV, sh), tM = bmax(sM, sh);
-    if (threadIdx.x == 0) {
-        FireState S = *Sp;
-        S.power = tP; S.forceNorm = tF; S.velNorm = tV; S.maxF2 = tM;
-        S.rmsOverN = sqrt(tF) / (double)nV;
-        S.maxForce = sqrt(tM);
-        S.scaling = tF > 0. ? sqrt(tV / tF) : 0.0;
-        S.alphaUsed = S.alpha;
-        S.zeroV = tP > 0 ? 0 : 1;
-        if (tP > 0) {
-            if (S.nSince > S.nMin) {
-                S.dt = fmin(S.dt * S.dtInc, S.dtMax);
-                S.alpha = S.alpha * S.alphaDec;
-                S.alpha = fmax(S.alpha, S.alphaMin);
-            }
-            S.nSince += 1;
-        } else {
-            S.nSince = 0;
-            S.dt = S.dt * S.dtDec;
-            S.dt = fmax(S.dt, S.dtMin);
-            S.alpha = S.alphaStart;
-        }
-        S.iterations += 1;
-        S.pending = 1;
-        const double crit = S.criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
-        if (S.iterations >= S.maxIterations || !(crit > S.cutoff)) S.done = 1;
-        *Sp = S;
-        *ticket = 0u;
-    }
+    fire_reduce_tail<true, true>(Sp, P, FF, VV, nV, partials, ticket, nullptr, sh, amLast);
+}
+
+// fireStep (energyMinimizerFIRE.h:56, fireStepCPU cpp:122-174) on the current forces and
+// velocities: the sums and the control, in blocks of 3 kSlotVerts threads whose first kSlotVerts
+// hold one vertex each, which is k_fire_force's layout, so the sums are bitwise those of a
+// minimize iteration.  With kControl false: the four totals to out4 (gpu_dVec_dot_products).
+template <bool kControl>
+__global__ void __launch_bounds__(3 * kSlotVerts) k_fire_sums(FireState* __restrict__ Sp, int nV,
+                                                              const double4_32a* __restrict__ force,
+                                                              const double4_32a* __restrict__ vel,
+                                                              double* __restrict__ partials,
+                                                              unsigned* __restrict__ ticket, double* __restrict__ out4) {
+    __shared__ double sh[32];
+    __shared__ bool amLast;
+    const int i = blockIdx.x * kSlotVerts + threadIdx.x;
+    double P = 0.0, FF = 0.0, VV = 0.0;
+    if (threadIdx.x < kSlotVerts && i < nV) fire_dots(ld3(force, i), ld3(vel, i), P, FF, VV);
+    fire_reduce_tail<kControl, false>(Sp, P, FF, VV, nV, partials, ticket, out4, sh, amLast);
 }
 
 // Applies a pending FIRE velocity update (after the loop ends).
@@ -310,6 +375,70 @@ int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value
     F->h = S;
     if (iterations) *iterations = S.iterations - it0;
     if (value) *value = criterion == SVM_FIRE_MAX_FORCE ? S.maxForce : S.rmsOverN;
+    return SVM_OK;
+}
+
+// ---- per-phase entry points (the reference's fireStep, velocityVerlet and dot-product launchers)
+
+int svm_fire_step(svm_fire* F) {
+    if (!F || !F->m) return SVM_ERR_ARG;
+    svm_model* m = F->m;
+    if (m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
+    const int nb = (m->nVertices + kSlotVerts - 1) / kSlotVerts;
+    k_fire_sums<true><<<nb, 3 * kSlotVerts, 0, m->stream>>>(F->d, m->nVertices, m->force, m->vel, F->partials,
+                                                            F->ticket, nullptr);
+    k_fire_finish<<<(m->nVertices + kB - 1) / kB, kB, 0, m->stream>>>(F->d, m->vel, m->force, m->nVertices);
+    k_fire_clear_pending<<<1, 1, 0, m->stream>>>(F->d);
+    return check_launch();
+}
+
+int svm_vv_half(svm_model* m, double dt) {
+    if (!m || !(dt == dt) || m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
+    k_vv_half<<<(m->nVertices + kB - 1) / kB, kB, 0, m->stream>>>(m->vel, m->force, m->nVertices, dt);
+    return check_launch();
+}
+
+int svm_velocity_verlet_step(svm_model* m, double dt, int nSteps) {
+    if (!m || !(dt == dt) || nSteps < 0 || m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
+    const int nb = (m->nVertices + kB - 1) / kB;
+    for (int k = 0; k < nSteps; ++k) {
+        {
+            PhaseTimer pt(m, SVM_PHASE_MOVE);
+            k_vv_drift<<<nb, kB, 0, m->stream>>>(m->pos[m->cur], m->vel, m->force, m->nVertices, dt, m->R);
+        }
+        m->cornersValid = false;
+        int rc;
+        if (!m->restricted) {  // moveParticles -> enforceTopology (sphericalVertexModel.cpp:111-148)
+            rc = launch_corners(m, true);
+            if (rc) return rc;
+            rc = launch_t1_apply(m, 0);
+            if (rc) return rc;
+        }
+        rc = launch_geometry(m);  // sim->computeForces(): geometry, then forces
+        if (rc) return rc;
+        {
+            PhaseTimer pt(m, SVM_PHASE_FORCE);
+            rc = launch_force_fp64(m);
+            if (rc) return rc;
+        }
+        k_vv_half<<<nb, kB, 0, m->stream>>>(m->vel, m->force, m->nVertices, dt);
+        if (check_launch()) return SVM_ERR_CUDA;
+    }
+    return SVM_OK;
+}
+
+int svm_reduce_dots(svm_model* m, double* out4) {
+    if (!m || !out4 || m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
+    const int nb = (m->nVertices + kSlotVerts - 1) / kSlotVerts;
+    if (!m->dotPartials && cudaMalloc(&m->dotPartials, sizeof(double) * 4 * (size_t)(nb + 1)) != cudaSuccess)
+        return SVM_ERR_CUDA;
+    k_fire_sums<false><<<nb, 3 * kSlotVerts, 0, m->stream>>>(nullptr, m->nVertices, m->force, m->vel, m->dotPartials,
+                                                             m->ticket + 3, m->scalars + 8);
+    if (check_launch()) return SVM_ERR_CUDA;
+    double r[4];
+    if (cudaMemcpyAsync(r, m->scalars + 8, sizeof(r), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    out4[0] = r[0]; out4[1] = r[1]; out4[2] = r[2]; out4[3] = sqrt(r[3]);
     return SVM_OK;
 }
 

@@ -378,6 +378,7 @@ struct svm_model {
     double* dispBuf = nullptr;         // [3*Nv]
     // reductions: per-block partials + ticket (last-block-done pattern)
     double* partials = nullptr;
+    double* dotPartials = nullptr;     // svm_reduce_dots: 4 per block of 64 vertices (allocated on first use)
     unsigned* ticket = nullptr;
     double* scalars = nullptr;         // [0] total area, [1] excess, [2] energy ...
     int* fallbackFlag = nullptr;

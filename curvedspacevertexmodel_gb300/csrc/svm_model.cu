@@ -2118,7 +2118,7 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
                     m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->dap32, m->repR, m->repNp, m->repCellOff,
                     m->repVertOff, m->t1.clocks,
-                    m->repFlag, m->repScal};
+                    m->repFlag, m->repScal, m->dotPartials};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
     for (auto& g : m->ioGraph)

@@ -5,6 +5,10 @@
 // With "batch" as the first argument it runs replicas of sizes N, 2N, 3N (seeds seed, seed+1,
 // seed+2; temperatures T, 2T, 3T) as one sphericalVertexModelBatch and prints each replica's
 // energy:  sphericalVertex_gpu batch [N] [iterations] [T] [p0] [dt] [seed]
+//
+// With "fire" it relaxes a stabilised model by FIRE driven phase by phase, as minimize does
+// (velocityVerlet step at the minimizer's dt, then fireStep), and prints the energy and the dot
+// products:  sphericalVertex_gpu fire [N] [iterations] [seed]
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -79,8 +83,45 @@ static int run_active(int argc, char** argv) {
     return 0;
 }
 
+// "fire N iterations seed": 50 stabilisation steps (T = 0, p0 = 1), then p0 = 3.8 and FIRE
+// (dt 0.01, alpha0 0.1, dtMax 0.1, finc 1.1, fdec 0.5, alphaDec 0.9, NMin 5) driven phase by phase.
+static int run_fire(int argc, char** argv) {
+    const int N = argc > 2 ? std::atoi(argv[2]) : 200;
+    const int iterations = argc > 3 ? std::atoi(argv[3]) : 100;
+    const int seed = argc > 4 ? std::atoi(argv[4]) : 1137;
+    try {
+        noiseSource noise(true);
+        noise.setReproducibleSeed(seed);
+        auto model = std::make_shared<sphericalVertexModel>(N, noise, 1.0, 1.0, true, false);
+        model->setT1Threshold(0.04);
+        auto BD = std::make_shared<brownianDynamics>(true);
+        BD->noise.setReproducibleSeed(seed + 1);
+        BD->setModel(model);
+        for (int i = 0; i < 50; ++i) BD->performUpdate();
+        model->setPreferredParameters(1.0, 3.8);
+        energyMinimizerFIRE fire(model);
+        fire.setFIREParameters(0.01, 0.1, 0.1, 1.1, 0.5, 0.9, 5, 1e-300, 0.0);
+        fire.setMaximumIterations(iterations);
+        model->computeForces();
+        for (int i = 0; i < iterations; ++i) {
+            fire.integrateEquationOfMotion();
+            fire.fireStep();
+        }
+        const std::array<double, 4> d = dotProducts(*model);
+        model->computeGeometry();
+        const double e = model->computeEnergy();
+        std::printf("{\"vertices\": %d, \"energy\": %.17g, \"dots\": [%.17g, %.17g, %.17g, %.17g]}\n",
+                    model->getNumberOfParticles(), e, d[0], d[1], d[2], d[3]);
+    } catch (const std::exception& ex) {
+        std::fprintf(stderr, "error: %s\n", ex.what());
+        return 1;
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc > 1 && std::string(argv[1]) == "batch") return run_batch(argc, argv);
+    if (argc > 1 && std::string(argv[1]) == "fire") return run_fire(argc, argv);
     if (argc > 1 && std::string(argv[1]) == "active") return run_active(argc, argv);
     const int N = argc > 1 ? std::atoi(argv[1]) : 200;
     const int iterations = argc > 2 ? std::atoi(argv[2]) : 100;

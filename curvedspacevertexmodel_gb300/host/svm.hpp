@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <iostream>
+#include <array>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -349,6 +350,25 @@ class neighborList {
     svm_neighbor_list* nl = nullptr;
 };
 
+// velocityVerlet (src/updaters/velocityVerlet.{h,cpp}), unit masses: per step the displacement
+// dt v + dt^2/2 F with the first half kick, the move (T1 flips unless motion is restricted),
+// geometry and forces, the second half kick.  Forces must be current before the first step.
+class velocityVerlet : public updater {
+  public:
+    void performUpdate() override { integrateEquationOfMotion(); }
+    void integrateEquationOfMotion() { check(svm_velocity_verlet_step(model->h(), deltaT, 1), "velocity Verlet"); }
+    // gpu_update_velocity (velocityVerlet.cuh:14-19): v += dt/2 F
+    void updateVelocity() { check(svm_vv_half(model->h(), deltaT), "velocity half kick"); }
+};
+
+// gpu_dVec_dot_products (src/utilities/utilities.cuh:74) over the model's forces and velocities:
+// {sum F.v, sum F.F, sum v.v, max |F|}
+inline std::array<double, 4> dotProducts(sphericalVertexModel& m) {
+    std::array<double, 4> out{};
+    check(svm_reduce_dots(m.h(), out.data()), "dot products");
+    return out;
+}
+
 // energyMinimizerFIRE (src/updaters/energyMinimizerFIRE.h:27-68)
 class energyMinimizerFIRE : public updater {
   public:
@@ -369,6 +389,15 @@ class energyMinimizerFIRE : public updater {
         int it = 0;
         double v = 0;
         check(svm_fire_minimize(f, criterion, &it, &v), "minimize");
+    }
+    // fireStep (energyMinimizerFIRE.h:56): sums, velocity update and dt/alpha control on the current
+    // forces and velocities; integrateEquationOfMotion is the velocity-Verlet step at the current dt
+    void fireStep() { ensure(); check(svm_fire_step(f), "fireStep"); }
+    void integrateEquationOfMotion() {
+        double s[7];
+        ensure();
+        check(svm_fire_state(f, s), "state");
+        check(svm_velocity_verlet_step(model->h(), s[0], 1), "velocity Verlet");
     }
     scalar getMaxForce() { double s[7]; ensure(); check(svm_fire_state(f, s), "state"); return s[3]; }
     int getCurrentIterations() { double s[7]; ensure(); check(svm_fire_state(f, s), "state"); return (int)s[6]; }

@@ -567,6 +567,43 @@ class brownianDynamics:
         call("svm_brownian_run", self.model.handle, self.temperature, self.deltaT, self.mu, self._seed(), int(nSteps))
 
 
+class velocityVerlet:
+    """Velocity-Verlet updater (src/updaters/velocityVerlet.{h,cpp}) with unit masses: per step,
+    disp = dt v + dt^2/2 F and v += dt/2 F, the move (with T1 flips unless motion is restricted),
+    geometry and forces, v += dt/2 F.  Forces must be current before the first step, as in the
+    reference (computeForces)."""
+
+    def __init__(self):
+        self.deltaT = 0.01
+        self.model: sphericalVertexModel | None = None
+
+    def setModel(self, model: sphericalVertexModel):
+        self.model = model
+
+    def setDeltaT(self, dt: float):
+        self.deltaT = float(dt)
+
+    def integrateEquationOfMotion(self):
+        call("svm_velocity_verlet_step", self.model.handle, self.deltaT, 1)
+
+    performUpdate = integrateEquationOfMotion
+
+    def run(self, nSteps: int):
+        call("svm_velocity_verlet_step", self.model.handle, self.deltaT, int(nSteps))
+
+    def halfKick(self):
+        """gpu_update_velocity (velocityVerlet.cuh:14-19): v += dt/2 F."""
+        call("svm_vv_half", self.model.handle, self.deltaT)
+
+
+def dotProducts(model: sphericalVertexModel) -> dict:
+    """gpu_dVec_dot_products (utilities.cuh:74) over the model's forces and velocities: sum F.v,
+    sum F.F, sum v.v and max |F|."""
+    out = np.empty(4)
+    call("svm_reduce_dots", model.handle, out)
+    return dict(power=out[0], force_norm2=out[1], velocity_norm2=out[2], max_force=out[3])
+
+
 class energyMinimizerFIRE:
     """FIRE minimiser (energyMinimizerFIRE.h:27-68) with device-side control."""
 
@@ -626,6 +663,18 @@ class energyMinimizerFIRE:
         call("svm_fire_state", self._h, out)
         return dict(dt=out[0], alpha=out[1], power=out[2], force_rms_over_n=out[3], max_force=out[4],
                     n_since=int(out[5]), iterations=int(out[6]))
+
+    def fireStep(self):
+        """fireStep (energyMinimizerFIRE.h:56): the sums, velocity update and dt/alpha control on
+        the model's current forces and velocities (no integration; minimize pairs it with a
+        velocity-Verlet step at the current dt)."""
+        self._ensure()
+        call("svm_fire_step", self._h)
+
+    def integrateEquationOfMotion(self):
+        """One velocity-Verlet step at the minimizer's current dt (energyMinimizerFIRE inherits
+        velocityVerlet::integrateEquationOfMotion)."""
+        call("svm_velocity_verlet_step", self.model.handle, self.state()["dt"], 1)
 
     def getMaxForce(self) -> float:
         return self.state()["force_rms_over_n"]

@@ -290,6 +290,29 @@ int svm_fire_set_max_iterations(svm_fire* f, int maxIterations);
 /* state: dt, alpha, power, rms_over_n, max_force, n_since, iterations (7 doubles). */
 int svm_fire_state(svm_fire* f, double* state7);
 
+/* ---- per-phase FIRE and velocity Verlet ------------------------------------------------------
+ * The pieces minimize strings together, for callers that drive their own loop.  All run on the
+ * model's stream in the FP64 forms (SVM_ERR_ARG in the mixed form); masses are 1, as the model's are.
+ *
+ * fireStep (src/updaters/energyMinimizerFIRE.h:56, fireStepCPU energyMinimizerFIRE.cpp:122-174):
+ * on the model's current forces and velocities, P = sum F.v, |F|^2, |v|^2 and max |F|; the velocity
+ * update v <- (1 - alpha) v + alpha |v|/|F| F (v <- 0 when P <= 0) and the dt / alpha adaptation.
+ * The sums run in the same blocks and order as a minimize iteration's, so a loop of
+ * svm_velocity_verlet_step(m, dt, 1) with dt = state[0] and svm_fire_step equals minimize bit for
+ * bit; like fireStep it does not count an iteration (minimize does, cpp:191). */
+int svm_fire_step(svm_fire* f);
+/* velocityVerlet::integrateEquationOfMotion (src/updaters/velocityVerlet.cpp:40-59, CPU 6-38),
+ * nSteps times: disp = dt v + (dt^2 / 2) F and v += (dt / 2) F (gpu_displacement_velocity_verlet,
+ * velocityVerlet.cuh:21-28), the move onto the sphere with T1 flips unless motion is restricted
+ * (moveParticles), geometry and forces (sim->computeForces), v += (dt / 2) F (gpu_update_velocity).
+ * Forces must be current on entry (svm_model_compute_forces), as in the reference. */
+int svm_velocity_verlet_step(svm_model* m, double dt, int nSteps);
+/* gpu_update_velocity (src/updaters/velocityVerlet.cuh:14-19): v += (dt / 2) F / m. */
+int svm_vv_half(svm_model* m, double dt);
+/* gpu_dVec_dot_products (src/utilities/utilities.cuh:74) over the model's forces F and velocities v:
+ * out4 = (sum F.v, sum F.F, sum v.v, max |F|), block sums in a fixed order; synchronises. */
+int svm_reduce_dots(svm_model* m, double* out4);
+
 /* ---- cell list -----------------------------------------------------------------------------
  * hyperrectangularCellList (src/utilities/hyperrectangularCellList.{h,cpp}): cubic grid over
  * [-radius, radius]^3 with side count floor(2 radius / a) made even, bin_d = floor((x_d +

@@ -95,6 +95,8 @@ def orc_lib():
         _sig(lib, "orc_fire_minimize", C.c_int, vp, vp, C.c_int)
         _sig(lib, "orc_fire_iterate", None, vp, vp, C.c_int)
         _sig(lib, "orc_fire_state", None, vp, _dp)
+        _sig(lib, "orc_vv_step", None, vp, C.c_double)
+        _sig(lib, "orc_fire_step", None, vp, vp)
         _sig(lib, "orc_cell_list_dims", C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double))
         _sig(lib, "orc_cell_list", C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int), _ip, _up, _ip, C.c_long)
         _sig(lib, "orc_set_portable_acos", None, C.c_int)
@@ -301,11 +303,20 @@ class OracleFire:
     def iterate(self, model: OracleModel, count: int):
         self.lib.orc_fire_iterate(model.h, self.h, count)
 
+    def fire_step(self, model: OracleModel):
+        """fireStepCPU alone (no integration, no iteration count)."""
+        self.lib.orc_fire_step(model.h, self.h)
+
     def state(self):
         out = np.empty(7, dtype=np.float64)
         self.lib.orc_fire_state(self.h, out)
         return dict(dt=out[0], alpha=out[1], power=out[2], force_rms_over_n=out[3], max_force=out[4],
                     n_since=int(out[5]), iterations=int(out[6]))
+
+
+def vv_step(model: OracleModel, dt: float) -> None:
+    """velocityVerlet::integrateEOMCPU at dt (forces must be current)."""
+    orc_lib().orc_vv_step(model.h, dt)
 
 
 def oracle_cell_list(points, a, radius, nmax=2):

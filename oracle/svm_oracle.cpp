@@ -814,6 +814,9 @@ int orc_fire_minimize(orc_model* m, orc_fire* f, int criterion) {
     }
     return done;
 }
+// The pieces of an iteration on their own: velocityVerlet::integrateEOMCPU at dt, and fireStepCPU.
+void orc_vv_step(orc_model* m, double dt) { vvStep(m, dt); }
+void orc_fire_step(orc_model* m, orc_fire* f) { fireStep(m, f); }
 // One VV + FIRE iteration without the stopping test (forces must be current).
 void orc_fire_iterate(orc_model* m, orc_fire* f, int count) {
     for (int k = 0; k < count; ++k) { f->iterations += 1; vvStep(m, f->deltaT); fireStep(m, f); }

@@ -96,3 +96,34 @@ def test_cpp_vicsek_and_neighbour_list_match_python_classes(svm):
     assert cpp["pairs"] == int(nl.neighborsPerParticle.sum())
     assert cpp["index_sum"] == int(nl.particleIndices.astype(np.int64).sum())
     nl.close()
+
+
+def test_cpp_fire_phases_match_python_classes(svm):
+    """FIRE driven phase by phase through the C++ classes (velocityVerlet step + fireStep, then the
+    dot products) and through the Python classes: the same energy and sums, bit for bit."""
+    exe = os.path.join(os.path.dirname(svm.__file__), "sphericalVertex_gpu")
+    N, iters, seed = 250, 60, 13
+    out = subprocess.run([exe, "fire", str(N), str(iters), str(seed)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    cpp = json.loads(out.stdout.strip().splitlines()[-1])
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(seed)
+    m = svm.sphericalVertexModel(N, noise, 1.0, 1.0)
+    m.setT1Threshold(0.04)
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.noise.setReproducibleSeed(seed + 1)
+    for _ in range(50):
+        bd.integrateEquationOfMotion()
+    m.setPreferredParameters(1.0, 3.8)
+    fire = svm.energyMinimizerFIRE(m)
+    fire.setFIREParameters(0.01, 0.1, 0.1, 1.1, 0.5, 0.9, 5, 1e-300, 0.0)
+    fire.setMaximumIterations(iters)
+    m.computeForces()
+    for _ in range(iters):
+        fire.integrateEquationOfMotion()
+        fire.fireStep()
+    d = svm.dotProducts(m)
+    m.computeGeometry()
+    assert cpp["energy"] == m.computeEnergy()
+    assert cpp["dots"] == [d["power"], d["force_norm2"], d["velocity_norm2"], d["max_force"]]
