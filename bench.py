@@ -28,6 +28,17 @@ every replica.  Under torchrun only rank 0 runs it.
 
 N > 1 GPUs: independent replicas, one per GPU (scaling "weak"); a barrier and the max over ranks
 of the timed region, value = all vertex-steps / that time.
+
+Other workloads (off by default, one JSON line each; --mode):
+  forms    the FP64 plain form against the FP32-bulk/FP64-area form over --steps (default 10,000)
+           steps at N = 100k with the same injected noise: energy, area and perimeter errors, T1-set
+           agreement, time-averaged energies with their standard errors, and each form's GB/s;
+  large    N = 1M cells: --steps (default 5,000) mixed-form Brownian steps with the HBM fraction of
+           the step, then FIRE to max|F| < 1e-8, plain and from the learned warm start;
+  batch    512 replicas for --steps (default 10,000) batched steps, and per-replica energy errors of
+           a 32-replica subset against FP64 single-sphere runs (same state, and time averages);
+  profile  a small untimed run for profilers (ncu -k ...): --cells, --stab, --steps, --equil and
+           the options --mixed, --replicas, --fire, --neighbors, --sub-grid, --active, --dynamics.
 """
 from __future__ import annotations
 
@@ -38,6 +49,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -54,6 +66,14 @@ WORKLOAD = ("spherical vertex model, overdamped Brownian step, FP64 plain form, 
             "seeded Voronoi start")
 METRIC = "vertex-steps/s at N=100k (FP64 Brownian step)"
 UNIT = "vertex-steps/s"
+
+
+def config_of(args, n_vertices, parallelism):
+    """The workload's config, the same for both arms except `parallelism`."""
+    return {"workload": WORKLOAD, "n_cells": args.cells, "n_vertices": n_vertices,
+            "stabilisation_steps": args.stab, "equilibration_steps": args.equil,
+            "l2": "GPU arm: flushed before every timed step (512 MB write); state is ~40 MB < 129 MB L2",
+            "parallelism": parallelism}
 
 
 def dist_env():
@@ -82,11 +102,11 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        self.dir = tempfile.mkdtemp(prefix="svm_bench_clocks_")
+        self.path = os.path.join(self.dir, f"clocks_rank{gpu_index}.csv")
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
@@ -121,6 +141,8 @@ class ClockSampler:
             for n, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
+        import shutil
+        shutil.rmtree(self.dir, ignore_errors=True)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
@@ -326,16 +348,15 @@ def run_ours(args):
         v, secs = cpu_baseline_sample(cpu_state, args.cpu_steps)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{args.cpu_steps} Brownian steps of the same N=100k workload from the same equilibrated "
-                         f"state on one host core ({secs:.1f} s), the reference's serial CPU path restated"}
+                         f"state on one host core ({secs:.1f} s), the reference's serial CPU path restated (bit for "
+                         f"bit the reference build's trajectory; the build runs {PORT_TIME_OVER_REFERENCE_BUILD}x "
+                         f"faster per step on an x86-64 core)"}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cell centres, reference init recipe)",
-        "config": {"workload": WORKLOAD, "n_cells": nc, "n_vertices": nv, "stabilisation_steps": args.stab,
-                   "equilibration_steps": args.equil,
-                   "l2": "flushed before every timed step (512 MB write); state is ~40 MB < 129 MB L2",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single sphere, one GPU",
-                   "noise": "in-kernel Philox4x32-10"},
+        "config": config_of(args, nv, f"replicas x{world}" if world > 1 else "single sphere, one GPU"),
+        "noise": "in-kernel Philox4x32-10 with ziggurat normals",
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * nv, "d2h_bytes_per_step": 24 * nv + 8,
                 "area_fallback_steps": fallbacks_e2e},
         # steps whose total-area check failed (a near-degenerate corner's angle wrapped by 2 pi) and
@@ -505,7 +526,14 @@ def _lib_phase_count():
 
 
 # --------------------------------------------------------------------------------------------
-def _ref_worker(idx, n, steps, warmup, stab, barrier, q):
+# The CPU restatement of the reference path (oracle/, bit for bit the reference's own build on the
+# same inputs) against that build, on one core of an x86-64 host, timed in lockstep on the identical
+# N = 20k trajectory (the build cannot run here: it is compiled from the reference's sources, which
+# only the development host has): the restatement takes 1.15x the reference build's time per step.
+PORT_TIME_OVER_REFERENCE_BUILD = 1.15
+
+
+def _ref_worker(idx, n, steps, warmup, stab, equil, barrier, q):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle
@@ -513,21 +541,23 @@ def _ref_worker(idx, n, steps, warmup, stab, barrier, q):
     pts = oracle.OracleNoise(SEED + idx).cell_centres(n)
     t = otopo.topology(pts)
     m = oracle.OracleModel(t["pos"], t["rings"], t["counts"], t["vcells"], t["vnbrs"], math.sqrt(n / (4 * math.pi)))
-    m.set_preferred(PARAMS["a0"], PARAMS["p0"])
     m.set_kr(PARAMS["kr"])
     m.set_t1_threshold(PARAMS["t1"])
     noise = oracle.OracleNoise(BD_SEED + idx)
-    m.set_preferred(PARAMS["a0"], 1.0)  # the reference driver's stabilisation (sphericalVertex.cpp:106-115)
+    # the preparation of the GPU arm (the reference driver's, sphericalVertex.cpp:104-125): stab steps
+    # at T = 0 with P0 = 1, then equil steps at the run parameters, then the warm-up steps
+    m.set_preferred(PARAMS["a0"], 1.0)
     for _ in range(stab):
         m.brownian_step(noise, 0.0, PARAMS["dt"], PARAMS["mu"])
     m.set_preferred(PARAMS["a0"], PARAMS["p0"])
-    for _ in range(warmup):
+    for _ in range(equil + warmup):
         m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])
+    f0 = m.fallback_count()
     barrier.wait()
     for _ in range(steps):
         m.brownian_step(noise, PARAMS["T"], PARAMS["dt"], PARAMS["mu"])
         barrier.wait()
-    q.put(int(np.asarray(m.positions()).shape[0]))
+    q.put((int(np.asarray(m.positions()).shape[0]), m.fallback_count() - f0))
 
 
 def run_reference(args):
@@ -542,56 +572,531 @@ def run_reference(args):
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(cores + 1)
     q = ctx.Queue()
-    procs = [ctx.Process(target=_ref_worker, args=(i, args.cells, args.steps, args.warmup, args.ref_stab, barrier, q))
+    procs = [ctx.Process(target=_ref_worker, args=(i, args.cells, args.steps, args.warmup, args.stab, args.equil,
+                                                   barrier, q))
              for i in range(cores)]
     for p in procs:
         p.start()
-    barrier.wait()  # all replicas built and warmed up
+    barrier.wait()  # all replicas built, prepared and warmed up
     t0 = time.perf_counter()
     for _ in range(args.steps):
         barrier.wait()
     dt = time.perf_counter() - t0
-    nvs = [q.get() for _ in procs]
+    res = [q.get() for _ in procs]
     for p in procs:
         p.join()
+    nvs = [r[0] for r in res]
     value = sum(nvs) * args.steps / dt
-    sample = (f"{cores} independent replicas (one per host core) of the N=100k workload, each bench step one "
-              f"Brownian timestep of every replica; CPU restatement of the reference path (-O3)")
+    sample = (f"{cores} independent replicas (one per host core) of the N=100k workload, each prepared as the GPU "
+              f"arm ({args.stab} stabilisation + {args.equil} equilibration steps), each bench step one Brownian "
+              f"timestep of every replica; CPU restatement of the reference path (-O3), bit for bit the reference "
+              f"build's trajectory, which runs {PORT_TIME_OVER_REFERENCE_BUILD}x faster per step on an x86-64 core")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded cell centres, reference init recipe)",
-        "config": {"workload": WORKLOAD, "n_cells": args.cells, "n_vertices": nvs[0] if nvs else None,
-                   "parallelism": f"{cores} host processes"},
+        "config": config_of(args, nvs[0] if nvs else None, f"{cores} host processes"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "area_fallback_steps": int(sum(r[1] for r in res)),
+        "area_fallback_note": "replica-steps of the timed region whose total-area check took the triangle fan",
+        "port_time_over_reference_build": PORT_TIME_OVER_REFERENCE_BUILD,
+        "value_at_reference_build_speed": value * PORT_TIME_OVER_REFERENCE_BUILD,
     }
     print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------------------------------------
+# Other workloads (--mode): each prints one JSON line.
+
+def _prepared_model(svm, n, seed, stab, equil, p0=PARAMS["p0"], T=PARAMS["T"]):
+    """A seeded model prepared with the reference driver's recipe: stab steps at T = 0 with P0 = 1,
+    then equil graph-replayed steps at (P0, T)."""
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(seed)
+    m = svm.sphericalVertexModel(n, noise, PARAMS["a0"], p0)
+    m.setT1Threshold(PARAMS["t1"])
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.setDeltaT(PARAMS["dt"])
+    bd.noise.setReproducibleSeed(seed + 1)
+    bd.setT(0.0)
+    m.setPreferredParameters(PARAMS["a0"], 1.0)
+    if stab:
+        bd.run(stab)
+    bd.setT(T)
+    m.setPreferredParameters(PARAMS["a0"], p0)
+    if equil:
+        bd.run(equil)
+    return m, bd
+
+
+def _timed_run(m, bd, steps):
+    """Milliseconds per step of `steps` graph-replayed steps, CUDA events on the model's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(m.streamHandle())
+    bd.run(steps)  # capture outside the timed region
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bd.run(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _mean_se(x):
+    """Mean and standard error of a series of (block) averages."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.float64)
+    return float(x.mean()), float(x.std(ddof=1) / math.sqrt(len(x))) if len(x) > 1 else float("nan")
+
+
+def mode_forms(args):
+    """The FP64 plain form against the FP32-bulk/FP64-area form at N = 100k over args.steps steps.
+    Both start from the same FP32-representable prepared state and are driven by the same host
+    normals (injected each step), so they differ only by arithmetic.  At every args.every steps:
+    energy per cell in each form, their relative difference, area and perimeter differences (cells
+    matched by index), the fraction of vertices whose neighbours agree, and the T1 flips of the
+    interval in both forms with how many coincide (same edge, same 200-step window).  The summary
+    gives time-averaged energies per cell over the checkpoints after the first with their standard
+    errors (the forms separate chaotically, so only statistics can be compared), and each form's
+    step time and GB/s (algorithmic bytes: 94 B per vertex-step FP64, 70 B mixed) from graph-replayed
+    steps timed with CUDA events."""
+    import numpy as np
+    import curvedspacevertexmodel_gb300 as svm
+    a, _ = _prepared_model(svm, args.cells, SEED, args.stab, args.equil)
+    st = a.saveState()
+    st["pos"] = st["pos"].astype(np.float32).astype(np.float64)
+    a.loadState(st)
+    nb = svm.noiseSource()
+    nb.setReproducibleSeed(SEED)
+    b = svm.sphericalVertexModel(args.cells, nb, radius=a.radius)
+    b.setT1Threshold(PARAMS["t1"])
+    b.loadState(st)
+    b.setPreferredParameters(PARAMS["a0"], PARAMS["p0"])
+    b.precision = "mixed"
+    bda, bdb = svm.brownianDynamics(), svm.brownianDynamics()
+    for bd, m in ((bda, a), (bdb, b)):
+        bd.setModel(m)
+        bd.setT(PARAMS["T"])
+        bd.setDeltaT(PARAMS["dt"])
+    rng = np.random.default_rng(SEED + 7)
+    a.takeFlips()
+    b.takeFlips()
+    nfa = nfb = ncommon = 0
+    rows = []
+    for step in range(1, args.steps + 1):
+        xi = rng.standard_normal((a.nVertices, 3))
+        for bd in (bda, bdb):
+            bd.injectNoise(xi)
+            bd.integrateEquationOfMotion()
+        if step % 200 == 0 or step % args.every == 0:  # the flip logs hold 65,536 flips
+            fa, fb = a.takeFlips(), b.takeFlips()
+            nfa += len(fa)
+            nfb += len(fb)
+            ncommon += len(set(map(tuple, fa)) & set(map(tuple, fb)))
+        if step % args.every == 0:
+            a.computeGeometry()
+            b.computeGeometry()
+            ea, eb = a.computeEnergy() / a.nCells, b.computeEnergy() / b.nCells
+            apa, apb = a.areaPerimeter(), b.areaPerimeter()
+            same_nb = np.mean(np.all(np.sort(a.vertexNeighbors(), 1) == np.sort(b.vertexNeighbors(), 1), 1))
+            rows.append({"step": step, "energy_per_cell_fp64": ea, "energy_per_cell_mixed": eb,
+                         "energy_rel_diff": abs(ea - eb) / ea,
+                         "area_abs_diff_median_max": [float(np.median(np.abs(apa[:, 0] - apb[:, 0]))),
+                                                      float(np.max(np.abs(apa[:, 0] - apb[:, 0])))],
+                         "perimeter_abs_diff_median_max": [float(np.median(np.abs(apa[:, 1] - apb[:, 1]))),
+                                                           float(np.max(np.abs(apa[:, 1] - apb[:, 1])))],
+                         "same_neighbour_fraction": float(same_nb), "flips_fp64": nfa, "flips_mixed": nfb,
+                         "flips_common": ncommon})
+            nfa = nfb = ncommon = 0
+    peak, peak_kind = peaks()
+    ms64 = _timed_run(a, bda, 50)
+    ms32 = _timed_run(b, bdb, 50)
+    later = rows[1:] if len(rows) > 2 else rows
+    m64, se64 = _mean_se([r["energy_per_cell_fp64"] for r in later])
+    m32, se32 = _mean_se([r["energy_per_cell_mixed"] for r in later])
+    nv = a.nVertices
+    out = {"mode": "forms", "workload": f"N={args.cells}, FP64 plain vs FP32-bulk/FP64-area, {args.steps} steps, "
+                                        f"same injected normals, A0=1 P0=3.8 T=0.01 dt=0.01 T1 0.04",
+           "checkpoints": rows,
+           "time_averaged_energy_per_cell": {"fp64": [m64, se64], "mixed": [m32, se32],
+                                             "difference_over_combined_se": abs(m64 - m32) / math.hypot(se64, se32),
+                                             "relative_difference": abs(m64 - m32) / m64,
+                                             "over": f"checkpoints {later[0]['step']}..{later[-1]['step']}"},
+           "flips_total": {"fp64": sum(r["flips_fp64"] for r in rows), "mixed": sum(r["flips_mixed"] for r in rows),
+                           "common": sum(r["flips_common"] for r in rows)},
+           "step_time": {"fp64_ms": ms64, "mixed_ms": ms32,
+                         "fp64_gbs": 94 * nv / (ms64 * 1e-3) / 1e9, "mixed_gbs": 70 * nv / (ms32 * 1e-3) / 1e9,
+                         "fp64_frac_of_" + peak_kind + "_hbm": 94 * nv / (ms64 * 1e-3) / 1e9 / peak,
+                         "mixed_frac_of_" + peak_kind + "_hbm": 70 * nv / (ms32 * 1e-3) / 1e9 / peak,
+                         "timing": "50 graph-replayed steps, CUDA events, warm L2"},
+           "device_status": [a.deviceStatus(), b.deviceStatus()]}
+    print(json.dumps(out), flush=True)
+
+
+def mode_large(args):
+    """N = 1,000,000 cells (1,999,996 vertices): the reference's initialisation recipe (seeded
+    Voronoi start; args.stab steps at T = 0, P0 = 1), then P0 = 3.75, T = 0.005, dt = 0.01, T1
+    threshold 0.04, args.steps mixed-form Brownian steps (graph-replayed, CUDA events; HBM fraction
+    from the 70 B per vertex-step of the mixed form), then FIRE to max|F| < 1e-8 (FP64 vector-form
+    forces, T1 on), plain and from the learned warm start (fallback to plain FIRE from the start
+    when the warm start raises the energy)."""
+    import numpy as np
+    import torch
+    import curvedspacevertexmodel_gb300 as svm
+    from curvedspacevertexmodel_gb300 import _lib
+    from curvedspacevertexmodel_gb300 import warm_start as ws
+    out = {"mode": "large", "workload": f"N={args.cells}, P0=3.75, T=0.005, dt=0.01, T1 0.04, {args.steps} mixed-form "
+                                        f"Brownian steps, then FIRE to max|F|<1e-8 (FP64 vector form, T1 on), plain "
+                                        f"vs learned warm start"}
+    t0 = time.perf_counter()
+    m, bd = _prepared_model(svm, args.cells, SEED, args.stab, 0, p0=3.75, T=0.005)
+    out["setup_s"] = time.perf_counter() - t0
+    m.precision = "mixed"
+    bd.run(10)
+    m.t1Stats()
+    stream = torch.cuda.ExternalStream(m.streamHandle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    bd.run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    peak, peak_kind = peaks()
+    t1 = m.t1Stats()
+    gbs = 70 * m.nVertices / (ms * 1e-3) / 1e9
+    out["brownian"] = {"ms_per_step": ms, "vertex_steps_per_s": m.nVertices / (ms * 1e-3),
+                       "algorithmic_gbs": gbs, "frac_of_" + peak_kind + "_hbm": gbs / peak,
+                       "t1_flips_per_step": t1["flips"] / args.steps, "device_status": m.deviceStatus(),
+                       "area_fallback_taken_last_step": bool(m.areaCheck()[2])}
+    m.computeGeometry()
+    out["brownian"]["energy_per_cell"] = m.computeEnergy() / m.nCells
+    if args.fire_cap > 0:
+        m.precision = "fp64_vector"
+        start = m.saveState()
+        e_start = ws.energy(m)
+
+        def fire(cap):
+            f = svm.energyMinimizerFIRE(m)
+            prm = list(ws.FIRE_PARAMS)
+            prm[7] = 1e-8
+            f.setFIREParameters(*prm)
+            f.setCriterion(_lib.SVM_FIRE_MAX_FORCE)
+            f.setMaximumIterations(cap)
+            m.synchronize()
+            ts = time.perf_counter()
+            f.minimize()
+            m.synchronize()
+            st = f.state()
+            return st["iterations"], time.perf_counter() - ts, st["max_force"]
+
+        it, secs, fmax = fire(args.fire_cap)
+        out["fire_plain"] = {"iterations": it, "seconds": secs, "max_force": fmax,
+                             "converged": bool(fmax < 1e-8), "energy_per_cell": ws.energy(m) / m.nCells,
+                             "ms_per_iteration": 1e3 * secs / max(1, it), "device_status": m.deviceStatus()}
+        m.loadState(start)
+        net = ws.load(os.path.join(ROOT, "curvedspacevertexmodel_gb300", "data", "warm_start_n20k.npz"))
+        m.synchronize()
+        ts = time.perf_counter()
+        base = net.outputScale
+        net.setOutputScale(0.25 * base)
+        net.warmStart(m)
+        net.setOutputScale(base)
+        e_w = ws.energy(m)
+        fallback = ws.fallback_reason(e_start, e_w)
+        if fallback:
+            m.loadState(start)
+        it_w, _, fmax_w = fire(args.fire_cap)
+        m.synchronize()
+        out["fire_warm"] = {"iterations": it_w, "seconds": time.perf_counter() - ts, "max_force": fmax_w,
+                            "converged": bool(fmax_w < 1e-8), "energy_start": e_start, "energy_after_warm_start": e_w,
+                            "fallback": fallback, "energy_per_cell": ws.energy(m) / m.nCells,
+                            "device_status": m.deviceStatus()}
+        net.close()
+    print(json.dumps(out), flush=True)
+
+
+def _replica_state(b, r):
+    """Replica r of a batch as a single sphere's arrays (indices renumbered from 0)."""
+    import numpy as np
+    cs, vs = b.cellSlice(r), b.vertexSlice(r)
+    rings, counts = b.rings()
+    rr = rings[cs].copy()
+    rr[rr >= 0] -= vs.start
+    return dict(pos=b.returnPositions()[vs], rings=rr, counts=counts[cs],
+                vcells=b.vertexCellNeighbors()[vs] - cs.start, vnbrs=b.vertexNeighbors()[vs] - vs.start)
+
+
+def _single_from_state(svm, st, radius, p0):
+    topo = svm.Topology.from_arrays(st["pos"], st["rings"], st["counts"], st["vcells"], st["vnbrs"])
+    m = svm.sphericalVertexModel(len(st["counts"]), topology=topo, a0=PARAMS["a0"], p0=p0, radius=radius)
+    m.setT1Threshold(PARAMS["t1"])
+    return m
+
+
+def mode_batch(args):
+    """512 replicas (N log-uniform in [100, 5000] cells, P0 U[3.6, 3.95], T logU[1e-4, 1e-1], dt
+    0.01, mixed form, T1 on), prepared like the single sphere (args.stab steps at T = 0, P0 = 1),
+    autotuned, then args.steps batched Brownian steps in graph-replayed chunks timed with CUDA events.
+    Errors against FP64 for a 32-replica subset (every 16th replica):
+    (1) same state: each replica's final state evaluated in FP64 as a single sphere against the
+        batch's mixed-form energy of that state;
+    (2) trajectories: the subset's prepared states as a batch of their own (mixed form) and as 32 FP64
+        single spheres, all driven by the same injected normals for args.compare_steps steps; the
+        relative energy-per-cell difference at checkpoints (the forms separate by FP32 rounding,
+        amplified along the trajectory)."""
+    import numpy as np
+    import torch
+    import curvedspacevertexmodel_gb300 as svm
+    rng = np.random.default_rng(BATCH_SEED)
+    n_rep = args.replicas
+    sizes = np.exp(rng.uniform(np.log(100), np.log(5000), n_rep)).astype(int)
+    p0s = rng.uniform(3.6, 3.95, n_rep)
+    temps = np.exp(rng.uniform(np.log(1e-4), np.log(1e-1), n_rep))
+    seeds = BATCH_SEED + 1000 + np.arange(n_rep)
+    b = svm.sphericalVertexModelBatch(sizes, seeds, p0=1.0)
+    b.setT1Threshold(PARAMS["t1"])
+    bd = svm.brownianDynamics()
+    bd.setModel(b)
+    bd.setDeltaT(PARAMS["dt"])
+    bd.noise.setReproducibleSeed(BATCH_SEED + 7)
+    b.setTemperatures(np.zeros(n_rep))
+    bd.run(args.stab)
+    b.setPreferredParameters(PARAMS["a0"], p0s)
+    b.setTemperatures(temps)
+    subset = list(range(0, n_rep, max(1, n_rep // 32)))[:32]
+    starts = [_replica_state(b, r) for r in subset]
+    b.autotune(64, 1024, 64, 3, 100000)
+    bd.run(100)  # tuner sampling; these steps count towards the run
+    chunk = max(1, min(1000, (args.steps - 100) // 10))
+    bd.run(chunk)  # graph capture
+    n_chunks = max(1, (args.steps - 100 - chunk) // chunk)
+    stream = torch.cuda.ExternalStream(b.streamHandle())
+    b.t1Stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(n_chunks):
+        bd.run(chunk)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / (chunk * n_chunks)
+    steps_done = 100 + chunk * (n_chunks + 1)
+    t1 = b.t1Stats()
+    b.computeGeometry()
+    final_mixed = b.replicaEnergies()
+    same = []
+    for r in subset:
+        s1 = _single_from_state(svm, _replica_state(b, r), float(b.radii[r]), float(p0s[r]))
+        s1.computeGeometry()
+        e64 = s1.computeEnergy()
+        same.append(abs(final_mixed[r] - e64) / abs(e64))
+        s1.close()
+    status = b.deviceStatus()
+    nv_all = b.nVertices
+    b.close()
+    # (2) the subset from its prepared states: a mixed-form batch and FP64 singles, same normals
+    topo = [svm.Topology.from_arrays(st["pos"], st["rings"], st["counts"], st["vcells"], st["vnbrs"]) for st in starts]
+    sub = svm.sphericalVertexModelBatch(sizes[subset], seeds[subset], p0=1.0, topologies=topo)
+    sub.setT1Threshold(PARAMS["t1"])
+    sub.setPreferredParameters(PARAMS["a0"], p0s[subset])
+    sub.setTemperatures(temps[subset])
+    bds = svm.brownianDynamics()
+    bds.setModel(sub)
+    bds.setDeltaT(PARAMS["dt"])
+    singles, sbd = [], []
+    for k, r in enumerate(subset):
+        m = _single_from_state(svm, starts[k], float(sub.radii[k]), float(p0s[r]))
+        d = svm.brownianDynamics()
+        d.setModel(m)
+        d.setDeltaT(PARAMS["dt"])
+        d.setT(float(temps[r]))
+        singles.append(m)
+        sbd.append(d)
+    nrng = np.random.default_rng(BATCH_SEED + 11)
+    checkpoints = sorted({c for c in (10, 100, 1000, args.compare_steps) if c <= args.compare_steps})
+    traj = {}
+    for step in range(1, args.compare_steps + 1):
+        xi = nrng.standard_normal((sub.nVertices, 3))
+        bds.injectNoise(xi)
+        bds.integrateEquationOfMotion()
+        for k in range(len(subset)):
+            sbd[k].injectNoise(xi[sub.vertexSlice(k)])
+            sbd[k].integrateEquationOfMotion()
+        if step in checkpoints:
+            sub.computeGeometry()
+            em = sub.replicaEnergies()
+            rel = []
+            for k, m in enumerate(singles):
+                m.computeGeometry()
+                e64 = m.computeEnergy()
+                rel.append(abs(em[k] - e64) / abs(e64))
+            rel = np.array(rel)
+            traj[str(step)] = {"median": float(np.median(rel)), "q90": float(np.quantile(rel, 0.9)),
+                               "max": float(rel.max())}
+    sub_status = [sub.deviceStatus()] + [m.deviceStatus() for m in singles]
+    for m in singles:
+        m.close()
+    sub.close()
+    same = np.array(same)
+    out = {"mode": "batch", "workload": f"{n_rep} replicas, N log-uniform [100, 5000] cells (total {int(sizes.sum())} "
+                                        f"cells, {nv_all} vertices), P0 U[3.6, 3.95], T logU[1e-4, 1e-1], dt 0.01, "
+                                        f"mixed form, T1 on, {steps_done} steps",
+           "steps": steps_done, "ms_per_step": ms, "value": nv_all / (ms * 1e-3), "unit": UNIT,
+           "t1_flips_per_step": t1["flips"] / (chunk * n_chunks), "device_status": status,
+           "fp64_subset": {"replicas": [int(r) for r in subset],
+                           "same_state_energy_rel_error": {"median": float(np.median(same)),
+                                                           "q90": float(np.quantile(same, 0.9)),
+                                                           "max": float(same.max())},
+                           "trajectory_energy_rel_error_by_step": traj,
+                           "trajectory": f"subset batch (mixed) vs FP64 singles from the prepared states, the same "
+                                         f"injected normals, {args.compare_steps} steps",
+                           "device_status": sub_status}}
+    print(json.dumps(out), flush=True)
+
+
+def mode_profile(args):
+    """A small, untimed run for profilers (e.g. ncu -k regex:k_force_bd): a model of args.cells
+    cells from the seeded recipe, args.stab stabilisation steps (T = 0, P0 = 1) one by one,
+    args.equil graph-replayed steps at the run parameters, then args.steps Brownian steps at
+    T = 0.01, P0 = 3.8 one launch per kernel per step (no graph), and the energy per cell.  --mixed
+    runs those steps in the mixed form; --replicas R runs a batch of R replicas instead
+    (stabilisation, then args.steps steps at per-replica P0 and T); --fire K adds K FIRE iterations
+    (the reference's default parameters, force tolerance 1e-12 so that all K run); --neighbors K,
+    K neighbour-list computations (range 1, radius R + 2.5); --active K, K self-propelled then K
+    Vicsek steps; --dynamics K, K MSD + overlap evaluations (each printing its mean time)."""
+    import numpy as np
+    import curvedspacevertexmodel_gb300 as svm
+    t0 = time.time()
+    if args.replicas:
+        rng = np.random.default_rng(SEED)
+        sizes = np.exp(rng.uniform(np.log(100), np.log(5000), args.replicas)).astype(int)
+        b = svm.sphericalVertexModelBatch(sizes, SEED + np.arange(args.replicas), p0=1.0)
+        b.setT1Threshold(PARAMS["t1"])
+        bd = svm.brownianDynamics()
+        bd.setModel(b)
+        b.setTemperatures(np.zeros(args.replicas))
+        for _ in range(args.stab):
+            bd.integrateEquationOfMotion()
+        b.setPreferredParameters(1.0, rng.uniform(3.6, 3.95, args.replicas))
+        b.setTemperatures(np.exp(rng.uniform(np.log(1e-4), np.log(1e-1), args.replicas)))
+        for _ in range(args.steps):
+            bd.integrateEquationOfMotion()
+        b.computeGeometry()
+        e = b.replicaEnergies() / sizes
+        print(json.dumps({"mode": "profile", "replicas": args.replicas, "cells": b.nCells, "vertices": b.nVertices,
+                          "median_energy_per_cell": float(np.median(e)), "status": b.deviceStatus(),
+                          "wall_s": time.time() - t0}), flush=True)
+        return
+    noise = svm.noiseSource()
+    noise.setReproducibleSeed(SEED)
+    m = svm.sphericalVertexModel(args.cells, noise, 1.0, 3.8)
+    m.setT1Threshold(PARAMS["t1"])
+    bd = svm.brownianDynamics()
+    bd.setModel(m)
+    bd.noise.setReproducibleSeed(SEED + 1)
+    bd.setT(0.0)
+    m.setPreferredParameters(1.0, 1.0)
+    for _ in range(args.stab):
+        bd.integrateEquationOfMotion()
+    bd.setT(PARAMS["T"])
+    m.setPreferredParameters(1.0, 3.8)
+    if args.equil:
+        bd.run(args.equil)
+    if args.mixed:
+        m.precision = "mixed"
+    for _ in range(args.steps):
+        bd.integrateEquationOfMotion()
+    out = {"mode": "profile", "cells": args.cells, "vertices": m.nVertices}
+    if args.fire:
+        fire = svm.energyMinimizerFIRE(m)
+        fire.setMaximumIterations(args.fire)
+        fire.setForceCutoff(1e-12)
+        fire.minimize()
+    if args.dynamics:
+        dyn = svm.dynamicalFeatures(m)
+        dyn._both(0.5)
+        t1 = time.perf_counter()
+        for _ in range(args.dynamics):
+            msd, ov = dyn._both(0.5)
+        out["dynamics_ms_per_evaluation"] = (time.perf_counter() - t1) / args.dynamics * 1e3
+    if args.active:
+        for name, upd in (("self_propelled", svm.sphericalSelfPropelledParticle()),
+                          ("vicsek", svm.sphericalVectorialVicsek())):
+            upd.setModel(m)
+            upd.setDeltaT(0.01)
+            upd.setV0(0.1)
+            if name == "vicsek":
+                upd.setEta(0.5)
+            upd.integrateEquationOfMotion()
+            m.deviceStatus()
+            t1 = time.perf_counter()
+            upd.run(args.active)
+            out[name + "_ms_per_step"] = (time.perf_counter() - t1) / args.active * 1e3
+    if args.neighbors:
+        nl = svm.neighborList(1.0, m.radius + 2.5, args.sub_grid)
+        nl.computeNeighborLists(m, fetch=False)  # sizes the lists
+        t1 = time.perf_counter()
+        for _ in range(args.neighbors):
+            nl.computeNeighborLists(m, fetch=False)
+        out["neighbor_list_ms"] = (time.perf_counter() - t1) / args.neighbors * 1e3
+        out["neighbor_list_nmax"] = nl.Nmax
+        nl.close()
+    m.computeGeometry()
+    out.update(energy_per_cell=m.computeEnergy() / args.cells, status=m.deviceStatus(), wall_s=time.time() - t0)
+    print(json.dumps(out), flush=True)
+
+
+MODE_DEFAULTS = {  # cells, steps, stab, equil, replicas
+    "headline": (N_CELLS, 20, 100, 200, 512),
+    "forms": (N_CELLS, 10000, 100, 200, 0),
+    "large": (1_000_000, 5000, 100, 0, 0),
+    "batch": (0, 10000, 100, 0, 512),
+    "profile": (1_000_000, 1, 2, 0, 0),
+}
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default per mode)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--cells", type=int, default=N_CELLS)
-    ap.add_argument("--stab", type=int, default=100, help="untimed stabilisation steps (T=0, P0=1)")
-    ap.add_argument("--equil", type=int, default=200, help="untimed equilibration steps before warm-up")
+    ap.add_argument("--mode", choices=tuple(MODE_DEFAULTS), default="headline")
+    ap.add_argument("--cells", type=int, default=None)
+    ap.add_argument("--stab", type=int, default=None, help="untimed stabilisation steps (T=0, P0=1)")
+    ap.add_argument("--equil", type=int, default=None, help="untimed equilibration steps before warm-up")
     ap.add_argument("--cpu-steps", type=int, default=25, help="steps of the one-core CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form's secondary timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-replica secondary timing")
-    ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--replicas", type=int, default=None)
     ap.add_argument("--no-fire", action="store_true", help="skip the FIRE warm-start comparison")
     ap.add_argument("--fire-instances", type=int, default=2)
     ap.add_argument("--ref-cores", type=int, default=0)
-    ap.add_argument("--ref-stab", type=int, default=30, help="stabilisation steps of each reference replica")
+    ap.add_argument("--every", type=int, default=1000, help="forms: checkpoint interval")
+    ap.add_argument("--compare-steps", type=int, default=2000, help="batch: steps of the FP64 trajectory comparison")
+    ap.add_argument("--fire-cap", type=int, default=12000, help="large: FIRE iteration cap (0: no FIRE)")
+    ap.add_argument("--mixed", action="store_true", help="profile: the steps in the mixed form")
+    ap.add_argument("--fire", type=int, default=0, help="profile: FIRE iterations after the steps")
+    ap.add_argument("--neighbors", type=int, default=0, help="profile: neighbour-list computations")
+    ap.add_argument("--sub-grid", type=int, default=1, help="profile: the neighbour list's subGridReduction")
+    ap.add_argument("--active", type=int, default=0, help="profile: timed self-propelled and Vicsek steps")
+    ap.add_argument("--dynamics", type=int, default=0, help="profile: timed MSD + overlap evaluations")
     args = ap.parse_args()
+    cells, steps, stab, equil, replicas = MODE_DEFAULTS[args.mode]
+    for k, v in (("cells", cells), ("steps", steps), ("stab", stab), ("equil", equil), ("replicas", replicas)):
+        if getattr(args, k) is None:
+            setattr(args, k, v)
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.mode == "headline":
         run_ours(args)
+    else:
+        {"forms": mode_forms, "large": mode_large, "batch": mode_batch, "profile": mode_profile}[args.mode](args)
 
 
 if __name__ == "__main__":
