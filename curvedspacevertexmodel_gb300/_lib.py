@@ -89,6 +89,8 @@ SIGNATURES = {
     "svm_model_get_area_perimeter": (i32, [vp, dp]),
     "svm_model_get_cell_positions": (i32, [vp, dp]),
     "svm_model_get_rings": (i32, [vp, ip, i32, up]),
+    "svm_model_set_ring_headroom": (i32, [vp, i32]),
+    "svm_model_ring_info": (i32, [vp, ip]),
     "svm_model_get_vertex_cells": (i32, [vp, ip]),
     "svm_model_get_vertex_neighbors": (i32, [vp, ip]),
     "svm_model_status": (i32, [vp, C.POINTER(i32)]),

@@ -340,8 +340,10 @@ int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value
     if (rc) return rc;
     // iterations in captured batches; kernels of a batch after convergence return at once
     const int batch = 32;
-    if (!F->graph || F->graphCriterion != criterion || F->graphIters != batch || F->graphCur != m->cur ||
-        F->graphVersion != m->paramsVersion) {
+    auto ensure_graph = [&]() -> int {
+        if (F->graph && F->graphCriterion == criterion && F->graphIters == batch && F->graphCur == m->cur &&
+            F->graphVersion == m->paramsVersion)
+            return SVM_OK;
         if (F->graph) { cudaGraphExecDestroy(F->graph); F->graph = nullptr; }
         cudaGraph_t g;
         if (cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SVM_ERR_CUDA;
@@ -356,10 +358,14 @@ int svm_fire_minimize(svm_fire* F, int criterion, int* iterations, double* value
         F->graphIters = batch;
         F->graphCur = m->cur;
         F->graphVersion = m->paramsVersion;
-    }
+        return SVM_OK;
+    };
     int* doneHost = nullptr;
     cudaMallocHost(&doneHost, sizeof(int));
     while (true) {
+        // the ring capacity is checked between batches (the host waits for each batch anyway)
+        if (!m->restricted && (rc = ensure_ring_headroom(m))) { cudaFreeHost(doneHost); return rc; }
+        if ((rc = ensure_graph())) { cudaFreeHost(doneHost); return rc; }
         if (cudaGraphLaunch(F->graph, m->stream) != cudaSuccess) { cudaFreeHost(doneHost); return SVM_ERR_CUDA; }
         cudaMemcpyAsync(doneHost, &F->d->done, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
         if (cudaStreamSynchronize(m->stream) != cudaSuccess) { cudaFreeHost(doneHost); return SVM_ERR_CUDA; }

@@ -324,6 +324,18 @@ constexpr int kResFree = 0x7f7f7f7f;
 
 struct svm_model {
     int nCells = 0, nVertices = 0, Wc = 0;
+    // Ring capacity grows as the reference's growCellVerticesList widens its ring storage: the T1
+    // commits keep the largest ring count in ringMax, every T1 pass copies it to the page-locked
+    // ringMaxHost, and before a pass the host grows the capacity whenever ringHeadroom or fewer
+    // slots are free in the largest ring.  passEv: the ends of the last two passes launched outside
+    // a capture (the host waits for the older before the next pass, so its reading is recent).
+    int* ringMax = nullptr;            // device
+    int* ringMaxHost = nullptr;        // page-locked, mapped
+    int* ringMaxHostDev = nullptr;     // its device address
+    int ringHeadroom = 2;
+    int ringGrowths = 0;
+    cudaEvent_t passEv[2] = {nullptr, nullptr};
+    int passSlot = 0;
     double R = 1.0, Kr = 1.0, t1Threshold = 0.1;
     bool restricted = false;
     bool ownStream = false;
@@ -388,6 +400,7 @@ struct svm_model {
     int maxPartialBlocks = 0;
     // graph cache for svm_brownian_run
     cudaGraphExec_t bdGraph = nullptr;
+    cudaEvent_t runEv[2] = {nullptr, nullptr};   // svm_brownian_run: ends of the last two chunks
     double bdT = 0, bdDt = 0, bdMu = 0;
     uint64_t bdSeed = 0;
     int bdGraphCur = -1;
@@ -427,6 +440,8 @@ struct PhaseTimer {
 int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
 int launch_t1_apply(svm_model* m, int bump);
+int grow_rings(svm_model* m, int newCapacity);
+int ensure_ring_headroom(svm_model* m);
 int check_launch();
 // A binned view of device points (svm_celllist.cu): per-bin counts and slots (ascending point
 // index), grid side nside and bin side h over [-radius, radius]^3.

@@ -492,6 +492,8 @@ struct ApplyArgs {
     int* status;
     unsigned long long* stepCounter;
     int bumpStep;
+    int* ringMax;          // largest ring count produced (atomicMax by the commits)
+    int* ringMaxOut;       // host-visible copy, written once per pass by k_t1_patch
 };
 
 __device__ __forceinline__ int& compRef(int4* a, int v, int s) { return reinterpret_cast<int*>(a + v)[s]; }
@@ -576,7 +578,7 @@ struct Ring16 {
     int n;
 };
 __device__ __forceinline__ void ring16_load(const ApplyArgs& A, int cell, Ring16& R) {
-    const int4* q = reinterpret_cast<const int4*>(A.ring + (long)cell * 16);
+    const int4* q = reinterpret_cast<const int4*>(A.ring + (long)cell * A.Wc);
     const int4 a = q[0], b = q[1], c = q[2], d = q[3];
     R.r[0] = a.x; R.r[1] = a.y; R.r[2] = a.z; R.r[3] = a.w; R.r[4] = b.x; R.r[5] = b.y; R.r[6] = b.z; R.r[7] = b.w;
     R.r[8] = c.x; R.r[9] = c.y; R.r[10] = c.z; R.r[11] = c.w; R.r[12] = d.x; R.r[13] = d.y; R.r[14] = d.z; R.r[15] = d.w;
@@ -640,7 +642,9 @@ struct FlipPlan16 {
     Ring16 Rc[3], Rw;              // the rings of v1's three cells and of v2's fourth cell
     int qx, qy, qz;                // which of Rc is cell cs.x, cs.y, cs.z
 };
-__device__ bool t1_plan16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, FlipPlan16& F) {
+// Returns 1 for a planned flip, 0 for none (forbidden, or a broken topology), 2 when a ring
+// involved holds (or would hold) more than 16 entries: then the general path decides.
+__device__ int t1_plan16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, FlipPlan16& F) {
     F.c1 = A.vcell[v1]; F.c2 = A.vcell[v2]; F.n1 = A.vnbr[v1]; F.n2 = A.vnbr[v2];
     const int c[3] = {F.c1.x, F.c1.y, F.c1.z};
     cs.w = -1;
@@ -651,6 +655,7 @@ __device__ bool t1_plan16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs
 #pragma unroll
     for (int q = 0; q < 3; ++q) ring16_load(A, c[q], F.Rc[q]);
     if (cs.w >= 0) ring16_load(A, cs.w, F.Rw);
+    if (F.Rc[0].n > 16 || F.Rc[1].n > 16 || F.Rc[2].n > 16 || (cs.w >= 0 && F.Rw.n > 16)) return 2;
     cs.x = cs.y = cs.z = -1;
     F.qx = F.qy = F.qz = 0;
     int yl = 0, yx = 0;
@@ -662,17 +667,17 @@ __device__ bool t1_plan16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs
         else if (vx == v2) { cs.z = c[q]; F.qz = q; }
         else { cs.y = c[q]; F.qy = q; yl = vl; yx = vx; }
     }
-    if (cs.x < 0 || cs.y < 0 || cs.z < 0 || cs.w < 0) { atomicOr(A.status, SVM_DEV_BAD_TOPOLOGY); return false; }
+    if (cs.x < 0 || cs.y < 0 || cs.z < 0 || cs.w < 0) { atomicOr(A.status, SVM_DEV_BAD_TOPOLOGY); return 0; }
     vs.x = yl; vs.y = yx;
     int vl, vx;
     ring16_neighbours(F.Rw, v2, vl, vx);
     vs.w = vl; vs.z = vx;
     // forbid a T1 that would shrink a triangular cell (sphericalVertexModel.cpp:485-487)
-    if (F.Rc[F.qx].n == 3 || F.Rc[F.qz].n == 3) return false;
-    if (F.Rc[F.qy].n + 1 > 16 || F.Rw.n + 1 > 16) { atomicOr(A.status, SVM_DEV_RING_OVERFLOW); return false; }
+    if (F.Rc[F.qx].n == 3 || F.Rc[F.qz].n == 3) return 0;
+    if (F.Rc[F.qy].n + 1 > 16 || F.Rw.n + 1 > 16) return 2;
     F.ny = A.vnbr[vs.y];
     F.nz = A.vnbr[vs.z];
-    return true;
+    return 1;
 }
 // p1, p2: the old positions of v1 and v2.
 __device__ void t1_commit16(const ApplyArgs& A, int v1, int v2, const int4& cs, const int4& vs, FlipPlan16& F,
@@ -689,9 +694,9 @@ __device__ void t1_commit16(const ApplyArgs& A, int v1, int v2, const int4& cs, 
         undo->vn[0] = F.n1; undo->vn[1] = F.n2; undo->vn[2] = F.ny; undo->vn[3] = F.nz;
         undo->counts[0] = RX.n; undo->counts[1] = RY.n; undo->counts[2] = RZ.n; undo->counts[3] = F.Rw.n;
         ring16_store(undoRings, RX);
-        ring16_store(undoRings + 16, RY);
-        ring16_store(undoRings + 32, RZ);
-        ring16_store(undoRings + 48, F.Rw);
+        ring16_store(undoRings + A.Wc, RY);
+        ring16_store(undoRings + 2 * A.Wc, RZ);
+        ring16_store(undoRings + 3 * A.Wc, F.Rw);
     }
     // the slot rewiring of t1_flip_positions, slot by slot in the same order (for a shared outer
     // neighbour both of its replacements apply, the first one first)
@@ -708,24 +713,30 @@ __device__ void t1_commit16(const ApplyArgs& A, int v1, int v2, const int4& cs, 
     ring16_insert_after(RY, v1, v2);
     ring16_remove(RZ, v1);
     ring16_insert_after(F.Rw, v2, v1);
-    ring16_store(A.ring + (long)cs.x * 16, RX);
-    ring16_store(A.ring + (long)cs.y * 16, RY);
-    ring16_store(A.ring + (long)cs.z * 16, RZ);
-    ring16_store(A.ring + (long)cs.w * 16, F.Rw);
+    ring16_store(A.ring + (long)cs.x * A.Wc, RX);
+    ring16_store(A.ring + (long)cs.y * A.Wc, RY);
+    ring16_store(A.ring + (long)cs.z * A.Wc, RZ);
+    ring16_store(A.ring + (long)cs.w * A.Wc, F.Rw);
     A.ringCount[cs.x] = RX.n; A.ringCount[cs.y] = RY.n; A.ringCount[cs.z] = RZ.n; A.ringCount[cs.w] = F.Rw.n;
+    atomicMax(A.ringMax, RY.n > F.Rw.n ? RY.n : F.Rw.n);
 }
+__device__ bool t1_flip_any(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings);
 __device__ bool t1_flip16(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings) {
     FlipPlan16 F;
-    if (!t1_plan16(A, v1, v2, cs, vs, F)) return false;
+    const int plan = t1_plan16(A, v1, v2, cs, vs, F);
+    if (plan == 2) return t1_flip_any(A, v1, v2, cs, vs, undo, undoRings);
+    if (!plan) return false;
     const D3 p1 = apos(A, v1), p2 = apos(A, v2);
     t1_move_pair(A, v1, v2, p1, p2, apos(A, vs.z));
     t1_commit16(A, v1, v2, cs, vs, F, undo, undoRings, p1, p2);
     return true;
 }
 
-__device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo = nullptr,
-                        int* undoRings = nullptr) {
-    if (A.Wc == 16) return t1_flip16(A, v1, v2, cs, vs, undo, undoRings);
+// The 16-entry fast path reads rings as int4 vectors at stride Wc, so it serves capacities that are
+// multiples of 4 from 16 on (and hands rings of more than 16 entries to the general path).
+__device__ __forceinline__ bool ring16_ok(const ApplyArgs& A) { return A.Wc >= 16 && (A.Wc & 3) == 0; }
+// The general path: any capacity, rings edited in place.
+__device__ bool t1_flip_any(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings) {
     const int c[3] = {A.vcell[v1].x, A.vcell[v1].y, A.vcell[v1].z};
     cs.w = -1;
     for (int ff = 0; ff < 3; ++ff) {
@@ -767,7 +778,13 @@ __device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, 
     ring_insert_after(A, cs.y, v1, v2);
     ring_remove(A, cs.z, v1);
     ring_insert_after(A, cs.w, v2, v1);
+    atomicMax(A.ringMax, max(A.ringCount[cs.y], A.ringCount[cs.w]));
     return true;
+}
+__device__ bool t1_flip(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo = nullptr,
+                        int* undoRings = nullptr) {
+    if (ring16_ok(A)) return t1_flip16(A, v1, v2, cs, vs, undo, undoRings);
+    return t1_flip_any(A, v1, v2, cs, vs, undo, undoRings);
 }
 
 // The rotation and separation of v1 and v2 and the rewiring of the vertex lists
@@ -831,17 +848,17 @@ __device__ __forceinline__ int4 shfl0(int4 a) {
 __device__ bool t1_flip_warp(const ApplyArgs& A, int v1, int v2, int4& cs, int4& vs, UndoEntry* undo, int* undoRings,
                              D3 p1, D3 p2, int lane) {
     int ok = 0;
-    if (A.Wc != 16) {  // other ring capacities: lane 0 alone
-        if (lane == 0) ok = t1_flip(A, v1, v2, cs, vs, undo, undoRings) ? 1 : 0;
+    FlipPlan16 F;
+    if (ring16_ok(A) && lane == 0) ok = t1_plan16(A, v1, v2, cs, vs, F);
+    ok = ring16_ok(A) ? __shfl_sync(kFull, ok, 0) : 2;
+    if (ok == 2) {  // other ring capacities, or rings of more than 16 entries: lane 0 alone
+        if (lane == 0) ok = t1_flip_any(A, v1, v2, cs, vs, undo, undoRings) ? 1 : 0;
         ok = __shfl_sync(kFull, ok, 0);
         cs = shfl0(cs);
         vs = shfl0(vs);
         __syncwarp();
         return ok != 0;
     }
-    FlipPlan16 F;
-    if (lane == 0) ok = t1_plan16(A, v1, v2, cs, vs, F) ? 1 : 0;
-    ok = __shfl_sync(kFull, ok, 0);
     if (!ok) return false;
     cs = shfl0(cs);
     vs = shfl0(vs);
@@ -856,6 +873,10 @@ __device__ bool t1_flip_warp(const ApplyArgs& A, int v1, int v2, int4& cs, int4&
 // position); every written value depends only on the final rings and positions, so duplicate
 // entries and concurrent writers of the same vertex agree.
 __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the pass's largest ring, for the host's capacity check
+        *(volatile int*)A.ringMaxOut = *(volatile int*)A.ringMax;
+        __threadfence_system();
+    }
     const int nt = *(volatile int*)(t1.ctr + 5);
     const long total = (long)nt * A.Wc;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
@@ -1727,6 +1748,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
     A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
+    A.ringMax = m->ringMax; A.ringMaxOut = m->ringMaxHostDev;
     t1_bracket(m->t1Threshold, m->R, &A.cosLo, &A.cosHi);
     t1_sin2_bracket(m->t1Threshold, m->R, &A.s2Lo, &A.s2Hi);
     return A;
@@ -1840,7 +1862,76 @@ static int t1_coop_blocks(svm_model* m) {
     return std::min(n, maxCoop);
 }
 
+// Copies the first ringCount[c] entries of every ring from stride Wc to stride Wn (the rest -1).
+__global__ void k_regrid_rings(const int* __restrict__ ring, int Wc, const int* __restrict__ ringCount, int nC,
+                               int* __restrict__ out, int Wn) {
+    const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (e >= (long)nC * Wn) return;
+    const int c = (int)(e / Wn), k = (int)(e % Wn);
+    out[e] = k < ringCount[c] ? ring[(long)c * Wc + k] : -1;
+}
+
+// growCellVerticesList (sphericalVertexModel.cpp:733-758): the rings re-laid out at capacity Wn
+// (rounded up to a multiple of 4, which keeps the 16-entry flip path), with the corner and undo
+// arrays that share their stride.  The width of the storage changes no result; captured graphs,
+// which hold the old arrays, are rebuilt on their next use.
+int grow_rings(svm_model* m, int Wn) {
+    Wn = (Wn + 3) & ~3;
+    if (Wn <= m->Wc) return SVM_OK;
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    const long nC = m->nCells;
+    int *ring = nullptr, *undoRings = nullptr;
+    double2* corner = nullptr;
+    if (cudaMalloc(&ring, sizeof(int) * nC * Wn) != cudaSuccess ||
+        cudaMalloc(&corner, sizeof(double2) * nC * Wn) != cudaSuccess ||
+        cudaMalloc(&undoRings, sizeof(int) * (size_t)m->t1.undoCap * 4 * Wn) != cudaSuccess) {
+        cudaFree(ring); cudaFree(corner); cudaFree(undoRings);
+        cudaGetLastError();
+        return SVM_ERR_CUDA;
+    }
+    k_regrid_rings<<<blocksFor(nC * Wn), kBlock, 0, m->stream>>>(m->ring, m->Wc, m->ringCount, m->nCells, ring, Wn);
+    if (check_launch() || cudaStreamSynchronize(m->stream) != cudaSuccess) {
+        cudaFree(ring); cudaFree(corner); cudaFree(undoRings);
+        return SVM_ERR_CUDA;
+    }
+    cudaFree(m->ring); cudaFree(m->corner); cudaFree(m->t1.undoRings);
+    m->ring = ring; m->corner = corner; m->t1.undoRings = undoRings;
+    m->Wc = Wn;
+    m->cornersValid = false;
+    m->paramsVersion++;
+    m->ringGrowths++;
+    return SVM_OK;
+}
+
+// Before a T1 pass launched outside a capture: grows the ring capacity when ringHeadroom or fewer
+// slots are free in the largest ring.  The host first waits for the pass before last, so the
+// maximum it reads lags at most two passes; a reading close to the capacity is confirmed after a
+// synchronisation.  (Graph launches check between replays instead.)
+int ensure_ring_headroom(svm_model* m) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(m->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return SVM_OK;
+    cudaEvent_t& ev = m->passEv[m->passSlot];
+    if (ev && cudaEventSynchronize(ev) != cudaSuccess) return SVM_ERR_CUDA;
+    volatile int* h = m->ringMaxHost;
+    if (*h + m->ringHeadroom < m->Wc) return SVM_OK;
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    const int mx = *h;
+    if (mx + m->ringHeadroom < m->Wc) return SVM_OK;
+    return grow_rings(m, mx + m->ringHeadroom + 8);
+}
+// Marks the end of a pass launched outside a capture (the wait of ensure_ring_headroom two passes on).
+static int mark_pass(svm_model* m) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(m->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return SVM_OK;
+    cudaEvent_t& ev = m->passEv[m->passSlot];
+    if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { ev = nullptr; return SVM_ERR_CUDA; }
+    if (cudaEventRecord(ev, m->stream) != cudaSuccess) return SVM_ERR_CUDA;
+    m->passSlot ^= 1;
+    return SVM_OK;
+}
+
 int launch_t1_apply(svm_model* m, int bump) {
+    if (int rc = ensure_ring_headroom(m)) return rc;
     PhaseTimer pt(m, SVM_PHASE_T1APPLY, 3);
     // touched-cell count (ctr[5]), per-pass round maximum (ctr[6]), block ticket (ctr[7]) and the
     // cooperative pass's counters and barrier (t1.ctl, after them)
@@ -1870,7 +1961,8 @@ int launch_t1_apply(svm_model* m, int bump) {
     }
     k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
     k_t1_patch<<<2 * 152, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
-    return check_launch();
+    if (int rc = check_launch()) return rc;
+    return mark_pass(m);
 }
 
 // The T1 edge test on its own (k_t1_test: the decisions of the test fused into the corner
@@ -2090,6 +2182,15 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     alloc((void**)&m->repVertOff, (nRep + 1) * sizeof(int));
     alloc((void**)&m->repFlag, nRep * sizeof(int));
     alloc((void**)&m->repScal, 3 * nRep * sizeof(double));
+    alloc((void**)&m->ringMax, sizeof(int));
+    if (ok && cudaHostAlloc((void**)&m->ringMaxHost, sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+        m->ringMaxHost = nullptr;
+        ok = false;
+    }
+    if (ok) {
+        *m->ringMaxHost = 0;
+        ok = cudaHostGetDevicePointer((void**)&m->ringMaxHostDev, m->ringMaxHost, 0) == cudaSuccess;
+    }
     if (!ok) { svm_model_destroy(m); return SVM_ERR_CUDA; }
     cudaMemcpy(m->repR, radius, nRep * sizeof(double), cudaMemcpyHostToDevice);
     m->repT.assign(nRep, 0.0);
@@ -2118,8 +2219,13 @@ int svm_model_destroy(svm_model* m) {
                     m->t1.resC, m->t1.comV, m->t1.comC, m->t1.undo, m->t1.undoRings, m->t1.ctr, m->t1.stats,
                     m->pos32[0], m->pos32[1], m->cellPos32, m->force32, m->dap32, m->repR, m->repNp, m->repCellOff,
                     m->repVertOff, m->t1.clocks,
-                    m->repFlag, m->repScal, m->dotPartials};
+                    m->repFlag, m->repScal, m->dotPartials, m->ringMax};
     for (void* p : ptrs) if (p) cudaFree(p);
+    if (m->ringMaxHost) cudaFreeHost(m->ringMaxHost);
+    for (cudaEvent_t e : m->passEv)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : m->runEv)
+        if (e) cudaEventDestroy(e);
     if (m->bdGraph) cudaGraphExecDestroy(m->bdGraph);
     for (auto& g : m->ioGraph)
         if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -2164,6 +2270,12 @@ static int upload_positions(svm_model* m, const double* in) {
 int svm_model_set_topology(svm_model* m, const double* vp, const int* rings, int stride, const unsigned* counts,
                            const int* vc, const int* vn) {
     if (!m || !vp || !rings || !counts || !vc || !vn || stride < 3) return SVM_ERR_ARG;
+    int maxCount = 0;
+    for (int c = 0; c < m->nCells; ++c) maxCount = std::max(maxCount, (int)counts[c]);
+    if (maxCount + m->ringHeadroom >= m->Wc) {  // room for the rings to grow (growCellVerticesList)
+        const int rc = svm::grow_rings(m, maxCount + m->ringHeadroom + 8);
+        if (rc) return rc;
+    }
     const int nC = m->nCells, nV = m->nVertices, Wc = m->Wc;
     std::vector<int> rg((size_t)nC * Wc, -1), cnt(nC);
     for (int c = 0; c < nC; ++c) {
@@ -2188,6 +2300,9 @@ int svm_model_set_topology(svm_model* m, const double* vp, const int* rings, int
     SVM_CUDA(cudaMemcpyAsync(m->vnbr, vnbr.data(), sizeof(int4) * nV, cudaMemcpyHostToDevice, m->stream));
     // a new state: status bits of the old one no longer apply, and this upload's checks set their own
     SVM_CUDA(cudaMemsetAsync(m->status, 0, sizeof(int), m->stream));
+    SVM_CUDA(cudaStreamSynchronize(m->stream));  // no pass may still write the host-visible maximum
+    SVM_CUDA(cudaMemcpy(m->ringMax, &maxCount, sizeof(int), cudaMemcpyHostToDevice));
+    *m->ringMaxHost = maxCount;
     k_ring_index<<<svm::blocksFor(nC), svm::kBlock, 0, m->stream>>>(m->ring, m->ringCount, Wc, nC, m->vcell, m->vlast,
                                                                     m->vnext, m->vrpos, m->status);
     if (svm::check_launch()) return SVM_ERR_CUDA;
@@ -2331,6 +2446,21 @@ int svm_model_get_area_perimeter(svm_model* m, double* out) {
     if (!m || !out) return SVM_ERR_ARG;
     SVM_CUDA(cudaMemcpyAsync(out, m->ap, sizeof(double2) * m->nCells, cudaMemcpyDeviceToHost, m->stream));
     SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_set_ring_headroom(svm_model* m, int slots) {
+    if (!m || slots < 0 || slots > 64) return SVM_ERR_ARG;
+    m->ringHeadroom = slots;
+    return SVM_OK;
+}
+
+int svm_model_ring_info(svm_model* m, int* out3) {
+    if (!m || !out3) return SVM_ERR_ARG;
+    SVM_CUDA(cudaStreamSynchronize(m->stream));
+    out3[0] = m->Wc;
+    out3[1] = *(volatile int*)m->ringMaxHost;
+    out3[2] = m->ringGrowths;
     return SVM_OK;
 }
 
@@ -2700,29 +2830,44 @@ int svm_brownian_run(svm_model* m, double T, double dt, double mu, uint64_t seed
     }
     if (nSteps == 0) return SVM_OK;
     svm::batch_tuner_untimed(m, nSteps);
-    rc = svm::launch_geometry(m);  // make corners valid outside the capture
-    if (rc) return rc;
-    const bool reuse = m->bdGraph && m->bdT == T && m->bdDt == dt && m->bdMu == mu && m->bdSeed == seed &&
-                       m->bdGraphCur == m->cur && m->bdGraphVersion == m->paramsVersion;
-    if (!reuse) {
-        if (m->bdGraph) { cudaGraphExecDestroy(m->bdGraph); m->bdGraph = nullptr; }
-        // a pair of steps returns the position buffers to their starting roles
-        cudaGraph_t g;
-        const int cur0 = m->cur;
-        SVM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-        int r1 = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
-        int r2 = r1 ? r1 : svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
-        cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
-        m->cur = cur0;
-        if (r2 || ce != cudaSuccess) { cudaGetLastError(); return SVM_ERR_CUDA; }
-        ce = cudaGraphInstantiate(&m->bdGraph, g, 0);
-        cudaGraphDestroy(g);
-        if (ce != cudaSuccess) { m->bdGraph = nullptr; return SVM_ERR_CUDA; }
-        m->bdT = T; m->bdDt = dt; m->bdMu = mu; m->bdSeed = seed;
-        m->bdGraphCur = m->cur; m->bdGraphVersion = m->paramsVersion;
+    for (cudaEvent_t& e : m->runEv)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { e = nullptr; return SVM_ERR_CUDA; }
+    // Chunks of up to 8 steps (4 replays of a captured pair of steps).  The host stays at most two
+    // chunks ahead of the device, so that the ring-capacity check before each chunk reads a recent
+    // maximum; when it grows the rings, the graph (which holds the old arrays) is captured again.
+    for (int chunk = 0; nSteps > 1; ++chunk) {
+        if (chunk >= 2) SVM_CUDA(cudaEventSynchronize(m->runEv[chunk % 2]));
+        if ((rc = svm::ensure_ring_headroom(m))) return rc;
+        const bool reuse = m->bdGraph && m->bdT == T && m->bdDt == dt && m->bdMu == mu && m->bdSeed == seed &&
+                           m->bdGraphCur == m->cur && m->bdGraphVersion == m->paramsVersion;
+        if (chunk == 0 || !reuse || !m->cornersValid) {
+            rc = svm::launch_geometry(m);  // make corners valid outside the capture
+            if (rc) return rc;
+        }
+        if (!reuse) {
+            if (m->bdGraph) { cudaGraphExecDestroy(m->bdGraph); m->bdGraph = nullptr; }
+            // a pair of steps returns the position buffers to their starting roles
+            cudaGraph_t g;
+            const int cur0 = m->cur;
+            SVM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+            int r1 = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+            int r2 = r1 ? r1 : svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
+            cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
+            m->cur = cur0;
+            if (r2 || ce != cudaSuccess) { cudaGetLastError(); return SVM_ERR_CUDA; }
+            ce = cudaGraphInstantiate(&m->bdGraph, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) { m->bdGraph = nullptr; return SVM_ERR_CUDA; }
+            m->bdT = T; m->bdDt = dt; m->bdMu = mu; m->bdSeed = seed;
+            m->bdGraphCur = m->cur; m->bdGraphVersion = m->paramsVersion;
+        }
+        const int pairs = std::min(nSteps / 2, 4);
+        for (int i = 0; i < pairs; ++i) SVM_CUDA(cudaGraphLaunch(m->bdGraph, m->stream));
+        m->cornersValid = true;  // a replayed pair leaves the moved state's corners
+        SVM_CUDA(cudaEventRecord(m->runEv[chunk % 2], m->stream));
+        nSteps -= 2 * pairs;
     }
-    for (int i = 0; i + 1 < nSteps; i += 2) SVM_CUDA(cudaGraphLaunch(m->bdGraph, m->stream));
-    if (nSteps % 2) {
+    if (nSteps == 1) {
         rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed);
         if (rc) return rc;
     }

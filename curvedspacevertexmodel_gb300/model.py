@@ -110,7 +110,9 @@ class sphericalVertexModel:
 
     def __init__(self, n: int, noise: noiseSource | None = None, a0: float = 1.0, p0: float = 3.8,
                  useGPU: bool = True, neverGPU: bool = False, ringCapacity: int = 16, stream=None,
-                 topology: Topology | None = None, radius: float | None = None):
+                 topology: Topology | None = None, radius: float | None = None, ringHeadroom: int | None = None):
+        """ringCapacity: the initial ring capacity (it grows on demand); ringHeadroom: free ring
+        slots at or below which it grows before a T1 pass (svm_model_set_ring_headroom, default 2)."""
         if not useGPU or neverGPU:
             raise ValueError("this model runs on the GPU only")
         self.nCells = int(n)
@@ -127,6 +129,8 @@ class sphericalVertexModel:
         call("svm_model_create", self.nCells, self.nVertices, cap, self.radius,
              C.c_void_p(stream) if stream else None, C.byref(h))
         self._h = h
+        if ringHeadroom is not None:
+            call("svm_model_set_ring_headroom", h, int(ringHeadroom))
         call("svm_model_set_topology", h, np.ascontiguousarray(topology.vertexPositions).reshape(-1),
              np.ascontiguousarray(topology.rings).reshape(-1), topology.rings.shape[1], topology.ringCounts,
              np.ascontiguousarray(topology.vertexCells).reshape(-1),
@@ -251,8 +255,20 @@ class sphericalVertexModel:
         call("svm_model_get_area_perimeter", self._h, out)
         return out.reshape(self.nCells, 2)
 
+    def ringInfo(self) -> dict:
+        """Ring capacity (it grows as the reference's growCellVerticesList widens its rings), the
+        largest ring count seen and the number of growths."""
+        out = np.zeros(3, dtype=np.int32)
+        call("svm_model_ring_info", self._h, out)
+        return dict(capacity=int(out[0]), max_ring=int(out[1]), growths=int(out[2]))
+
+    def setRingHeadroom(self, slots: int):
+        """The ring capacity grows before a T1 pass when this many slots or fewer are free in the
+        largest ring (default 2)."""
+        call("svm_model_set_ring_headroom", self._h, int(slots))
+
     def rings(self, stride: int | None = None):
-        W = stride or self.ringCapacity
+        W = stride or self.ringInfo()["capacity"]
         out = np.empty(self.nCells * W, dtype=np.int32)
         cnt = np.empty(self.nCells, dtype=np.uint32)
         call("svm_model_get_rings", self._h, out, W, cnt)

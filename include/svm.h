@@ -94,9 +94,9 @@ void svm_topology_free(svm_topology* t);
 
 /* ---- model ---------------------------------------------------------------------------------
  * Device-resident state of sphericalVertexModel (src/model/sphericalVertexModel.h:10-123).
- * ringCapacity is the fixed per-cell ring capacity (the reference grows its ring width on
- * demand, sphericalVertexModel.cpp:733-758; here a ring that would outgrow the capacity sets
- * SVM_DEV_RING_OVERFLOW).  stream may be NULL (the model then creates its own stream). */
+ * ringCapacity is the initial per-cell ring capacity; it grows on demand as the reference's ring
+ * width does (sphericalVertexModel.cpp:733-758; svm_model_set_ring_headroom below).  stream may
+ * be NULL (the model then creates its own stream). */
 typedef struct svm_model svm_model;
 int svm_model_create(int nCells, int nVertices, int ringCapacity, double radius, void* stream, svm_model** out);
 int svm_model_destroy(svm_model* m);
@@ -156,6 +156,17 @@ int svm_model_set_velocities(svm_model* m, const double* in);
 int svm_model_get_area_perimeter(svm_model* m, double* out);
 int svm_model_get_cell_positions(svm_model* m, double* out);
 int svm_model_get_rings(svm_model* m, int* rings, int ringStride, unsigned* ringCounts);
+/* Ring capacity.  growCellVerticesList (src/model/sphericalVertexModel.cpp:733-758, called from the
+ * T1 passes at :492 and :824) widens the reference's ring storage when a flip would fill a ring.
+ * Here every T1 pass records its largest ring, and before a pass (between replays of 8 steps for
+ * svm_brownian_run, between batches of 32 iterations for svm_fire_minimize) the capacity grows --
+ * the rings re-laid out at a width that is a multiple of 4 -- whenever `slots` or fewer are free in
+ * the largest ring (default 2).  The width changes no result.  The host waits for the pass before
+ * last before launching a pass, so its reading lags at most two passes (16 steps of
+ * svm_brownian_run); a flip that still finds its ring full is refused and sets
+ * SVM_DEV_RING_OVERFLOW.  svm_model_ring_info: capacity, largest ring count, growths so far. */
+int svm_model_set_ring_headroom(svm_model* m, int slots);
+int svm_model_ring_info(svm_model* m, int* out3);
 int svm_model_get_vertex_cells(svm_model* m, int* out);
 int svm_model_get_vertex_neighbors(svm_model* m, int* out);
 /* The last geometry pass's total-area check (sphericalVertexModel.cpp:304-310): sum of cell

@@ -47,12 +47,12 @@ def params(g):
     return dict(N=int(N), seed=int(SEED), bd_seed=int(BD_SEED), a0=A0, p0=P0, kr=KR, T=T, mu=MU, dt=DT, t1=T1)
 
 
-def gpu_model(svm, g, prefix="init_", ring_capacity=16):
+def gpu_model(svm, g, prefix="init_", ring_capacity=16, ring_headroom=None):
     p = params(g)
     topo = svm.Topology.from_arrays(g[prefix + "pos"], g[prefix + "rings"], g[prefix + "counts"],
                                     g[prefix + "vcells"], g[prefix + "vnbrs"])
     m = svm.sphericalVertexModel(p["N"], topology=topo, a0=p["a0"], p0=p["p0"], radius=float(g["init_radius"]),
-                                 ringCapacity=ring_capacity)
+                                 ringCapacity=ring_capacity, ringHeadroom=ring_headroom)
     m.setScalarModelParameter(p["kr"])
     m.setT1Threshold(p["t1"])
     return m

@@ -3,7 +3,7 @@ how far apart they are.  Used by tests/test_gpu_portable_acos.py in a subprocess
 SVM_LIBRARY is curvedspacevertexmodel_gb300/libsvm_pacos.so (the device library built with
 -DSVM_PORTABLE_ACOS); the oracle is switched to the same function with set_portable_acos.
 
-    SVM_LIBRARY=.../libsvm_pacos.so python tests/portable_acos_run.py n200|n20k
+    SVM_LIBRARY=.../libsvm_pacos.so python tests/portable_acos_run.py n200|n20k|growth
 
 Prints one JSON object: the number of steps and values compared and every difference found
 (0 everywhere means bit for bit).
@@ -48,8 +48,8 @@ def compare(gm, om, rep, kr, a0p0, full):
     rep["flips_differ"] += int(not np.array_equal(gm.takeFlips(), om.flips()))
     if full:
         rep["checks"] += 1
-        rings_g, counts_g = gm.rings(16)
-        rings_o, counts_o = om.rings(16)
+        rings_g, counts_g = gm.rings(32)
+        rings_o, counts_o = om.rings(32)
         rep["topology_differ"] += int(not (np.array_equal(rings_g, rings_o) and np.array_equal(counts_g, counts_o)
                                            and np.array_equal(gm.vertexCellNeighbors(), om.vertex_cells())
                                            and np.array_equal(gm.vertexNeighbors(), om.vertex_neighbors())))
@@ -116,12 +116,41 @@ def run_n20k(steps=60):
     return rep
 
 
+def run_growth(steps=700):
+    """The N = 200 start at P0 = 4.2, T = 0.1, T1 threshold 0.2 with ring capacity 11 (its largest
+    ring plus one) and no headroom: a ring fills the capacity, which grows before the next pass;
+    compared with the restatement after every step."""
+    g = load_gold()
+    gm = gpu_model(svm, g, ring_capacity=11, ring_headroom=0)
+    om = oracle_model(oracle, g)
+    gm.setPreferredParameters(1.0, 4.2)
+    gm.setT1Threshold(0.2)
+    om.set_preferred(1.0, 4.2)
+    om.set_t1_threshold(0.2)
+    bd = svm.brownianDynamics()
+    bd.setModel(gm)
+    bd.setT(0.1)
+    noise = oracle.OracleNoise(11)
+    rep = dict(case="growth", steps=0, checks=0, pos_bits_differ=0, flips_differ=0, topology_differ=0,
+               area_perimeter_bits_differ=0, energy_cpu_order_bits_differ=0, energy_reduction_rel=0.0, flips=0)
+    for step in range(1, steps + 1):
+        xi = noise.normals(3 * gm.nVertices)
+        bd.injectNoise(xi)
+        bd.integrateEquationOfMotion()
+        om.brownian_step_noise(xi, 0.1, 0.01, 1.0)
+        rep["flips"] += len(om.flips(clear=False))
+        compare(gm, om, rep, 1.0, (1.0, 4.2), step % 50 == 0)
+    rep["status"] = gm.deviceStatus()
+    rep["ring_info"] = gm.ringInfo()
+    return rep
+
+
 def main():
     if not os.environ.get("SVM_LIBRARY", "").endswith("libsvm_pacos.so"):
         raise SystemExit("run with SVM_LIBRARY pointing at libsvm_pacos.so")
     oracle.set_portable_acos(True)
     case = sys.argv[1] if len(sys.argv) > 1 else "n200"
-    rep = run_n200() if case == "n200" else run_n20k()
+    rep = {"n200": run_n200, "n20k": run_n20k, "growth": run_growth}[case]()
     print(json.dumps(rep), flush=True)
 
 

@@ -55,3 +55,12 @@ def test_n20k_free_run_bitwise(svm_lib):
     rep = _run("n20k", svm_lib)
     assert rep["steps"] == 60 and rep["flips"] > 30, rep
     _assert_bitwise(rep)
+
+
+def test_ring_growth_bitwise(svm_lib):
+    """A ring driven to the model's capacity (11, no headroom, the hot fluid setting of
+    test_gpu_ring_growth.py): the capacity grows before the next T1 pass and the run stays equal to
+    the restatement bit for bit, growth included."""
+    rep = _run("growth", svm_lib)
+    assert rep["steps"] == 700 and rep["ring_info"]["growths"] >= 1 and rep["ring_info"]["capacity"] > 11, rep
+    _assert_bitwise(rep)
