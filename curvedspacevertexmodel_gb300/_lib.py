@@ -100,6 +100,7 @@ SIGNATURES = {
     "svm_model_t1_clocks": (i32, [vp, i32, _nullable(np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS"))]),
     "svm_model_fallback_count": (i32, [vp, C.POINTER(i32)]),
     "svm_model_set_t1_blocks": (i32, [vp, i32]),
+    "svm_model_set_t1_wait_limit": (i32, [vp, i32]),
     "svm_model_t1_stats": (i32, [vp, ip]),
     "svm_model_profile": (i32, [vp, i32]),
     "svm_model_profile_read": (i32, [vp, dp, ip]),

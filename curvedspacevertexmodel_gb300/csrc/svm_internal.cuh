@@ -343,6 +343,7 @@ struct svm_model {
     int cur = 0;                       // index of the current position buffer
     bool cornersValid = false;         // corner/vsph arrays match the current state
     int t1Blocks = 0;                  // svm_model_set_t1_blocks (0: automatic)
+    int t1WaitLimit = 1 << 20;         // polls of a cooperative T1 pass's grid-barrier wait
     double4_32a* pos[2] = {nullptr, nullptr};
     double4_32a* vsph = nullptr;
     double* vnorm = nullptr;           // |p| per vertex, from the last corner pass (FP64 form)

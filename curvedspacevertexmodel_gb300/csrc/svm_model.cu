@@ -492,6 +492,7 @@ struct ApplyArgs {
     int* status;
     unsigned long long* stepCounter;
     int bumpStep;
+    int barrierSpins;      // polls of a grid-barrier wait before it gives up
     int* ringMax;          // largest ring count produced (atomicMax by the commits)
     int* ringMaxOut;       // host-visible copy, written once per pass by k_t1_patch
 };
@@ -877,7 +878,9 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
         *(volatile int*)A.ringMaxOut = *(volatile int*)A.ringMax;
         __threadfence_system();
     }
-    const int nt = *(volatile int*)(t1.ctr + 5);
+    // appends past the list's capacity roll the pass back; a pass cut short by an exhausted barrier
+    // wait may leave the counter above it, and only the stored entries are read
+    const int nt = min(*(volatile int*)(t1.ctr + 5), t1.touchedCap);
     const long total = (long)nt * A.Wc;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
         const int cell = t1.touched[e / A.Wc], k = (int)(e % A.Wc);
@@ -1131,8 +1134,8 @@ __device__ int block_excl_scan(int v, int* total) {
 // kBarrierSpins times, after which the wait gives up and the barrier returns false.  Fences before
 // the arrival and after the wait order every block's writes before the barrier with every read
 // after it.
-constexpr int kBarrierSpins = 1 << 20;  // at least 67 ms with 64 ns naps
-__device__ bool grid_barrier(T1Ctl* ctl) {
+constexpr int kBarrierSpins = 1 << 20;  // at least 67 ms with 64 ns naps (svm_model_set_t1_wait_limit)
+__device__ bool grid_barrier(T1Ctl* ctl, int spinLimit) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1146,7 +1149,7 @@ __device__ bool grid_barrier(T1Ctl* ctl) {
         } else {
             int spins = 0;
             while (*(volatile unsigned*)&ctl->barGen == gen) {
-                if (++spins > kBarrierSpins) { ok = 0; break; }
+                if (++spins > spinLimit) { ok = 0; break; }
                 __nanosleep(64);
             }
         }
@@ -1201,7 +1204,7 @@ __global__ void __launch_bounds__(kCoop ? kCoopThreads : kParThreads) k_t1_paral
     if ((kCoop || gridDim.x == 1) && *t1.count == 0) return;
     auto group_sync = [&]() -> bool {
         if (!kCoop) { __syncthreads(); return true; }
-        if (grid_barrier(ctl)) return true;
+        if (grid_barrier(ctl, A.barrierSpins)) return true;
         if (tid == 0) atomicOr(A.status, SVM_DEV_T1_TIMEOUT);
         return false;
     };
@@ -1748,7 +1751,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     A.vnext = m->vnext; A.vrpos = m->vrpos; A.ring = m->ring; A.ringCount = m->ringCount; A.corner = m->corner;
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
     A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
-    A.ringMax = m->ringMax; A.ringMaxOut = m->ringMaxHostDev;
+    A.ringMax = m->ringMax; A.ringMaxOut = m->ringMaxHostDev; A.barrierSpins = m->t1WaitLimit;
     t1_bracket(m->t1Threshold, m->R, &A.cosLo, &A.cosHi);
     t1_sin2_bracket(m->t1Threshold, m->R, &A.s2Lo, &A.s2Hi);
     return A;
@@ -2446,6 +2449,13 @@ int svm_model_get_area_perimeter(svm_model* m, double* out) {
     if (!m || !out) return SVM_ERR_ARG;
     SVM_CUDA(cudaMemcpyAsync(out, m->ap, sizeof(double2) * m->nCells, cudaMemcpyDeviceToHost, m->stream));
     SVM_CUDA(cudaStreamSynchronize(m->stream));
+    return SVM_OK;
+}
+
+int svm_model_set_t1_wait_limit(svm_model* m, int polls) {
+    if (!m || polls < 0) return SVM_ERR_ARG;
+    m->t1WaitLimit = polls;
+    m->paramsVersion++;  // captured graphs hold the old limit
     return SVM_OK;
 }
 

@@ -329,6 +329,11 @@ class sphericalVertexModel:
         performance only, the results do not depend on it."""
         call("svm_model_set_t1_blocks", self._h, int(blocks))
 
+    def setT1WaitLimit(self, polls: int = 1 << 20):
+        """Polls of a cooperative T1 pass's grid-barrier wait before it gives up and reports
+        SVM_DEV_T1_TIMEOUT (a diagnostic hook; a model whose pass gave up is to be recreated)."""
+        call("svm_model_set_t1_wait_limit", self._h, int(polls))
+
     def t1Clocks(self, enable: bool = True):
         """SM cycles of the parallel T1 pass's phases since the last call (extraction, reserve,
         flips, release, end) and re-arms the counters (or turns them off)."""

@@ -193,6 +193,12 @@ int svm_model_t1_clocks(svm_model* m, int enable, unsigned long long* cycles5);
  * cooperative grid of n blocks (capped at the device's co-resident count).  Performance only:
  * the flips and every later value are the same for any count.  Ignored by batches. */
 int svm_model_set_t1_blocks(svm_model* m, int blocks);
+/* Polls of each grid-barrier wait of a cooperative T1 pass before it gives up (default 2^20, at
+ * least 67 ms).  A wait that runs out sets SVM_DEV_T1_TIMEOUT and ends the kernel: the pass is then
+ * incomplete and the model's topology is not to be trusted (recreate it).  No counterpart in the
+ * reference (its T1 loop runs on one CPU thread); a diagnostic hook, e.g. to check that an
+ * exhausted wait is reported rather than hung. */
+int svm_model_set_t1_wait_limit(svm_model* m, int polls);
 int svm_model_synchronize(svm_model* m);
 /* Dynamical observables of the cell positions (dynamicalFeatures, src/analysis/dynamicalFeatures.cpp):
  * svm_model_set_dynamics_reference snapshots the current cell positions (as computed by the last

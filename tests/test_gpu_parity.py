@@ -477,3 +477,30 @@ def test_t1_pass_block_count_does_not_change_the_run(svm):
         assert np.array_equal(r[2][0], ref[2][0]) and np.array_equal(r[2][1], ref[2][1])
         assert np.array_equal(r[3], ref[3])
         assert r[4] == 0
+
+
+def test_exhausted_t1_barrier_wait_is_reported(svm, gold):
+    """A cooperative T1 pass whose grid-barrier waits may poll only once: the blocks that arrive
+    first give up, the kernel ends instead of hanging, and SVM_DEV_T1_TIMEOUT comes back; the
+    device stays usable (a fresh model steps and reads back normally)."""
+    from curvedspacevertexmodel_gb300 import _lib
+    m, bd = stabilised(svm, 20000, seed=21, stab=20, steps=20)
+    m.setT1Threshold(0.08)   # flagged edges every step, so the cooperative pass runs
+    m.setT1Blocks(64)
+    m.setT1WaitLimit(0)
+    status = 0
+    for _ in range(5):
+        bd.integrateEquationOfMotion()
+        status |= m.deviceStatus()
+        if status & _lib.SVM_DEV_T1_TIMEOUT:
+            break
+    assert status & _lib.SVM_DEV_T1_TIMEOUT, status
+    m.close()
+    fresh = gpu_model(svm, gold)
+    bd2 = svm.brownianDynamics()
+    bd2.setModel(fresh)
+    bd2.setT(0.01)
+    for _ in range(10):
+        bd2.integrateEquationOfMotion()
+    fresh.computeGeometry()
+    assert np.isfinite(fresh.computeEnergy()) and fresh.deviceStatus() == 0
