@@ -168,10 +168,13 @@ def algorithmic_bytes_step(nv: int) -> int:
 # FP64 pipe's busy fraction in that kernel.
 FORCE_BD_DRAM_BYTES_PER_VERTEX = (1.247151e9 + 0.124883e9) / 1_999_996
 FORCE_BD_FP64_PIPE_PCT = 83.4
-# FP64 arithmetic thread operations (DMUL + DFMA + DADD) per vertex in one k_force_bd launch (ncu
-# at N = 100k), and the FP64 issue rate they are bound by: 16 SM cycles per FP64 warp instruction
-# (ncu: sm__pipe_fp64_cycles_active / sm__inst_executed_pipe_fp64 in every FP64 kernel), i.e. two
-# lanes per clock on each of the 152 SMs at the 2070 MHz maximum SM clock.
+# FP64 arithmetic thread operations (DMUL + DFMA + DADD) per vertex in one k_force_bd launch of the
+# build whose divisions and square roots are the hardware sequences (ncu at N = 100k), and the FP64
+# issue rate they are bound by: 16 SM cycles per FP64 warp instruction (ncu:
+# sm__pipe_fp64_cycles_active / sm__inst_executed_pipe_fp64 in every FP64 kernel), i.e. two lanes
+# per clock on each of the 152 SMs at the 2070 MHz maximum SM clock.  The default build computes the
+# divisions and square roots on the integer pipes (same results), so the rate below is
+# FP64-pipe-equivalent work: above 1 it would beat what the FP64 pipe alone can issue.
 FORCE_BD_FP64_OPS_PER_VERTEX = 1420
 FP64_LANES_PER_CLOCK_PER_SM = 2
 GB300_SMS = 152
@@ -179,12 +182,15 @@ SM_MAX_MHZ = 2070
 
 
 def fp64_roofline(avg_launch_ms: float, nv: int) -> dict:
-    """The force kernel against the FP64 issue rate: achieved and peak in G thread-ops/s."""
+    """The force kernel against the FP64 issue rate: the hardware-division build's FP64 instructions
+    per vertex over the measured launch (FP64-pipe-equivalent work), and the peak, in G thread-ops/s."""
     achieved = FORCE_BD_FP64_OPS_PER_VERTEX * nv / (avg_launch_ms * 1e-3) / 1e9
     peak = GB300_SMS * FP64_LANES_PER_CLOCK_PER_SM * SM_MAX_MHZ * 1e6 / 1e9
     return {"unit": "G FP64 thread-ops/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
             "ops_per_vertex_ncu": FORCE_BD_FP64_OPS_PER_VERTEX,
-            "peak_basis": "152 SMs x 2 FP64 lanes/clock x 2070 MHz (16 cycles per FP64 warp instruction, ncu)"}
+            "peak_basis": "152 SMs x 2 FP64 lanes/clock x 2070 MHz (16 cycles per FP64 warp instruction, ncu)",
+            "work_basis": "FP64 instructions per vertex of the build with hardware divisions and square roots; "
+                          "the measured build computes those on the integer pipes (bit-identical results)"}
 
 
 def peaks():
@@ -368,7 +374,8 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "fp64_pipe_busy_pct_ncu": FORCE_BD_FP64_PIPE_PCT,
                      "fp64": fp64_roofline(avg_launch_ms, nv) if names[dom] == "force" else None,
-                     "note": "FP64-pipe bound (ncu: FP64 pipe 83% busy, DRAM 3%); HBM fraction is small by construction",
+                     "note": "FP64-issue bound (ncu: FP64 pipe 83% busy, DRAM 3% before the integer-pipe divisions); "
+                             "HBM fraction is small by construction",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
         "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
         "warm_l2_ms_per_step": warm_ms,

@@ -129,6 +129,7 @@ SIGNATURES = {
     "svm_fire_minimize": (i32, [vp, i32, C.POINTER(i32), C.POINTER(f64)]),
     "svm_fire_state": (i32, [vp, dp]),
     "svm_fire_step": (i32, [vp]),
+    "svm_softf64_check": (i32, [C.c_longlong, C.c_ulonglong, vp]),
     "svm_velocity_verlet_step": (i32, [vp, f64, i32]),
     "svm_vv_half": (i32, [vp, f64]),
     "svm_reduce_dots": (i32, [vp, dp]),

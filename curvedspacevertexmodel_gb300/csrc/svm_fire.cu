@@ -68,11 +68,11 @@ __device__ double bmax(double v, double* sh) {
 __device__ __forceinline__ D3 move_exact_f(D3 p, D3 v, double R) {
     const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
     const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
-    const double s = vp / pp;
+    const double s = f64_div(vp, pp);
     D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
          __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
     const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
-    const double inv = 1.0 / sqrt(qq);
+    const double inv = f64_div(1.0, f64_sqrt(qq));
     return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
 }
 

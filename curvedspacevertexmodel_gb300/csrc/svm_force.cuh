@@ -32,7 +32,7 @@ __device__ __forceinline__ int comp(const int4& a, int s) { return s == 0 ? a.x 
 // (any radius), from the raw position difference d.
 __device__ __forceinline__ D3 grad_geo_vec(D3 a, D3 d) {
     const D3 t = sub3(d, scl3(dot3(d, a), a));
-    return scl3(-1.0 / sqrt(dot3(t, t)), t);
+    return scl3(f64_div(-1.0, f64_sqrt(dot3(t, t))), t);
 }
 // Gradient w.r.t. v = |v| a of the signed spherical triangle area R^2 E(a, a + beta, a + gamma),
 // beta and gamma the raw differences to the other corners over |v|: tan(E/2) = N/D (Van Oosterom
@@ -42,7 +42,7 @@ __device__ __forceinline__ D3 grad_tri_vec(D3 a, D3 beta, D3 gamma, double R) {
     const D3 bxc = add3(add3(cross3(a, gamma), cross3(beta, a)), bg);
     const double N = dot3(a, bg);
     const double D = 4.0 - dot3(beta, beta) - dot3(gamma, gamma) + dot3(beta, gamma);
-    const double w = 2.0 / (N * N + D * D);
+    const double w = f64_div(2.0, N * N + D * D);
     const D3 g = scl3(w, sub3(scl3(D, bxc), scl3(N, add3(beta, gamma))));
     return scl3(R, sub3(g, scl3(dot3(g, a), a)));
 }
@@ -51,7 +51,7 @@ __device__ __forceinline__ D3 grad_tri_vec(D3 a, D3 beta, D3 gamma, double R) {
 // formulas; the reference's formulas below lose digits for short edges and thin fan triangles.
 __device__ __forceinline__ D3 vertex_force_vec(const ForceArgs& A, int v) {
     const D3 P = ld3(A.pos, v);
-    const double inv = 1.0 / sqrt(dot3(P, P));
+    const double inv = f64_div(1.0, f64_sqrt(dot3(P, P)));
     const D3 a = scl3(inv, P);
     const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
     D3 f{0.0, 0.0, 0.0};
@@ -126,7 +126,7 @@ __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s, const
     const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
     if (A.vec) {
         const D3 P = ld3(A.pos, v);
-        const double inv = 1.0 / sqrt(dot3(P, P));
+        const double inv = f64_div(1.0, f64_sqrt(dot3(P, P)));
         const D3 a = scl3(inv, P);
         const D3 dc = sub3(ld3(A.cellPos, c), P);
         const D3 dl = sub3(ld3(A.pos, L), P), dx = sub3(ld3(A.pos, X), P);
@@ -282,11 +282,11 @@ __device__ __forceinline__ double bd_disp(double xi, double np, double f, double
 __device__ __forceinline__ D3 move_exact(D3 p, D3 v, double R) {
     const double vp = __dadd_rn(__dadd_rn(__dmul_rn(v.x, p.x), __dmul_rn(v.y, p.y)), __dmul_rn(v.z, p.z));
     const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
-    const double s = vp / pp;
+    const double s = f64_div(vp, pp);
     D3 q{__dadd_rn(p.x, __dsub_rn(v.x, __dmul_rn(s, p.x))), __dadd_rn(p.y, __dsub_rn(v.y, __dmul_rn(s, p.y))),
          __dadd_rn(p.z, __dsub_rn(v.z, __dmul_rn(s, p.z)))};
     const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q.x, q.x), __dmul_rn(q.y, q.y)), __dmul_rn(q.z, q.z));
-    const double inv = 1.0 / sqrt(qq);
+    const double inv = f64_div(1.0, f64_sqrt(qq));
     return D3{__dmul_rn(R, __dmul_rn(inv, q.x)), __dmul_rn(R, __dmul_rn(inv, q.y)), __dmul_rn(R, __dmul_rn(inv, q.z))};
 }
 

@@ -21,6 +21,7 @@
 #include <vector>
 #include "../../include/svm.h"
 #include "svm_acos.h"
+#include "svm_softf64.cuh"
 
 namespace svm {
 
@@ -29,6 +30,26 @@ constexpr double kPI = 3.141592653589793115997963468544185161590576171875;
 constexpr double kPILo = 1.2246467991473532e-16;
 
 struct D3 { double x, y, z; };
+
+// Division and square root of the FP64 kernels.  Both are the IEEE correctly rounded operations
+// either way; by default they run on the integer and FP32 pipes (svm_softf64.cuh), which leaves
+// GB300's FP64 pipe -- 2 lanes per clock per SM, the bound of these kernels -- to the products and
+// sums, where a hardware division or square root would take about eight FP64 instructions.  A build
+// with -DSVM_NATIVE_FP64_DIV uses the hardware sequences (same results).
+__device__ __forceinline__ double f64_div(double a, double b) {
+#ifdef SVM_NATIVE_FP64_DIV
+    return __ddiv_rn(a, b);
+#else
+    return sf::div(a, b);
+#endif
+}
+__device__ __forceinline__ double f64_sqrt(double a) {
+#ifdef SVM_NATIVE_FP64_DIV
+    return __dsqrt_rn(a);
+#else
+    return sf::sqrt(a);
+#endif
+}
 
 // The arccosine of the FP64 geometry (arcs, included angles, triangle areas, T1 length tests).
 // The default build uses CUDA's acos; a build with -DSVM_PORTABLE_ACOS uses svm_portable::acos,
@@ -76,27 +97,27 @@ __device__ __forceinline__ double det3(D3 a, D3 b, D3 c) {    // a . (b x c), sp
 
 // putInBoxReal (sphericalDomain.h:183-187): p <- R p / |p|
 __device__ __forceinline__ D3 renorm(D3 p, double R) {
-    double inv = 1.0 / sqrt(dot3(p, p));
+    double inv = f64_div(1.0, f64_sqrt(dot3(p, p)));
     return scl3(R, scl3(inv, p));
 }
 // move(p, v) (sphericalDomain.h:203-209): project v onto the tangent plane at p, add, renormalise
 __device__ __forceinline__ D3 sphere_move(D3 p, D3 v, double R) {
-    double s = dot3(v, p) / dot3(p, p);
+    double s = f64_div(dot3(v, p), dot3(p, p));
     D3 d = sub3(v, scl3(s, p));
     return renorm(add3(p, d), R);
 }
 // geodesicDistance (sphericalDomain.h:94-112)
 __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
-    double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
-    return R * svm_acos(num / den);
+    double den = f64_sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * f64_sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    return R * svm_acos(f64_div(num, den));
 }
 // |p| as geodesic and sph_coords evaluate it (same operations, so the same value)
-__device__ __forceinline__ double pos_norm(D3 p) { return sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
+__device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
 // geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
 __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
     const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
-    return R * svm_acos(num / (n1 * n2));
+    return R * svm_acos(f64_div(num, n1 * n2));
 }
 // The T1 length test geodesic(p1, p2) < t, i.e. R acos(c) < t with c = p1.p2 / (|p1||p2|).  acos
 // is decreasing, so away from c = cos(t / R) the answer is c > cos(t / R); the formula itself is
@@ -137,8 +158,8 @@ __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, d
         if (xx < s2Lo * d && xx > 1e-13 * d) return true;
         if (xx > s2Hi * d) return false;
     }
-    const double den = sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
-    const double c = num / den;
+    const double den = f64_sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * f64_sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    const double c = f64_div(num, den);
     if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
     if (c < cosLo) return false;
     return R * svm_acos(c) < t;
@@ -154,7 +175,7 @@ __device__ __forceinline__ float arc32(float4 p, float4 q, float R) {
 __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
-    double a = svm_acos(-dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1))));
+    double a = svm_acos(f64_div(-dot3(ci, cim1), f64_sqrt(dot3(ci, ci)) * f64_sqrt(dot3(cim1, cim1))));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -170,7 +191,7 @@ __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
 template <bool clamp = false>
 __device__ __forceinline__ double included_angle_pre(D3 Cx, D3 Cl, double nx, double nl, D3 pl) {
     const double det = dot3(pl, Cx);
-    double c = dot3(Cx, Cl) / (nx * nl);
+    double c = f64_div(dot3(Cx, Cl), nx * nl);
     if (clamp) c = fmin(1.0, fmax(-1.0, c));
     double a = svm_acos(c);
     if (det > 0) a = -a;
@@ -186,7 +207,7 @@ __device__ __forceinline__ int nbr_slot(int4 nb, int u) { return u == nb.x ? 0 :
 __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
-    double c = -dot3(ci, cim1) / (sqrt(dot3(ci, ci)) * sqrt(dot3(cim1, cim1)));
+    double c = f64_div(-dot3(ci, cim1), f64_sqrt(dot3(ci, ci)) * f64_sqrt(dot3(cim1, cim1)));
     double a = svm_acos(fmin(1.0, fmax(-1.0, c)));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
@@ -194,7 +215,7 @@ __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
 }
 // sphericalTriangleArea (sphericalDomain.h:135-166)
 // q / |q| as sphericalTriangleArea normalises each corner
-__device__ __forceinline__ D3 unit_corner(D3 q) { return scl3(1.0 / sqrt(dot3(q, q)), q); }
+__device__ __forceinline__ D3 unit_corner(D3 q) { return scl3(f64_div(1.0, f64_sqrt(dot3(q, q))), q); }
 __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R);
 __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
     return triangle_area_unit(unit_corner(q1), unit_corner(q2), unit_corner(q3), R);
@@ -203,9 +224,9 @@ __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
 __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R) {
     double d12 = dot3(p1, p2), d13 = dot3(p1, p3), d23 = dot3(p2, p3);
     double area = -kPI;
-    area += svm_acos((d23 - d12 * d13) / (sqrt(1 - d12 * d12) * sqrt(1 - d13 * d13)));
-    area += svm_acos((d12 - d13 * d23) / (sqrt(1 - d13 * d13) * sqrt(1 - d23 * d23)));
-    area += svm_acos((d13 - d12 * d23) / (sqrt(1 - d12 * d12) * sqrt(1 - d23 * d23)));
+    area += svm_acos(f64_div(d23 - d12 * d13, f64_sqrt(1 - d12 * d12) * f64_sqrt(1 - d13 * d13)));
+    area += svm_acos(f64_div(d12 - d13 * d23, f64_sqrt(1 - d13 * d13) * f64_sqrt(1 - d23 * d23)));
+    area += svm_acos(f64_div(d13 - d12 * d23, f64_sqrt(1 - d12 * d12) * f64_sqrt(1 - d23 * d23)));
     return area * (R * R);
 }
 
@@ -213,10 +234,10 @@ __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double
 // (sphericalDomain.h:218-232, 251-261): cos t = z/|p|, sin t = sqrt(1 - cos^2 t),
 // cos p = x / sqrt(x^2+y^2), sin p = y / sqrt(x^2+y^2).
 __device__ __forceinline__ double4_32a sph_coords_n(D3 p, double r) {  // r = pos_norm(p)
-    double cosT = p.z / r;
-    double sinT = sqrt(1. - cosT * cosT);
-    double rxy = sqrt(p.x * p.x + p.y * p.y);
-    return make_double4_32a(cosT, sinT, p.x / rxy, p.y / rxy);
+    double cosT = f64_div(p.z, r);
+    double sinT = f64_sqrt(1. - cosT * cosT);
+    double rxy = f64_sqrt(p.x * p.x + p.y * p.y);
+    return make_double4_32a(cosT, sinT, f64_div(p.x, rxy), f64_div(p.y, rxy));
 }
 __device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n(p, pos_norm(p)); }
 
@@ -226,7 +247,7 @@ __device__ __forceinline__ double2 grad_geodesic(double4_32a s1, double4_32a s2)
     double sP12 = s1.w * s2.z - s1.z * s2.w;
     double cP12 = s1.z * s2.z + s1.w * s2.w;
     double dp = s1.x * s2.x + cP12 * s1.y * s2.y;
-    double dinv = 1. / sqrt(1 - dp * dp);
+    double dinv = f64_div(1., f64_sqrt(1 - dp * dp));
     double gT = 1.0 * (s2.x * s1.y - s1.x * cP12 * s2.y) * dinv;
     double gP = s2.y * sP12 * dinv;
     return make_double2(gT, gP);
@@ -247,16 +268,16 @@ __device__ __forceinline__ double2 grad_triangle(double4_32a a, double4_32a b, d
     double d13 = a.x * cP13 * c.y - c.x * a.y;
     double g = 1 - s12 * s12 - s13 * s13 - s23 * s23 + 2.0 * s12 * s13 * s23;
     double q12 = (-1. + s12 * s12), q13 = (-1. + s13 * s13);
-    double den1 = sqrt(q12 * q12 * g);
-    double den2 = sqrt(q13 * q13 * g);
-    double den3 = sqrt((s12 * s12 - 1.) * (s13 * s13 - 1.) * (s12 * s12 - 1.) * (s13 * s13 - 1.) * g);
-    double gT = (d13 * (s12 * s12 - 1.0) + d12 * (s23 - s12 * s13)) / den1
-              + (d12 * (s13 * s13 - 1.0) + d13 * (s23 - s12 * s13)) / den2
-              - (d12 * (s13 * s13 - 1.) * (s13 - s12 * s23) + d13 * (s12 * s12 - 1.0) * (s12 - s13 * s23)) / den3;
+    double den1 = f64_sqrt(q12 * q12 * g);
+    double den2 = f64_sqrt(q13 * q13 * g);
+    double den3 = f64_sqrt((s12 * s12 - 1.) * (s13 * s13 - 1.) * (s12 * s12 - 1.) * (s13 * s13 - 1.) * g);
+    double gT = f64_div(d13 * (s12 * s12 - 1.0) + d12 * (s23 - s12 * s13), den1)
+              + f64_div(d12 * (s13 * s13 - 1.0) + d13 * (s23 - s12 * s13), den2)
+              - f64_div(d12 * (s13 * s13 - 1.) * (s13 - s12 * s23) + d13 * (s12 * s12 - 1.0) * (s12 - s13 * s23), den3);
     gT *= R;
-    double gP = ((s12 * s13 - s23) * sP12 * b.y - (-1 + s12 * s12) * sP13 * c.y) / (den1)
-              - ((-1 + s13 * s13) * sP12 * b.y + (-(s12 * s13) + s23) * sP13 * c.y) / (den2)
-              + ((-1 + s13 * s13) * (s13 - s12 * s23) * sP12 * b.y + (-1 + s12 * s12) * (s12 - s13 * s23) * sP13 * c.y) / (den3);
+    double gP = f64_div((s12 * s13 - s23) * sP12 * b.y - (-1 + s12 * s12) * sP13 * c.y, den1)
+              - f64_div((-1 + s13 * s13) * sP12 * b.y + (-(s12 * s13) + s23) * sP13 * c.y, den2)
+              + f64_div((-1 + s13 * s13) * (s13 - s12 * s23) * sP12 * b.y + (-1 + s12 * s12) * (s12 - s13 * s23) * sP13 * c.y, den3);
     gP *= R;
     if (det3(v1, v2, v3) < 0) { gT = -gT; gP = -gP; }
     return make_double2(gT, gP);

@@ -154,7 +154,7 @@ __global__ void k_edges(const double4_32a* __restrict__ pos, const double* __res
         const D3 C = cross3(p, U);
         const double arc = geodesic_n(U, p, vnorm[u], vnorm[w], R);
         const int e = 3 * w + j;
-        edgeC[e] = make_double4_32a(C.x, C.y, C.z, sqrt(dot3(C, C)));
+        edgeC[e] = make_double4_32a(C.x, C.y, C.z, f64_sqrt(dot3(C, C)));
         edgeArc[e] = arc;
         // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475)
         if (t1test && arc < t1Threshold) {
@@ -310,7 +310,7 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
         // ~4N (pi - kPI) R^2 (4e-7 at N = 100k, 4e-5 at N = 1M) and trips its absolute 1e-6 area
         // check by itself at large N.  The FP64 form keeps the reference's arithmetic.
         if (std::is_same<PT, float4>::value) area = __dsub_rn(area, __dmul_rn((double)(n - 2), kPILo));
-        const int extra = (int)floor(area / (1.0 * kPI));
+        const int extra = (int)floor(f64_div(area, 1.0 * kPI));
         if (extra > 0) area = __dsub_rn(area, __dmul_rn((double)extra, kPI));
         area = __dmul_rn(__dmul_rn(area, R), R);
         ap[c] = make_double2(area, per);
@@ -564,7 +564,7 @@ __device__ __forceinline__ D3 rodrigues(D3 v, D3 k, double c, double s) {
 }
 __device__ __forceinline__ D3 renorm_exact(D3 p, double R) {
     const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
-    const double inv = 1.0 / sqrt(pp);
+    const double inv = f64_div(1.0, f64_sqrt(pp));
     return D3{__dmul_rn(R, __dmul_rn(inv, p.x)), __dmul_rn(R, __dmul_rn(inv, p.y)), __dmul_rn(R, __dmul_rn(inv, p.z))};
 }
 
@@ -1662,7 +1662,7 @@ __global__ void k_spp_dirs(const double4_32a* __restrict__ pos, double4_32a* __r
     D3 n = ld3(dir, v);
     const double s = __ddiv_rn(dot3(n, p), dot3(p, p));
     n = D3{__dsub_rn(n.x, __dmul_rn(s, p.x)), __dsub_rn(n.y, __dmul_rn(s, p.y)), __dsub_rn(n.z, __dmul_rn(s, p.z))};
-    const double inv = 1.0 / sqrt(dot3(n, n));
+    const double inv = f64_div(1.0, f64_sqrt(dot3(n, n)));
     n = D3{__dmul_rn(inv, n.x), __dmul_rn(inv, n.y), __dmul_rn(inv, n.z)};
     double rv;
     if (kNoise == SVM_NOISE_BUFFER) {
@@ -1710,7 +1710,7 @@ __global__ void k_vicsek_target(const double4_32a* __restrict__ pos, const doubl
     D3 sp{__dmul_rn(st, cos(phi)), __dmul_rn(st, sin(phi)), cos(theta)};
     const double ps = __ddiv_rn(dot3(sp, p), dot3(p, p));
     sp = D3{__dsub_rn(sp.x, __dmul_rn(ps, p.x)), __dsub_rn(sp.y, __dmul_rn(ps, p.y)), __dsub_rn(sp.z, __dmul_rn(ps, p.z))};
-    const double is = 1.0 / sqrt(dot3(sp, sp));
+    const double is = f64_div(1.0, f64_sqrt(dot3(sp, sp)));
     sp = D3{__dmul_rn(sp.x, is), __dmul_rn(sp.y, is), __dmul_rn(sp.z, is)};
     const int4 nb = vnbr[v];
     D3 t = ld3(dir, v);
@@ -1724,7 +1724,7 @@ __global__ void k_vicsek_target(const double4_32a* __restrict__ pos, const doubl
            __dadd_rn(__dmul_rn(t.z, mi), __dmul_rn(sp.z, eta))};
     const double ts = __ddiv_rn(dot3(t, p), dot3(p, p));
     t = D3{__dsub_rn(t.x, __dmul_rn(ts, p.x)), __dsub_rn(t.y, __dmul_rn(ts, p.y)), __dsub_rn(t.z, __dmul_rn(ts, p.z))};
-    const double it = 1.0 / sqrt(dot3(t, t));
+    const double it = f64_div(1.0, f64_sqrt(dot3(t, t)));
     st3(target, v, D3{__dmul_rn(t.x, it), __dmul_rn(t.y, it), __dmul_rn(t.z, it)});
 }
 // n += (dt / tau)(target - n), projected onto the tangent plane and normalised.
@@ -1738,7 +1738,7 @@ __global__ void k_vicsek_update(const double4_32a* __restrict__ pos, double4_32a
            __dadd_rn(n.z, __dmul_rn(rate, __dsub_rn(t.z, n.z)))};
     const double s = __ddiv_rn(dot3(n, p), dot3(p, p));
     n = D3{__dsub_rn(n.x, __dmul_rn(s, p.x)), __dsub_rn(n.y, __dmul_rn(s, p.y)), __dsub_rn(n.z, __dmul_rn(s, p.z))};
-    const double inv = 1.0 / sqrt(dot3(n, n));
+    const double inv = f64_div(1.0, f64_sqrt(dot3(n, n)));
     st3(dir, v, D3{__dmul_rn(n.x, inv), __dmul_rn(n.y, inv), __dmul_rn(n.z, inv)});
 }
 

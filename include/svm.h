@@ -445,6 +445,13 @@ int svm_mlp_predict(svm_mlp* mlp, const float* X, int n, float* Y);   /* DEVICE 
  * move by outputScale * (y0 e1 + y1 e2) onto the sphere (all vertices from the same state). */
 int svm_mlp_warm_start(svm_mlp* mlp, svm_model* m);
 
+/* ---- diagnostics ---------------------------------------------------------------------------
+ * The FP64 kernels compute their divisions and square roots with integer-pipe IEEE arithmetic
+ * (csrc/svm_softf64.cuh; no counterpart in the reference).  svm_softf64_check runs that device code
+ * against the hardware's correctly rounded instructions on `cases` random operand pairs per
+ * operation and returns the mismatches of multiply, add, divide and square root (all zero). */
+int svm_softf64_check(long long cases, unsigned long long seed, unsigned long long* mismatches4);
+
 #ifdef __cplusplus
 }
 #endif
