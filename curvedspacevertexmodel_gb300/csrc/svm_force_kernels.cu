@@ -48,7 +48,14 @@ __global__ void __launch_bounds__(3 * kSlotVerts) k_force(ForceArgs A, int nV, d
 
 // Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
 template <int kNoise>
-__global__ void __launch_bounds__(3 * kSlotVerts) k_force_bd(ForceArgs A, int nV, double4_32a* __restrict__ force,
+// Three blocks of 192 threads per SM (the register budget falls from 120 to 96 with a few bytes of
+// spill): 18 resident warps hide the latency of the integer-pipe divisions and square roots better
+// than 12; measured 0.49 -> 0.475 ms per launch at 100k cells.
+#ifndef SVM_FORCE_MIN_BLOCKS
+#define SVM_FORCE_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(3 * kSlotVerts, SVM_FORCE_MIN_BLOCKS) k_force_bd(
+                                                             ForceArgs A, int nV, double4_32a* __restrict__ force,
                                                              double4_32a* __restrict__ posNext,
                                                              const double* __restrict__ noise, uint64_t seed,
                                                              const unsigned long long* __restrict__ stepCounter,

@@ -253,32 +253,47 @@ __device__ __forceinline__ double2 grad_geodesic(double4_32a s1, double4_32a s2)
     return make_double2(gT, gP);
 }
 
+// The products of grad_triangle: the hardware multiply, or (-DSVM_TRI_SOFT_MUL) the integer-pipe one
+// (same result), which shifts part of the force kernel's FP64 work off the FP64 pipe.
+__device__ __forceinline__ double tri_mul(double x, double y) {
+#ifdef SVM_TRI_SOFT_MUL
+    return sf::mul(x, y);
+#else
+    return __dmul_rn(x, y);
+#endif
+}
+
 // gradientTriangleArea (sphericalDomain.h:347-411) in the (theta, phi) basis of v1; the sign
-// follows det(v1, v2, v3).  Returns (d/dtheta, d/dphi) components.
+// follows det(v1, v2, v3).  Returns (d/dtheta, d/dphi) components.  Every product and sum in the
+// order the reference's expressions evaluate them (left to right, products first).
 __device__ __forceinline__ double2 grad_triangle(double4_32a a, double4_32a b, double4_32a c, D3 v1, D3 v2, D3 v3, double R) {
-    double sP12 = a.w * b.z - a.z * b.w;
-    double sP13 = a.w * c.z - a.z * c.w;
-    double cP12 = a.z * b.z + a.w * b.w;
-    double cP13 = a.z * c.z + a.w * c.w;
-    double cP23 = b.z * c.z + b.w * c.w;
-    double s12 = a.x * b.x + cP12 * a.y * b.y;
-    double s13 = a.x * c.x + cP13 * a.y * c.y;
-    double s23 = b.x * c.x + cP23 * b.y * c.y;
-    double d12 = a.x * cP12 * b.y - b.x * a.y;
-    double d13 = a.x * cP13 * c.y - c.x * a.y;
-    double g = 1 - s12 * s12 - s13 * s13 - s23 * s23 + 2.0 * s12 * s13 * s23;
-    double q12 = (-1. + s12 * s12), q13 = (-1. + s13 * s13);
-    double den1 = f64_sqrt(q12 * q12 * g);
-    double den2 = f64_sqrt(q13 * q13 * g);
-    double den3 = f64_sqrt((s12 * s12 - 1.) * (s13 * s13 - 1.) * (s12 * s12 - 1.) * (s13 * s13 - 1.) * g);
-    double gT = f64_div(d13 * (s12 * s12 - 1.0) + d12 * (s23 - s12 * s13), den1)
-              + f64_div(d12 * (s13 * s13 - 1.0) + d13 * (s23 - s12 * s13), den2)
-              - f64_div(d12 * (s13 * s13 - 1.) * (s13 - s12 * s23) + d13 * (s12 * s12 - 1.0) * (s12 - s13 * s23), den3);
-    gT *= R;
-    double gP = f64_div((s12 * s13 - s23) * sP12 * b.y - (-1 + s12 * s12) * sP13 * c.y, den1)
-              - f64_div((-1 + s13 * s13) * sP12 * b.y + (-(s12 * s13) + s23) * sP13 * c.y, den2)
-              + f64_div((-1 + s13 * s13) * (s13 - s12 * s23) * sP12 * b.y + (-1 + s12 * s12) * (s12 - s13 * s23) * sP13 * c.y, den3);
-    gP *= R;
+    const auto M = tri_mul;
+    const double sP12 = M(a.w, b.z) - M(a.z, b.w);
+    const double sP13 = M(a.w, c.z) - M(a.z, c.w);
+    const double cP12 = M(a.z, b.z) + M(a.w, b.w);
+    const double cP13 = M(a.z, c.z) + M(a.w, c.w);
+    const double cP23 = M(b.z, c.z) + M(b.w, c.w);
+    const double s12 = M(a.x, b.x) + M(M(cP12, a.y), b.y);
+    const double s13 = M(a.x, c.x) + M(M(cP13, a.y), c.y);
+    const double s23 = M(b.x, c.x) + M(M(cP23, b.y), c.y);
+    const double d12 = M(M(a.x, cP12), b.y) - M(b.x, a.y);
+    const double d13 = M(M(a.x, cP13), c.y) - M(c.x, a.y);
+    const double s12s12 = M(s12, s12), s13s13 = M(s13, s13), s12s13 = M(s12, s13);
+    const double g = (((1 - s12s12) - s13s13) - M(s23, s23)) + M(M(M(2.0, s12), s13), s23);
+    const double q12 = -1. + s12s12, q13 = -1. + s13s13;
+    const double den1 = f64_sqrt(M(M(q12, q12), g));
+    const double den2 = f64_sqrt(M(M(q13, q13), g));
+    const double a12 = s12s12 - 1., a13 = s13s13 - 1.;
+    const double den3 = f64_sqrt(M(M(M(M(a12, a13), a12), a13), g));
+    const double s12s23 = M(s12, s23), s13s23 = M(s13, s23);
+    double gT = f64_div(M(d13, a12) + M(d12, s23 - s12s13), den1)
+              + f64_div(M(d12, a13) + M(d13, s23 - s12s13), den2)
+              - f64_div(M(M(d12, a13), s13 - s12s23) + M(M(d13, a12), s12 - s13s23), den3);
+    gT = M(gT, R);
+    double gP = f64_div(M(M(s12s13 - s23, sP12), b.y) - M(M(-1 + s12s12, sP13), c.y), den1)
+              - f64_div(M(M(-1 + s13s13, sP12), b.y) + M(M(-s12s13 + s23, sP13), c.y), den2)
+              + f64_div(M(M(M(-1 + s13s13, s13 - s12s23), sP12), b.y) + M(M(M(-1 + s12s12, s12 - s13s23), sP13), c.y), den3);
+    gP = M(gP, R);
     if (det3(v1, v2, v3) < 0) { gT = -gT; gP = -gP; }
     return make_double2(gT, gP);
 }
