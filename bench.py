@@ -163,11 +163,11 @@ def algorithmic_bytes_step(nv: int) -> int:
     return 94 * nv
 
 
-# From an ncu --set full capture of k_force_bd at N = 1M cells (the profiling case of this package,
-# --cells 1000000 --stab 2 --steps 1): DRAM bytes read + written per vertex by one launch, and the
-# FP64 pipe's busy fraction in that kernel.
-FORCE_BD_DRAM_BYTES_PER_VERTEX = (1.247151e9 + 0.124883e9) / 1_999_996
-FORCE_BD_FP64_PIPE_PCT = 83.4
+# From an ncu --set full capture of one k_force_bd launch at N = 100k cells (bench.py --mode profile
+# --cells 100000 --stab 2 --steps 1; profiles/k_force_bd_n100k_full.md): DRAM bytes read + written
+# per vertex by one launch, and the FP64 pipe's busy fraction in that kernel.
+FORCE_BD_DRAM_BYTES_PER_VERTEX = (32.219648e6 + 0.745728e6) / 199_996
+FORCE_BD_FP64_PIPE_PCT = 78.3
 # FP64 arithmetic thread operations (DMUL + DFMA + DADD) per vertex in one k_force_bd launch of the
 # build whose divisions and square roots are the hardware sequences (ncu at N = 100k), and the FP64
 # issue rate they are bound by: 16 SM cycles per FP64 warp instruction (ncu:
@@ -374,8 +374,8 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "fp64_pipe_busy_pct_ncu": FORCE_BD_FP64_PIPE_PCT,
                      "fp64": fp64_roofline(avg_launch_ms, nv) if names[dom] == "force" else None,
-                     "note": "FP64-issue bound (ncu: FP64 pipe 83% busy, DRAM 3% before the integer-pipe divisions); "
-                             "HBM fraction is small by construction",
+                     "note": "FP64-issue bound (ncu: FP64 pipe 78% busy, DRAM under 1%; divisions and square roots "
+                             "on the integer pipes); HBM fraction is small by construction",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
         "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
         "warm_l2_ms_per_step": warm_ms,
