@@ -19,7 +19,8 @@
 // carried as a double-double (hi + lo).  Maximum error 1.35 ulp over [-1, 1] (measured against a
 // 60-digit acos at 75,000 points, densest near 0 and +-1); acos(1) = 0, acos(-1) = kPI, NaN
 // outside [-1, 1] and for NaN.  Only +, -, * and sqrt are used, each rounded separately (explicit
-// round-to-nearest intrinsics on the device; the host side is compiled without FP contraction).
+// round-to-nearest intrinsics on the device, the square root on the integer pipes; the host side is
+// compiled without FP contraction).
 #pragma once
 
 #if defined(__CUDACC__)
@@ -29,6 +30,8 @@
 #endif
 
 #include <cmath>
+
+#include "svm_softf64.cuh"
 
 namespace svm_portable {
 
@@ -55,7 +58,7 @@ SVM_ACOS_HD double sub(double a, double b) {
 }
 SVM_ACOS_HD double root(double a) {
 #if defined(__CUDA_ARCH__)
-    return __dsqrt_rn(a);
+    return sf::sqrt(a);  // the IEEE square root on the integer pipes (svm_softf64.cuh): same bits
 #else
     return std::sqrt(a);
 #endif
@@ -83,13 +86,12 @@ SVM_ACOS_HD double acos(double x) {
     const double kPio2Lo = 6.123233995736766e-17;   // pi/2 - kPio2Hi
     const double ax = x < 0.0 ? -x : x;
     if (!(ax <= 1.0)) return sub(x, x) / sub(x, x);  // NaN for |x| > 1 and NaN input
-    if (ax <= 0.5) {
-        const double r = asin_tail(mul(x, x));
-        return sub(kPio2Hi, sub(x, sub(kPio2Lo, mul(x, r))));
-    }
-    const double z = mul(sub(1.0, ax), 0.5);
-    const double s = root(z);
-    const double r = asin_tail(z);
+    // the polynomial's argument first (t = x^2, or z = (1 - |x|) / 2), so that it is evaluated once
+    const bool small = ax <= 0.5;
+    const double t = small ? mul(x, x) : mul(sub(1.0, ax), 0.5);
+    const double r = asin_tail(t);
+    if (small) return sub(kPio2Hi, sub(x, sub(kPio2Lo, mul(x, r))));
+    const double s = root(t);
     if (x > 0.0) return mul(2.0, add(s, mul(s, r)));
     return mul(2.0, sub(kPio2Hi, add(s, sub(mul(s, r), kPio2Lo))));
 }
