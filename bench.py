@@ -38,7 +38,9 @@ Other workloads (off by default, one JSON line each; --mode):
   batch    512 replicas for --steps (default 10,000) batched steps, and per-replica energy errors of
            a 32-replica subset against FP64 single-sphere runs (same state, and time averages);
   profile  a small untimed run for profilers (ncu -k ...): --cells, --stab, --steps, --equil and
-           the options --mixed, --replicas, --fire, --neighbors, --sub-grid, --active, --dynamics.
+           the options --mixed, --replicas, --fire, --neighbors, --sub-grid, --active, --dynamics;
+  fire-ablation  where FIRE's iterations go at N = 20k, and how many remain from the minimum
+           itself after a few thermal steps (the bound on any warm start).
 """
 from __future__ import annotations
 
@@ -1057,12 +1059,81 @@ def mode_profile(args):
     print(json.dumps(out), flush=True)
 
 
+def mode_fire_ablation(args):
+    """Where FIRE's iterations go, and what any warm start could save (N = 20k, the fire_warm_start
+    instances: P0 U[3.6, 3.8], start = stabilisation + 500 Brownian steps at T = 0.01, FIRE with the
+    vector-form forces and T1 on).  (a) Plain FIRE driven phase by phase (velocity-Verlet step +
+    fireStep, bit for bit minimize), recording the iteration at which max|F| first drops below each
+    decade from 1e-1 to 1e-9 and the energy per cell above the final minimum at that point.  (b) FIRE
+    to max|F| < 1e-9 from the final minimum itself after k Brownian steps at T: a start far closer
+    to the minimum than any predictor's -- a lower bound on the iterations a warm start can leave."""
+    import numpy as np
+    import curvedspacevertexmodel_gb300 as svm
+    from curvedspacevertexmodel_gb300 import _lib, warm_start as ws
+    rng = np.random.default_rng(FIRE_SEED)
+    rows = []
+    levels = [1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9]
+    for i, p0 in enumerate(rng.uniform(3.6, 3.8, args.fire_instances)):
+        seed = FIRE_SEED + i
+        m = ws.start_state(args.cells, float(p0), seed)
+        start = m.saveState()
+        fire = svm.energyMinimizerFIRE(m)
+        fire.setFIREParameters(*ws.FIRE_PARAMS)
+        fire.setCriterion(_lib.SVM_FIRE_MAX_FORCE)
+        fire.setMaximumIterations(10 ** 9)
+        m.computeForces()
+        reached, e_at, it = {}, {}, 0
+        while it < 100000:
+            fire.integrateEquationOfMotion()
+            fire.fireStep()
+            it += 1
+            if it % 10 == 0:
+                f = fire.state()["max_force"]
+                for level in levels:
+                    if level not in reached and f < level:
+                        reached[level], e_at[level] = it, ws.energy(m)
+                if f < 1e-9:
+                    break
+        e_min = ws.energy(m)
+        minimum = m.saveState()
+        del fire
+        near = {}
+        for k, T in ((1, 0.01), (10, 0.01), (10, 0.001)):
+            m.loadState(minimum)
+            bd = svm.brownianDynamics()
+            bd.setModel(m)
+            bd.setT(T)
+            bd.noise.setReproducibleSeed(seed + 77)
+            m.precision = "fp64"
+            bd.run(k)
+            m.precision = "fp64_vector"
+            e0 = ws.energy(m)
+            its, secs, _ = ws.minimize(m, 1e-9)
+            near[f"{k} steps at T={T}"] = {"iterations": its, "seconds": secs,
+                                           "start_energy_per_cell_above_min": (e0 - e_min) / m.nCells,
+                                           "end_energy_per_cell_minus_min": (ws.energy(m) - e_min) / m.nCells}
+        m.loadState(start)
+        e_start = ws.energy(m)
+        its_p, secs_p, _ = ws.minimize(m, 1e-9)
+        rows.append({"p0": float(p0), "seed": seed, "plain_iterations": its_p, "plain_seconds": secs_p,
+                     "first_below": {str(level): reached.get(level) for level in levels},
+                     "energy_per_cell_above_min_when_first_below": {str(level): (e_at[level] - e_min) / m.nCells
+                                                                    for level in e_at},
+                     "start_energy_per_cell_above_min": (e_start - e_min) / m.nCells,
+                     "from_the_minimum_after_brownian_steps": near,
+                     "best_near_start_over_plain_iterations": min(v["iterations"] for v in near.values()) / its_p})
+        m.close()
+    print(json.dumps({"mode": "fire-ablation", "workload": f"N={args.cells}, P0 U[3.6, 3.8], FIRE to max|F|<1e-9 "
+                      "(vector-form forces, T1 on)", "rows": rows}), flush=True)
+
+
 MODE_DEFAULTS = {  # cells, steps, stab, equil, replicas
     "headline": (N_CELLS, 20, 100, 200, 512),
     "forms": (N_CELLS, 10000, 100, 200, 0),
     "large": (1_000_000, 5000, 100, 0, 0),
     "batch": (0, 10000, 100, 0, 512),
     "profile": (1_000_000, 1, 2, 0, 0),
+    "fire-ablation": (20000, 0, 0, 0, 0),
 }
 
 
@@ -1103,7 +1174,8 @@ def main():
     elif args.mode == "headline":
         run_ours(args)
     else:
-        {"forms": mode_forms, "large": mode_large, "batch": mode_batch, "profile": mode_profile}[args.mode](args)
+        {"forms": mode_forms, "large": mode_large, "batch": mode_batch, "profile": mode_profile,
+         "fire-ablation": mode_fire_ablation}[args.mode](args)
 
 
 if __name__ == "__main__":
