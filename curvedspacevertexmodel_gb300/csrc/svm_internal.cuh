@@ -22,6 +22,7 @@
 #include "../../include/svm.h"
 #include "svm_acos.h"
 #include "svm_softf64.cuh"
+#include "svm_edge_filter.h"
 
 namespace svm {
 
@@ -124,6 +125,10 @@ __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2,
 // evaluated only when c lies within [cosLo, cosHi], a bracket around cos(t / R) of half-width
 // 1e-9, which is many orders wider than the error of acos and of the rounding of c, or when c > 1.
 __host__ __device__ inline void t1_bracket(double t, double R, double* lo, double* hi) {
+    if (!(t > 0.0)) {   // an arc is never below a threshold of 0 or less: every c < lo decides "no"
+        *lo = *hi = 2.0;
+        return;
+    }
     const double c = cos(t / R);
     *lo = c - 1e-9;
     *hi = c + 1e-9;
@@ -151,6 +156,7 @@ __host__ inline void t1_sin2_bracket(double t, double R, double* lo, double* hi)
 }
 __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, double cosLo, double cosHi,
                                              double s2Lo, double s2Hi) {
+    if (svm_edge::clearly_longer(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, R, t)) return false;
     const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
     if (num > 0) {
         const D3 x = cross3(p1, p2);

@@ -2656,6 +2656,10 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
             m->ioEnergy = nullptr;
             return SVM_ERR_CUDA;
         }
+        // the ring-capacity check of a T1 pass launched outside a capture (a growth recaptures)
+        if (!m->restricted) {
+            if (int rc = svm::ensure_ring_headroom(m)) return rc;
+        }
         auto& g = m->ioGraph[m->cur];
         const bool reuse = g.exec && g.T == T && g.dt == dt && g.mu == mu && g.seed == seed && g.in == posIn &&
                            g.out == posOut && g.version == m->paramsVersion && g.precision == m->precision;

@@ -83,3 +83,35 @@ def test_graph_run_grows_like_the_step_loop(svm):
     assert ia["growths"] >= 1 and ib["growths"] >= 1, (ia, ib)
     assert np.array_equal(pa, pb) and np.array_equal(na, nb)
     assert np.array_equal(ra[0], rb[0]) and np.array_equal(ra[1], rb[1])
+
+
+def test_host_buffer_steps_grow_like_the_step_loop(svm):
+    """svm_brownian_step_io with page-locked buffers (a replayed graph per buffer role, the capacity
+    checked before each replay) and the device-resident step loop, from the golden N=200 start in
+    the hot setting with capacity 12 and one slot of headroom: both grow their rings and end bit for
+    bit equal, with no overflow."""
+    import ctypes as C
+    import torch
+    from curvedspacevertexmodel_gb300 import _lib
+    g = load_gold()
+    a = gpu_model(svm, g, ring_capacity=12, ring_headroom=1)
+    b = gpu_model(svm, g, ring_capacity=12, ring_headroom=1)
+    for m in (a, b):
+        m.setPreferredParameters(1.0, P0)
+        m.setT1Threshold(THRESHOLD)
+    n = 3 * a.nVertices
+    pos = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    out = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    pos[:] = a.returnPositions().reshape(-1)
+    e_io = C.c_double()
+    for _ in range(3000):
+        _lib.call("svm_brownian_step_io", a.handle, T, 0.01, 1.0, 5, pos, out, C.byref(e_io))
+        _lib.call("svm_brownian_step", b.handle, T, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, 5)
+        pos, out = out, pos
+    ia, ib = a.ringInfo(), b.ringInfo()
+    assert a.deviceStatus() == 0 and b.deviceStatus() == 0, (ia, ib)
+    assert ia["growths"] >= 1 and ib["growths"] >= 1, (ia, ib)
+    assert np.array_equal(pos.reshape(-1, 3), b.returnPositions())
+    assert np.array_equal(a.vertexNeighbors(), b.vertexNeighbors())
+    ra, rb = a.rings(64), b.rings(64)
+    assert np.array_equal(ra[0], rb[0]) and np.array_equal(ra[1], rb[1])
