@@ -974,7 +974,8 @@ def mode_profile(args):
     T = 0.01, P0 = 3.8 one launch per kernel per step (no graph), and the energy per cell.  --mixed
     runs those steps in the mixed form; --replicas R runs a batch of R replicas instead
     (stabilisation, then args.steps steps at per-replica P0 and T); --fire K adds K FIRE iterations
-    (the reference's default parameters, force tolerance 1e-12 so that all K run); --neighbors K,
+    (the reference's default parameters, force tolerance 1e-12 so that all K run, in the force form
+    --fire-form, timed per iteration with the host synchronised on both sides); --neighbors K,
     K neighbour-list computations (range 1, radius R + 2.5); --active K, K self-propelled then K
     Vicsek steps; --dynamics K, K MSD + overlap evaluations (each printing its mean time)."""
     import numpy as np
@@ -1021,10 +1022,19 @@ def mode_profile(args):
         bd.integrateEquationOfMotion()
     out = {"mode": "profile", "cells": args.cells, "vertices": m.nVertices}
     if args.fire:
+        m.precision = args.fire_form
         fire = svm.energyMinimizerFIRE(m)
         fire.setMaximumIterations(args.fire)
         fire.setForceCutoff(1e-12)
+        m.synchronize()
+        m.t1Stats()
+        t1 = time.perf_counter()
         fire.minimize()
+        m.synchronize()
+        out["fire_ms_per_iteration"] = (time.perf_counter() - t1) / args.fire * 1e3
+        out["fire_t1_per_iteration"] = {k: v / args.fire for k, v in m.t1Stats().items()}
+        out["fire_form"] = args.fire_form
+        m.precision = "fp64"
     if args.dynamics:
         dyn = svm.dynamicalFeatures(m)
         dyn._both(0.5)
@@ -1160,6 +1170,8 @@ def main():
     ap.add_argument("--fire-cap", type=int, default=12000, help="large: FIRE iteration cap (0: no FIRE)")
     ap.add_argument("--mixed", action="store_true", help="profile: the steps in the mixed form")
     ap.add_argument("--fire", type=int, default=0, help="profile: FIRE iterations after the steps")
+    ap.add_argument("--fire-form", default="fp64_vector", choices=("fp64", "fp64_vector"),
+                    help="profile: force form of the FIRE iterations")
     ap.add_argument("--neighbors", type=int, default=0, help="profile: neighbour-list computations")
     ap.add_argument("--sub-grid", type=int, default=1, help="profile: the neighbour list's subGridReduction")
     ap.add_argument("--active", type=int, default=0, help="profile: timed self-propelled and Vicsek steps")

@@ -44,9 +44,12 @@ namespace {
 
 constexpr int kB = 256;
 
-__device__ double bsum(double v, double* sh) {
+// Block sum (bmax: maximum) in a fixed order, valid in thread 0.  Warps from `live` on hold zeros and
+// skip their shuffles (their +0.0 leaves the sum's bits unchanged).
+__device__ double bsum(double v, double* sh, int live = 32) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (warp < live)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) sh[warp] = v;
     __syncthreads();
     double r = 0.0;
@@ -54,9 +57,10 @@ __device__ double bsum(double v, double* sh) {
     __syncthreads();
     return r;
 }
-__device__ double bmax(double v, double* sh) {
+__device__ double bmax(double v, double* sh, int live = 32) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (warp < live)
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
     if (lane == 0) sh[warp] = v;
     __syncthreads();
     double r = 0.0;
@@ -143,7 +147,8 @@ template <bool kControl, bool kCount>
 __device__ void fire_reduce_tail(FireState* __restrict__ Sp, double P, double FF, double VV, int nV,
                                  double* __restrict__ partials, unsigned* __restrict__ ticket, double* __restrict__ out4,
                                  double* sh, bool& amLast) {
-    const double bP = bsum(P, sh), bF = bsum(FF, sh), bV = bsum(VV, sh), bM = bmax(FF, sh);
+    constexpr int kLive = kSlotVerts / 32;  // the warps of the block's vertex threads
+    const double bP = bsum(P, sh, kLive), bF = bsum(FF, sh, kLive), bV = bsum(VV, sh, kLive), bM = bmax(FF, sh, kLive);
     if (threadIdx.x == 0) {
         double* q = partials + 4 * blockIdx.x;
         q[0] = bP; q[1] = bF; q[2] = bV; q[3] = bM;
@@ -200,11 +205,9 @@ __global__ void k_fire_consume(FireState* S) {
 
 // Blocks of 3 kSlotVerts threads: three per vertex for the force (one per cell slot), then the
 // first kSlotVerts threads finish their vertex.
-__global__ void __launch_bounds__(3 * kSlotVerts) k_fire_force(ForceArgs A, FireState* __restrict__ Sp, int nV,
-                                                               double4_32a* __restrict__ force,
-                                                               double4_32a* __restrict__ vel,
-                                                               double* __restrict__ partials,
-                                                               unsigned* __restrict__ ticket) {
+__global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks)
+    k_fire_force(ForceArgs A, FireState* __restrict__ Sp, int nV, double4_32a* __restrict__ force,
+                 double4_32a* __restrict__ vel, double* __restrict__ partials, unsigned* __restrict__ ticket) {
     __shared__ double sh[32];
     __shared__ bool amLast;
     __shared__ SlotShared slots;
@@ -256,10 +259,10 @@ ForceArgs fargs(svm_model* m) { return force_args(m, m->cur); }
 
 int fire_iteration(svm_fire* F) {
     svm_model* m = F->m;
-    const int nb = (m->nVertices + kB - 1) / kB;
+    const int bs = spread_block(m, m->nVertices), nb = (m->nVertices + bs - 1) / bs;
     {
         PhaseTimer pt(m, SVM_PHASE_MOVE);
-        k_fire_vv1<<<nb, kB, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
+        k_fire_vv1<<<nb, bs, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
         k_fire_consume<<<1, 1, 0, m->stream>>>(F->d);
     }
     m->cornersValid = false;
@@ -406,11 +409,11 @@ int svm_vv_half(svm_model* m, double dt) {
 
 int svm_velocity_verlet_step(svm_model* m, double dt, int nSteps) {
     if (!m || !(dt == dt) || nSteps < 0 || m->precision == SVM_PRECISION_MIXED) return SVM_ERR_ARG;
-    const int nb = (m->nVertices + kB - 1) / kB;
+    const int bs = spread_block(m, m->nVertices), nb = (m->nVertices + bs - 1) / bs;
     for (int k = 0; k < nSteps; ++k) {
         {
             PhaseTimer pt(m, SVM_PHASE_MOVE);
-            k_vv_drift<<<nb, kB, 0, m->stream>>>(m->pos[m->cur], m->vel, m->force, m->nVertices, dt, m->R);
+            k_vv_drift<<<nb, bs, 0, m->stream>>>(m->pos[m->cur], m->vel, m->force, m->nVertices, dt, m->R);
         }
         m->cornersValid = false;
         int rc;
@@ -427,7 +430,7 @@ int svm_velocity_verlet_step(svm_model* m, double dt, int nSteps) {
             rc = launch_force_fp64(m);
             if (rc) return rc;
         }
-        k_vv_half<<<nb, kB, 0, m->stream>>>(m->vel, m->force, m->nVertices, dt);
+        k_vv_half<<<nb, bs, 0, m->stream>>>(m->vel, m->force, m->nVertices, dt);
         if (check_launch()) return SVM_ERR_CUDA;
     }
     return SVM_OK;

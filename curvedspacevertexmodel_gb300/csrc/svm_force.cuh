@@ -164,6 +164,12 @@ __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s, const
 // geodesic gradients of the reference form are evaluated once per neighbour (thread 3 i + s for
 // the predecessor in slot s) and shared through the block.
 constexpr int kSlotVerts = 64;
+// Resident blocks per SM the slot-force kernels are compiled for: three blocks of 3 kSlotVerts
+// threads (the register budget falls from 120 to 96 with a few bytes of spill), whose 18 warps hide
+// the latency of the integer-pipe divisions and square roots better than two blocks' 12 (the
+// Brownian step's force kernel at 100k cells: 0.49 -> 0.475 ms per launch; FIRE's at 20k cells
+// likewise).  Blocks of 32 vertices (six per SM) measured no faster at 20k or 100k cells.
+constexpr int kSlotMinBlocks = 3;
 struct SlotShared { double x[3 * kSlotVerts], y[3 * kSlotVerts], z[3 * kSlotVerts]; };
 __device__ __forceinline__ D3 block_slot_force(const ForceArgs& A, int nV, SlotShared& sh) {
     const int t = threadIdx.x, base = blockIdx.x * kSlotVerts;

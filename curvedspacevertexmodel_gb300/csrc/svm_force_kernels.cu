@@ -38,7 +38,8 @@ namespace {
 using namespace svm;
 
 // Blocks of 3 kSlotVerts threads, three per vertex (one per cell slot), kSlotVerts vertices each.
-__global__ void __launch_bounds__(3 * kSlotVerts) k_force(ForceArgs A, int nV, double4_32a* __restrict__ force) {
+__global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force(ForceArgs A, int nV,
+                                                                         double4_32a* __restrict__ force) {
     __shared__ SlotShared sh;
     const D3 f = block_slot_force(A, nV, sh);
     const int v = blockIdx.x * kSlotVerts + threadIdx.x;
@@ -48,13 +49,7 @@ __global__ void __launch_bounds__(3 * kSlotVerts) k_force(ForceArgs A, int nV, d
 
 // Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
 template <int kNoise>
-// Three blocks of 192 threads per SM (the register budget falls from 120 to 96 with a few bytes of
-// spill): 18 resident warps hide the latency of the integer-pipe divisions and square roots better
-// than 12; measured 0.49 -> 0.475 ms per launch at 100k cells.
-#ifndef SVM_FORCE_MIN_BLOCKS
-#define SVM_FORCE_MIN_BLOCKS 3
-#endif
-__global__ void __launch_bounds__(3 * kSlotVerts, SVM_FORCE_MIN_BLOCKS) k_force_bd(
+__global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force_bd(
                                                              ForceArgs A, int nV, double4_32a* __restrict__ force,
                                                              double4_32a* __restrict__ posNext,
                                                              const double* __restrict__ noise, uint64_t seed,

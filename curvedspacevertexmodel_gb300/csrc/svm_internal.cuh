@@ -441,6 +441,7 @@ struct svm_model {
     unsigned long long* stepCounter = nullptr;
     svm::T1Scratch t1;
     int maxPartialBlocks = 0;
+    int sms = 152;                     // SMs of the model's device
     // graph cache for svm_brownian_run
     cudaGraphExec_t bdGraph = nullptr;
     cudaEvent_t runEv[2] = {nullptr, nullptr};   // svm_brownian_run: ends of the last two chunks
@@ -484,6 +485,15 @@ int launch_geometry(svm_model* m);
 int launch_corners(svm_model* m, bool t1test);
 int launch_t1_apply(svm_model* m, int bump);
 int grow_rings(svm_model* m, int newCapacity);
+// Threads per block for a one-thread-per-item FP64 kernel over n items: the largest of 256, 128, 64
+// and 32 that still gives every SM four blocks (or 32).  An SM's FP64 pipe -- one warp instruction
+// per 16 clocks -- is kept busy by a few warps, so a small grid goes over all SMs in small blocks
+// rather than over some of them in full ones.
+inline int spread_block(const svm_model* m, long n) {
+    int bs = 256;
+    while (bs > 32 && n < 4L * m->sms * bs) bs >>= 1;
+    return bs;
+}
 int ensure_ring_headroom(svm_model* m);
 int check_launch();
 // A binned view of device points (svm_celllist.cu): per-bin counts and slots (ascending point

@@ -1764,8 +1764,9 @@ int launch_corners(svm_model* m, bool t1test) {
         return m->nRep > 1 ? batch_tuned_corners(m, t1test) : mixed_launch_corners(m, t1test);
     }
     if (!m->edgeC) return SVM_ERR_ARG;  // FP64 corners exist for single spheres only
-    k_vnorm<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
-    k_edges<<<blocksFor(m->nVertices), kBlock, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->vsph, m->vnbr, m->edgeC,
+    const int bv = spread_block(m, m->nVertices);
+    k_vnorm<<<blocksFor(m->nVertices, bv), bv, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
+    k_edges<<<blocksFor(m->nVertices, bv), bv, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->vsph, m->vnbr, m->edgeC,
                                                               m->edgeArc, m->nVertices, m->R, t1test ? 1 : 0,
                                                               m->t1Threshold, m->t1);
     // both corner kernels write the same values; the three-thread one is faster below ~100k vertices
@@ -2112,6 +2113,12 @@ int svm::model_alloc(int nCells, int nVertices, int Wc, const double* radius, in
     if (svm_device_count(&ndev) != SVM_OK) return SVM_ERR_NO_DEVICE;
     svm_model* m = new svm_model();
     m->nCells = nCells; m->nVertices = nVertices; m->Wc = Wc; m->R = radius[0]; m->nRep = nRep;
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+            m->sms = sms;
+    }
     if (stream) { m->stream = (cudaStream_t)stream; }
     else {
         if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) { delete m; return SVM_ERR_CUDA; }
