@@ -69,18 +69,19 @@ __device__ __forceinline__ D3 ld3(const double4_32a* p, int i) {
     return D3{t.x, t.y, t.z};
 }
 __device__ __forceinline__ void st3(double4_32a* p, int i, D3 v) { p[i] = make_double4_32a(v.x, v.y, v.z, 0.0); }
-// FP32 positions (mixed-precision form): widened exactly on load, rounded to nearest on store.
+// FP32 positions (mixed-precision form): widened exactly on load, rounded to nearest on store (the
+// conversions on the integer pipes: sf::widen, sf::narrow).
 __device__ __forceinline__ D3 ld3(const float4* p, int i) {
     const float4 t = p[i];
-    return D3{(double)t.x, (double)t.y, (double)t.z};
+    return D3{sf::widen(t.x), sf::widen(t.y), sf::widen(t.z)};
 }
 __device__ __forceinline__ void st3(float4* p, int i, D3 v) {
-    p[i] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), 0.f);
+    p[i] = make_float4(sf::narrow(v.x), sf::narrow(v.y), sf::narrow(v.z), 0.f);
 }
 // In the mixed form the w component of a vertex's FP32 position holds its replica index (0 for a
 // single sphere); rounded stores of a vertex keep it.
 __device__ __forceinline__ void st3_keep(float4* p, int i, D3 v) {
-    p[i] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y), __double2float_rn(v.z), p[i].w);
+    p[i] = make_float4(sf::narrow(v.x), sf::narrow(v.y), sf::narrow(v.z), p[i].w);
 }
 __device__ __forceinline__ int rep_of(const float4& p) { return (int)p.w; }
 __device__ __forceinline__ int rep_of(const double4_32a&) { return 0; }

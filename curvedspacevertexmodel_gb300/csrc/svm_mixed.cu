@@ -98,9 +98,10 @@ __device__ __forceinline__ F3 vertex_force32(const Args32& A, int v, float R) {
 __device__ __forceinline__ float4 move_fp64(float4 p, F3 d, double R) {
     const F3 pf = f3(p);
     const F3 dt = d - (dotf(d, pf) / dotf(pf, pf)) * pf;
-    const double qx = (double)p.x + (double)dt.x, qy = (double)p.y + (double)dt.y, qz = (double)p.z + (double)dt.z;
+    const double qx = sf::widen(p.x) + sf::widen(dt.x), qy = sf::widen(p.y) + sf::widen(dt.y),
+                 qz = sf::widen(p.z) + sf::widen(dt.z);
     const double k = R * rsqrt(qx * qx + qy * qy + qz * qz);
-    return make_float4(__double2float_rn(k * qx), __double2float_rn(k * qy), __double2float_rn(k * qz), p.w);
+    return make_float4(sf::narrow(k * qx), sf::narrow(k * qy), sf::narrow(k * qz), p.w);
 }
 
 // Philox4x32-10 (Salmon et al., SC'11), as in the FP64 form.
@@ -134,7 +135,7 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
     const float4 p = pos[v];
-    const float R = (float)repR[rep_of(p)];
+    const float R = sf::narrow(repR[rep_of(p)]);
     const D3 pd = ld3(pos, v);
     const int4 cells = vcell[v], lasts = vlast[v], nexts = vnext[v], rp = vrpos[v], nb = vnbr[v];
     // per neighbour: FP64 cross product with p and its norm (for the included angles), FP32 arc
@@ -144,9 +145,9 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         const float4 q = pos[comp(nb, j)];
-        U[j] = D3{(double)q.x, (double)q.y, (double)q.z};
+        U[j] = D3{sf::widen(q.x), sf::widen(q.y), sf::widen(q.z)};
         C[j] = cross3(pd, U[j]);
-        nC[j] = sqrt(dot3(C[j], C[j]));
+        nC[j] = f64_sqrt(dot3(C[j], C[j]));
         arc[j] = arc32(q, p, R);
     }
 #pragma unroll
@@ -154,11 +155,11 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
         const int jl = nbr_slot(nb, comp(lasts, s)), jx = nbr_slot(nb, comp(nexts, s));
         double2 cr;
         if (jl >= 0 && jx >= 0) {
-            cr = make_double2((double)pick3(arc, jl), included_angle_pre<true>(pick3(C, jx), pick3(C, jl),
+            cr = make_double2(sf::widen(pick3(arc, jl)), included_angle_pre<true>(pick3(C, jx), pick3(C, jl),
                                                                                pick3(nC, jx), pick3(nC, jl), pick3(U, jl)));
         } else {  // inconsistent lists: evaluate directly
             const int L = comp(lasts, s), X = comp(nexts, s);
-            cr = make_double2((double)arc32(pos[L], p, R), included_angle_clamped(ld3(pos, L), pd, ld3(pos, X)));
+            cr = make_double2(sf::widen(arc32(pos[L], p, R)), included_angle_clamped(ld3(pos, L), pd, ld3(pos, X)));
         }
         corner[(long)comp(cells, s) * Wc + comp(rp, s)] = cr;
     }
@@ -179,7 +180,7 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
 __global__ void k32_force(Args32 A, int nV, float4* __restrict__ force) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nV) return;
-    const F3 f = vertex_force32(A, v, (float)A.repR[rep_of(A.pos[v])]);
+    const F3 f = vertex_force32(A, v, sf::narrow(A.repR[rep_of(A.pos[v])]));
     force[v] = make_float4(f.x, f.y, f.z, 0.f);
 }
 
@@ -194,10 +195,10 @@ __global__ void k32_force_bd(Args32 A, int nV, float4* __restrict__ force, float
     const float4 p = A.pos[v];
     const int rep = rep_of(p);
     const double R = A.repR[rep];
-    const F3 f = vertex_force32(A, v, (float)R);
+    const F3 f = vertex_force32(A, v, sf::narrow(R));
     force[v] = make_float4(f.x, f.y, f.z, 0.f);
     F3 xi;
-    if (kNoise == SVM_NOISE_BUFFER) xi = F3{(float)noise[3 * v], (float)noise[3 * v + 1], (float)noise[3 * v + 2]};
+    if (kNoise == SVM_NOISE_BUFFER) xi = F3{sf::narrow(noise[3 * v]), sf::narrow(noise[3 * v + 1]), sf::narrow(noise[3 * v + 2])};
     else xi = normals32(seed, *stepCounter, v);
     const float a = repNp ? repNp[rep] : np;
     posNext[v] = move_fp64(p, a * xi + fp * f, R);

@@ -316,7 +316,7 @@ __global__ void k_cells(const PT* __restrict__ pos, const int* __restrict__ ring
         ap[c] = make_double2(area, per);
         if (dap32) {
             const double2 pr = pref[c];
-            dap32[c] = make_float2((float)(area - pr.x), (float)(per - pr.y));
+            dap32[c] = make_float2(sf::narrow(area - pr.x), sf::narrow(per - pr.y));
         }
     }
     if (!ticket) return;
@@ -372,7 +372,7 @@ __global__ void k_fallback(const PT* __restrict__ pos, const int* __restrict__ r
         cur = next;
     }
     ap[c].x = area;
-    if (dap32) dap32[c].x = (float)(area - pref[c].x);
+    if (dap32) dap32[c].x = sf::narrow(area - pref[c].x);
 }
 
 // k_fallback with a block's fan triangles packed densely over its threads (the triangle areas are
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(kFanThreads) k_fallback_fan(
     double area = 0.0;
     for (int k = 0; k < cnt[t]; ++k) area += tri[off[t] + k];
     ap[c].x = area;
-    if (dap32) dap32[c].x = (float)(area - pref[c].x);
+    if (dap32) dap32[c].x = sf::narrow(area - pref[c].x);
 }
 
 // ---- forces and integration ------------------------------------------------------------------

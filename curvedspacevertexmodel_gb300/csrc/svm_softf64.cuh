@@ -19,6 +19,8 @@
 //         reciprocal, then corrected against the exact integer remainder and rounded from it.
 //   sqrt  reciprocal square root: an FP32 seed, two Newton-Raphson steps r <- r (3 - x r^2) / 2 in
 //         64-bit fixed point; the root from it, corrected against the exact integer remainder.
+//   widen / narrow  float <-> double by moving the fields (narrow: round to nearest even on the
+//         29 dropped bits).
 // (Newton-Raphson refinement of reciprocals and the final correction by an exact remainder are the
 // classical methods of P. Markstein, "IA-64 and Elementary Functions", 2000, and of integer
 // division by invariant integers, T. Granlund and P. Montgomery, PLDI 1994.)
@@ -251,6 +253,63 @@ SF_HD double sqrt(double a) {
         return pack(0ull, E, s >> 1, rest);
     }
     return hw_sqrt(a);
+}
+
+// Conversions between float and double, on the integer pipes (conversion instructions with a 64-bit
+// operand issue on GB300's FP64 pipe, at its rate).  widen is exact; narrow rounds to nearest even.
+// Zeros, subnormals, infinities and NaN -- and doubles outside the normal float range -- take the
+// hardware conversion.
+SF_HD unsigned f32bits(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    unsigned u;
+    __builtin_memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+SF_HD float f32of(unsigned u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    __builtin_memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+SF_HD double hw_widen(float f) {
+#if defined(__CUDA_ARCH__)
+    return (double)f;
+#else
+    volatile double r = (double)f;
+    return r;
+#endif
+}
+SF_HD float hw_narrow(double d) {
+#if defined(__CUDA_ARCH__)
+    return __double2float_rn(d);
+#else
+    volatile float r = (float)d;
+    return r;
+#endif
+}
+SF_HD double widen(float f) {
+    const unsigned u = f32bits(f), e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return hw_widen(f);
+    // sign, exponent rebiased by 1023 - 127, the 23 significand bits on top of the double's 52
+    return dbl(((unsigned long long)(u & 0x80000000u) << 32) | ((unsigned long long)(e + 896u) << 52) |
+               ((unsigned long long)(u & 0x7fffffu) << 29));
+}
+SF_HD float narrow(double d) {
+    const unsigned long long b = bits(d);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 126 || e > 1023 + 127) return hw_narrow(d);
+    // 23 significand bits kept, 29 rounded: to nearest, ties to even; a carry out of the
+    // significand raises the exponent (up to infinity from the largest binade), as IEEE rounding does
+    const unsigned m = (unsigned)((b >> 29) & 0x7fffffu), r = (unsigned)(b & 0x1fffffffu);
+    unsigned f = ((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)(e - 896) << 23) | m;
+    if (r > 0x10000000u || (r == 0x10000000u && (m & 1u))) f += 1u;
+    return f32of(f);
 }
 
 }  // namespace sf

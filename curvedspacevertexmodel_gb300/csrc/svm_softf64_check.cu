@@ -1,5 +1,5 @@
 // svm_softf64_check: the device build of svm_softf64.cuh against the hardware's correctly rounded
-// FP64 instructions, on random operands.  A diagnostic entry point (no counterpart in the
+// FP64 instructions and conversions, on random operands.  A diagnostic entry point (no counterpart in the
 // reference): the FP64 kernels' divisions and square roots go through these functions.
 #include <cuda_runtime.h>
 #include "svm_softf64.cuh"
@@ -16,7 +16,7 @@ __device__ unsigned long long splitmix(unsigned long long z) {  // splitmix64 (S
 __device__ bool same_bits(double x, double y) { return (x != x && y != y) || sf::bits(x) == sf::bits(y); }
 
 __global__ void k_softf64_check(unsigned long long seed, long long cases, unsigned long long* bad) {
-    unsigned nb[4] = {0, 0, 0, 0};
+    unsigned nb[6] = {0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cases; i += stride) {
         const unsigned long long k = seed ^ ((unsigned long long)i * 8ull);
@@ -36,23 +36,33 @@ __global__ void k_softf64_check(unsigned long long seed, long long cases, unsign
         nb[1] += !same_bits(sf::add(a, b), __dadd_rn(a, b));
         nb[2] += !same_bits(sf::div(a, b), __ddiv_rn(a, b));
         nb[3] += !same_bits(sf::sqrt(fabs(a)), __dsqrt_rn(fabs(a)));
+        // conversions: a float from the low word of ua (any bit pattern), and a double whose 29
+        // dropped bits sit at, next to or away from a rounding tie (mode 7: the largest binade)
+        const float f = sf::f32of((unsigned)ua);
+        nb[4] += !same_bits(sf::widen(f), (double)f);
+        unsigned long long ud = ub;
+        if (mode & 1) ud = (ud & ~0x1FFFFFFFull) | (0x10000000ull + (r >> 40) % 5) - 2;
+        if (mode == 7) ud = (ud & ~(0x7FFull << 52)) | (1150ull << 52) | 0xFFFFFE0000000ull;
+        const double dn = sf::dbl(ud);
+        const float fn = sf::narrow(dn), fh = __double2float_rn(dn);
+        nb[5] += !((fn != fn && fh != fh) || sf::f32bits(fn) == sf::f32bits(fh));
     }
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < 6; ++q)
         if (nb[q]) atomicAdd(bad + q, (unsigned long long)nb[q]);
 }
 
 }  // namespace
 
-extern "C" int svm_softf64_check(long long cases, unsigned long long seed, unsigned long long* mismatches4) {
-    if (cases < 0 || !mismatches4) return SVM_ERR_ARG;
+extern "C" int svm_softf64_check(long long cases, unsigned long long seed, unsigned long long* mismatches6) {
+    if (cases < 0 || !mismatches6) return SVM_ERR_ARG;
     unsigned long long* d = nullptr;
-    if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return SVM_ERR_CUDA;
-    cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+    if (cudaMalloc(&d, 6 * sizeof(unsigned long long)) != cudaSuccess) return SVM_ERR_CUDA;
+    cudaMemset(d, 0, 6 * sizeof(unsigned long long));
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     k_softf64_check<<<8 * (sms > 0 ? sms : 1), 256>>>(seed, cases, d);
     const bool ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
-                    cudaMemcpy(mismatches4, d, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) == cudaSuccess;
+                    cudaMemcpy(mismatches6, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) == cudaSuccess;
     cudaFree(d);
     return ok ? SVM_OK : SVM_ERR_CUDA;
 }

@@ -447,10 +447,11 @@ int svm_mlp_warm_start(svm_mlp* mlp, svm_model* m);
 
 /* ---- diagnostics ---------------------------------------------------------------------------
  * The FP64 kernels compute their divisions and square roots with integer-pipe IEEE arithmetic
- * (csrc/svm_softf64.cuh; no counterpart in the reference).  svm_softf64_check runs that device code
- * against the hardware's correctly rounded instructions on `cases` random operand pairs per
- * operation and returns the mismatches of multiply, add, divide and square root (all zero). */
-int svm_softf64_check(long long cases, unsigned long long seed, unsigned long long* mismatches4);
+ * (csrc/svm_softf64.cuh; no counterpart in the reference), and the FP32-bulk form's float <-> double
+ * conversions likewise.  svm_softf64_check runs that device code against the hardware's correctly
+ * rounded instructions on `cases` random operands per operation and returns the mismatches of
+ * multiply, add, divide, square root, widening and narrowing (all zero). */
+int svm_softf64_check(long long cases, unsigned long long seed, unsigned long long* mismatches6);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,8 @@
 // Host check of csrc/svm_softf64.cuh: every operation against the host's IEEE operations on random
 // operands (any bit patterns, exponents near 1, near-cancelling pairs, short significands, divisors
-// next to powers of two) and on exact cases (products divided back, squares).  Prints the number of
-// mismatches per operation; exit status 1 if any.   Usage: softf64_check [cases]
+// next to powers of two) and on exact cases (products divided back, squares); the float <-> double
+// conversions likewise.  Prints the number of mismatches per operation; exit status 1 if any.
+//   Usage: softf64_check [cases]
 #include "svm_softf64.cuh"
 #include <cmath>
 #include <cstdio>
@@ -40,7 +41,32 @@ int main(int argc, char** argv) {
         bad[2] += !same(sf::div(p, y), sf::hw_div(p, y));
         bad[3] += !same(sf::sqrt(s), sf::hw_sqrt(s));
     }
-    std::printf("{\"cases\": %ld, \"mul\": %ld, \"add\": %ld, \"div\": %ld, \"sqrt\": %ld, \"sub\": %ld}\n", n, bad[0],
-                bad[1], bad[2], bad[3], bad[4]);
-    return (bad[0] | bad[1] | bad[2] | bad[3] | bad[4]) ? 1 : 0;
+    // conversions: every float bit pattern at a stride (plus every pattern of the special and the
+    // smallest exponents), and doubles around the float range, at and next to rounding ties
+    long badW = 0, badN = 0;
+    auto sameF = [](float x, float y) { return (x != x && y != y) || sf::f32bits(x) == sf::f32bits(y); };
+    for (unsigned long long u = 0; u < (1ull << 32); u += 251) {
+        const float f = sf::f32of((unsigned)u);
+        badW += !same(sf::widen(f), sf::hw_widen(f));
+    }
+    for (unsigned e : {0u, 1u, 254u, 255u})
+        for (unsigned m = 0; m < (1u << 23); m += 7)
+            for (unsigned sgn : {0u, 0x80000000u}) {
+                const float f = sf::f32of(sgn | (e << 23) | m);
+                badW += !same(sf::widen(f), sf::hw_widen(f));
+            }
+    for (long i = 0; i < n; ++i) {
+        const unsigned long long r = g();
+        unsigned long long u = g();
+        if (i % 2) u = (u & (sf::kMant | sf::kSign)) | ((unsigned long long)(1023 - 150 + (int)(r % 300)) << 52);
+        if (i % 5 == 1) u = (u & ~0x1FFFFFFFull) | 0x10000000ull;                      // exact tie
+        if (i % 5 == 2) u = (u & ~0x1FFFFFFFull) | (0x10000000ull + (r >> 40) % 5) - 2;  // next to a tie
+        if (i % 5 == 3) u = (u & ~0x1FFFFFFFull) | 0x1FFFFFFFull;                        // carries upwards
+        if (i % 7 == 0) u = (u & ~(0x7FFull << 52)) | ((unsigned long long)(1023 + 127) << 52) | 0xFFFFFE0000000ull;
+        const double d = sf::dbl(u);
+        badN += !sameF(sf::narrow(d), sf::hw_narrow(d));
+    }
+    std::printf("{\"cases\": %ld, \"mul\": %ld, \"add\": %ld, \"div\": %ld, \"sqrt\": %ld, \"sub\": %ld, "
+                "\"widen\": %ld, \"narrow\": %ld}\n", n, bad[0], bad[1], bad[2], bad[3], bad[4], badW, badN);
+    return (bad[0] | bad[1] | bad[2] | bad[3] | bad[4] | badW | badN) ? 1 : 0;
 }

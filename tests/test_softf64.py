@@ -25,15 +25,15 @@ def test_softf64_bit_exact_on_the_host():
                         os.path.join(ROOT, "tests", "native", "softf64_check.cpp"), "-o", exe], check=True)
         r = subprocess.run([exe, "1500000"], capture_output=True, text=True, timeout=300)
     out = json.loads(r.stdout)
-    assert r.returncode == 0 and all(out[k] == 0 for k in ("mul", "add", "div", "sqrt", "sub")), out
+    assert r.returncode == 0 and all(out[k] == 0 for k in ("mul", "add", "div", "sqrt", "sub", "widen", "narrow")), out
 
 
 @pytest.mark.gpu
 def test_softf64_bit_exact_on_the_device(svm_lib):
     """2^28 random operand pairs per operation (every bit pattern, exponents near 1, near-cancelling
-    pairs, short significands, divisors next to powers of two), the device functions against the
-    hardware's correctly rounded instructions."""
+    pairs, short significands, divisors next to powers of two; conversions at and next to rounding
+    ties), the device functions against the hardware's correctly rounded instructions."""
     from curvedspacevertexmodel_gb300 import _lib
-    bad = np.zeros(4, dtype=np.uint64)
+    bad = np.zeros(6, dtype=np.uint64)
     _lib.call("svm_softf64_check", 1 << 28, 7, bad.ctypes.data)
     assert not bad.any(), bad
