@@ -47,14 +47,16 @@ __global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force(ForceA
     st3(force, v, f);
 }
 
-// Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext.
+// Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext (and
+// hostOut, when non-null).
 template <int kNoise>
 __global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force_bd(
                                                              ForceArgs A, int nV, double4_32a* __restrict__ force,
                                                              double4_32a* __restrict__ posNext,
                                                              const double* __restrict__ noise, uint64_t seed,
                                                              const unsigned long long* __restrict__ stepCounter,
-                                                             double np, double fp, const ZigTable* __restrict__ zig) {
+                                                             double np, double fp, const ZigTable* __restrict__ zig,
+                                                             double* __restrict__ hostOut) {
     __shared__ SlotShared sh;
     const D3 f = block_slot_force(A, nV, sh);
     const int v = blockIdx.x * kSlotVerts + threadIdx.x;
@@ -64,7 +66,10 @@ __global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force_bd(
     if (kNoise == SVM_NOISE_BUFFER) xi = D3{noise[3 * v], noise[3 * v + 1], noise[3 * v + 2]};
     else xi = philox_normals3(zig, seed, *stepCounter, v);
     const D3 d{bd_disp(xi.x, np, f.x, fp), bd_disp(xi.y, np, f.y, fp), bd_disp(xi.z, np, f.z, fp)};
-    st3(posNext, v, move_exact(ld3(A.pos, v), d, A.R));
+    const D3 q = move_exact(ld3(A.pos, v), d, A.R);
+    st3(posNext, v, q);
+    // a host-buffer step's output, straight into the caller's mapped page-locked array (AoS)
+    if (hostOut) { hostOut[3 * v] = q.x; hostOut[3 * v + 1] = q.y; hostOut[3 * v + 2] = q.z; }
 }
 
 }  // namespace
@@ -101,10 +106,12 @@ int launch_force_bd_fp64(svm_model* m, double np, double fp, int noiseMode, cons
     const ZigTable* zig = gZigAddr[dev];
     if (noiseMode == SVM_NOISE_BUFFER)
         k_force_bd<SVM_NOISE_BUFFER><<<nb, 3 * kSlotVerts, 0, m->stream>>>(
-            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp, zig);
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp, zig,
+            m->ioHostOut);
     else
         k_force_bd<SVM_NOISE_PHILOX><<<nb, 3 * kSlotVerts, 0, m->stream>>>(
-            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp, zig);
+            force_args(m, m->cur), m->nVertices, m->force, m->pos[nxt], noise, seed, m->stepCounter, np, fp, zig,
+            m->ioHostOut);
     return check_launch();
 }
 

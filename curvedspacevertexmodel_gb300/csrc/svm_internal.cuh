@@ -432,6 +432,8 @@ struct svm_model {
     std::vector<svm_fire*> fires;
     double* noiseBuf = nullptr;        // [3*Nv] staging for host-supplied noise / displacements
     double* dispBuf = nullptr;         // [3*Nv]
+    double* ioHostOut = nullptr;       // while a host-buffer step is issued: the caller's mapped output
+                                       // positions (AoS), written by the force kernel and the T1 patch
     // reductions: per-block partials + ticket (last-block-done pattern)
     double* partials = nullptr;
     double* dotPartials = nullptr;     // svm_reduce_dots: 4 per block of 64 vertices (allocated on first use)

@@ -495,6 +495,8 @@ struct ApplyArgs {
     int barrierSpins;      // polls of a grid-barrier wait before it gives up
     int* ringMax;          // largest ring count produced (atomicMax by the commits)
     int* ringMaxOut;       // host-visible copy, written once per pass by k_t1_patch
+    double* hostOut;       // a host-buffer step's mapped AoS output (FP64 form), else null: k_t1_patch
+                           // rewrites the vertices the pass may have moved
 };
 
 __device__ __forceinline__ int& compRef(int4* a, int v, int s) { return reinterpret_cast<int*>(a + v)[s]; }
@@ -880,9 +882,20 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
     }
     // appends past the list's capacity roll the pass back; a pass cut short by an exhausted barrier
     // wait may leave the counter above it, and only the stored entries are read
-    const int nt = min(*(volatile int*)(t1.ctr + 5), t1.touchedCap);
+    const int ntRaw = *(volatile int*)(t1.ctr + 5);
+    const int nt = min(ntRaw, t1.touchedCap);
+    const long gs = (long)gridDim.x * blockDim.x, g0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    // A host-buffer step's output: the force kernel wrote the moved positions; the flips moved
+    // vertices of the touched cells, whose ring entries below rewrite them.  A list that may have
+    // lost entries (full) rewrites every vertex instead.
+    const bool hostAll = A.hostOut && ntRaw > t1.touchedCap - 4;
+    if (hostAll)
+        for (long v = g0; v < A.nV; v += gs) {
+            const D3 p = ld3(A.pos, (int)v);
+            A.hostOut[3 * v] = p.x; A.hostOut[3 * v + 1] = p.y; A.hostOut[3 * v + 2] = p.z;
+        }
     const long total = (long)nt * A.Wc;
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    for (long e = g0; e < total; e += gs) {
         const int cell = t1.touched[e / A.Wc], k = (int)(e % A.Wc);
         const int n = A.ringCount[cell];
         if (k >= n) continue;
@@ -896,6 +909,7 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
                 compRef(A.vnext, u, s) = next;
             }
         const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
+        if (A.hostOut && !hostAll) { A.hostOut[3L * u] = p.x; A.hostOut[3L * u + 1] = p.y; A.hostOut[3L * u + 2] = p.z; }
         if (A.pos32) {
             A.corner[(long)cell * A.Wc + k] =
                 make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped(pl, p, px));
@@ -1752,6 +1766,7 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     A.Wc = m->Wc; A.nV = m->nVertices; A.nC = m->nCells; A.R = m->R; A.t1Threshold = m->t1Threshold;
     A.status = m->status; A.stepCounter = m->stepCounter; A.bumpStep = bump;
     A.ringMax = m->ringMax; A.ringMaxOut = m->ringMaxHostDev; A.barrierSpins = m->t1WaitLimit;
+    A.hostOut = A.pos32 ? nullptr : m->ioHostOut;
     t1_bracket(m->t1Threshold, m->R, &A.cosLo, &A.cosHi);
     t1_sin2_bracket(m->t1Threshold, m->R, &A.s2Lo, &A.s2Hi);
     return A;
@@ -2649,15 +2664,25 @@ static bool pinned(const void* p) {
 }  // namespace svm
 
 static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
-                            double* posOut, double* energyOut);
+                            double* posOut, double* energyOut, double* hostOut);
+// The device address of a mapped page-locked output array for the FP64 forms' host-buffer step, else
+// null (pageable memory, or the mixed form, whose output goes through a conversion and a copy).
+// Resolved outside any stream capture.
+static double* io_mapped_out(svm_model* m, double* posOut) {
+    if (!posOut || m->precision == SVM_PRECISION_MIXED) return nullptr;
+    void* dp = nullptr;
+    if (cudaHostGetDevicePointer(&dp, posOut, 0) == cudaSuccess) return (double*)dp;
+    cudaGetLastError();
+    return nullptr;
+}
 
 int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
                          double* posOut, double* energyOut) {
     if (!m) return SVM_ERR_ARG;
-    // With both position buffers page-locked (and no per-phase profiling) the whole sequence,
-    // copies included, is one graph launch: captured once per position-buffer role and reused
-    // while the parameters, buffers and form stay the same.  The energy lands in a page-locked slot
-    // of the model and is copied out after the synchronisation.
+    // With both position buffers page-locked (and no per-phase profiling) the whole sequence, the
+    // upload included, is one graph launch: captured once per position-buffer role and reused while
+    // the parameters, buffers and form stay the same.  The energy lands in a page-locked slot of the
+    // model and is copied out after the synchronisation.
     if (posIn && posOut && m->nRep == 1 && !m->prof && svm::pinned(posIn) && svm::pinned(posOut)) {
         if (!m->ioEnergy && cudaMallocHost((void**)&m->ioEnergy, sizeof(double)) != cudaSuccess) {
             m->ioEnergy = nullptr;
@@ -2667,6 +2692,7 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
         if (!m->restricted) {
             if (int rc = svm::ensure_ring_headroom(m)) return rc;
         }
+        double* hostOut = io_mapped_out(m, posOut);
         auto& g = m->ioGraph[m->cur];
         const bool reuse = g.exec && g.T == T && g.dt == dt && g.mu == mu && g.seed == seed && g.in == posIn &&
                            g.out == posOut && g.version == m->paramsVersion && g.precision == m->precision;
@@ -2675,7 +2701,7 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
             if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
             cudaGraph_t graph;
             SVM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-            const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, m->ioEnergy);
+            const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, m->ioEnergy, hostOut);
             cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
             m->cur = cur0;
             if (rc || ce != cudaSuccess) { cudaGetLastError(); return rc ? rc : SVM_ERR_CUDA; }
@@ -2693,7 +2719,7 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
         if (energyOut) *energyOut = *m->ioEnergy;
         return SVM_OK;
     }
-    const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, energyOut);
+    const int rc = step_io_sequence(m, T, dt, mu, seed, posIn, posOut, energyOut, io_mapped_out(m, posOut));
     if (rc) return rc;
     SVM_CUDA(cudaStreamSynchronize(m->stream));
     return SVM_OK;
@@ -2701,7 +2727,7 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
 
 // The launches of one host-io step, in stream order (no synchronisation).
 static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
-                            double* posOut, double* energyOut) {
+                            double* posOut, double* energyOut, double* hostOut) {
     const bool mixedForm = m->precision == SVM_PRECISION_MIXED;
     if (posIn) {
         SVM_CUDA(cudaMemcpyAsync(m->dispBuf, posIn, sizeof(double) * 3 * m->nVertices, cudaMemcpyHostToDevice, m->stream));
@@ -2713,8 +2739,13 @@ static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64
         }
         m->cornersValid = false;
     }
+    // with a mapped output array (hostOut, io_mapped_out) the force kernel and the T1 patch write the
+    // moved positions into it directly, the force kernel's stores hidden under its FP64 work, so no
+    // copy follows the step
+    m->ioHostOut = hostOut;
     // a caller that passes positions in is likely to replace them again before the next step
     int rc = svm::bd_step(m, T, dt, mu, SVM_NOISE_PHILOX, nullptr, seed, posIn != nullptr);
+    m->ioHostOut = nullptr;
     if (rc) return rc;
     if (energyOut) {
         k_energy<<<svm::blocksFor(m->nCells), svm::kBlock, 0, m->stream>>>(m->ap, m->pref, m->Kr, m->nCells,
@@ -2723,7 +2754,7 @@ static int step_io_sequence(svm_model* m, double T, double dt, double mu, uint64
         if (svm::check_launch()) return SVM_ERR_CUDA;
         SVM_CUDA(cudaMemcpyAsync(energyOut, m->scalars + 2, sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     }
-    if (posOut) {
+    if (posOut && !hostOut) {
         if (mixedForm) {
             if (svm::mixed_download(m, m->pos32[m->cur], m->nVertices, m->dispBuf)) return SVM_ERR_CUDA;
         } else {

@@ -281,7 +281,9 @@ int svm_brownian_step_host_noise(svm_model* m, double T, double dt, double mu, c
  * synchronisation: positions[3 nV] uploaded from posIn (NULL: keep the device state), the step,
  * *energyOut = the energy of the geometry the step's forces used (what svm_model_compute_energy
  * returns after a step; computeEnergy, sphericalVertexModel.cpp:150-160), and the new positions
- * copied to posOut (NULL: none).  Pinned host buffers make the copies asynchronous DMA. */
+ * in posOut (NULL: none).  Pinned host buffers make the upload asynchronous DMA; in the FP64 forms
+ * a page-locked (mapped) posOut is written by the step's own kernels -- the force kernel as it
+ * moves the vertices, the T1 pass for the vertices its flips move -- so no copy follows the step. */
 int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t seed, const double* posIn,
                          double* posOut, double* energyOut);
 /* nSteps timesteps with Philox noise, launched as a captured CUDA graph. */
