@@ -238,8 +238,10 @@ __global__ void __launch_bounds__(3 * kCornerVerts) k_corner_s(
 
 // Per vertex: for each of its three cells, the arc from the ring predecessor and the included
 // angle at the vertex (the per-corner terms of computeGeometryCPU, sphericalVertexModel.cpp:257-276)
-// from the edge terms of k_edges.
-__global__ void k_corner(const double4_32a* __restrict__ pos, const int4* __restrict__ vcell,
+// from the edge terms of k_edges.  Compiled for three blocks of 256 per SM (80 registers, with some
+// spill, instead of 114 at two): the FP64-bound kernel's last of 2.6 waves shrinks (159 against 162 us
+// per corner phase at 100k cells).
+__global__ void __launch_bounds__(256, 3) k_corner(const double4_32a* __restrict__ pos, const int4* __restrict__ vcell,
                          const int4* __restrict__ vlast, const int4* __restrict__ vnext, const int4* __restrict__ vrpos,
                          const int4* __restrict__ vnbr, const double4_32a* __restrict__ edgeC,
                          const double* __restrict__ edgeArc, double2* __restrict__ corner, int Wc, int nV, double R) {
