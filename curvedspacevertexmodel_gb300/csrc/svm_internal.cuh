@@ -93,6 +93,29 @@ __device__ __forceinline__ double dot3(D3 a, D3 b) { double s = a.x * b.x; s += 
 __device__ __forceinline__ D3 cross3(D3 p1, D3 p2) {          // inc/functions.h:160-167
     return D3{p1.y * p2.z - p1.z * p2.y, p1.z * p2.x - p1.x * p2.z, p1.x * p2.y - p1.y * p2.x};
 }
+// A product on the integer pipes (sf::mul: the same bits as the hardware multiply) for the products
+// that start the FP64 kernels' dependency chains -- the pair terms of the geodesic and triangle-area
+// gradients, which depend only on the spherical coordinates, and the cross and dot products ahead of
+// the geometry's divisions and arccosines.  The FP64 pipe, which bounds the force
+// kernel, keeps the rest; the integer pipes, otherwise busy only with the divisions and square
+// roots, take these early, mutually independent products, whose latency the resident warps hide.
+// Measured at 100k cells: 0.476 -> 0.447 ms per force launch, and 0.442 with grad_triangle's
+// d/dtheta numerators, which are formed while the denominators' square roots run.  Moving the
+// d/dphi numerators too (chains of three products: 0.487 ms), the products at the end of
+// grad_triangle's chains (0.509 ms), all its products, or the pair terms' sums (0.531 ms) was slower.
+// The corner phase (k_edges' cross products and arcs, the included angles' products): 0.159 -> 0.151 ms.
+__device__ __forceinline__ double early_mul(double x, double y) { return sf::mul(x, y); }
+// dot3 and cross3 with their products on the integer pipes (the same bits)
+__device__ __forceinline__ double dot3e(D3 a, D3 b) {
+    double s = early_mul(a.x, b.x);
+    s += early_mul(a.y, b.y);
+    s += early_mul(a.z, b.z);
+    return s;
+}
+__device__ __forceinline__ D3 cross3e(D3 p1, D3 p2) {
+    return D3{early_mul(p1.y, p2.z) - early_mul(p1.z, p2.y), early_mul(p1.z, p2.x) - early_mul(p1.x, p2.z),
+              early_mul(p1.x, p2.y) - early_mul(p1.y, p2.x)};
+}
 __device__ __forceinline__ double det3(D3 a, D3 b, D3 c) {    // a . (b x c), sphericalDomain.h:123-125
     return a.x * (b.y * c.z - b.z * c.y) + a.y * (b.z * c.x - b.x * c.z) + a.z * (b.x * c.y - b.y * c.x);
 }
@@ -118,8 +141,7 @@ __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
 __device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
 // geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
 __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
-    const double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
-    return R * svm_acos(f64_div(num, n1 * n2));
+    return R * svm_acos(f64_div(dot3e(p1, p2), early_mul(n1, n2)));
 }
 // The T1 length test geodesic(p1, p2) < t, i.e. R acos(c) < t with c = p1.p2 / (|p1||p2|).  acos
 // is decreasing, so away from c = cos(t / R) the answer is c > cos(t / R); the formula itself is
@@ -197,8 +219,8 @@ __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
 // form keeps that behaviour).
 template <bool clamp = false>
 __device__ __forceinline__ double included_angle_pre(D3 Cx, D3 Cl, double nx, double nl, D3 pl) {
-    const double det = dot3(pl, Cx);
-    double c = f64_div(dot3(Cx, Cl), nx * nl);
+    const double det = dot3e(pl, Cx);
+    double c = f64_div(dot3e(Cx, Cl), early_mul(nx, nl));
     if (clamp) c = fmin(1.0, fmax(-1.0, c));
     double a = svm_acos(c);
     if (det > 0) a = -a;
@@ -248,16 +270,6 @@ __device__ __forceinline__ double4_32a sph_coords_n(D3 p, double r) {  // r = po
 }
 __device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n(p, pos_norm(p)); }
 
-// A product on the integer pipes (sf::mul: the same bits as the hardware multiply) for the products
-// that start the force's dependency chains -- the pair terms of the geodesic and triangle-area
-// gradients, which depend only on the spherical coordinates.  The FP64 pipe, which bounds the force
-// kernel, keeps the rest; the integer pipes, otherwise busy only with the divisions and square
-// roots, take these early, mutually independent products, whose latency the resident warps hide.
-// Measured at 100k cells: 0.476 -> 0.447 ms per force launch.  Moving the products at the end of
-// grad_triangle's chains (0.509 ms), all its products, or the pair terms' sums as well (0.531 ms)
-// was slower.
-__device__ __forceinline__ double early_mul(double x, double y) { return sf::mul(x, y); }
-
 // gradientGeodesicDistance (sphericalDomain.h:248-273) in the (theta, phi) basis of v1:
 // returns (d/dtheta, d/dphi) components.
 __device__ __forceinline__ double2 grad_geodesic(double4_32a s1, double4_32a s2) {
@@ -298,9 +310,10 @@ __device__ __forceinline__ double2 grad_triangle(double4_32a a, double4_32a b, d
     const double a12 = s12s12 - 1., a13 = s13s13 - 1.;
     const double den3 = f64_sqrt(M(M(M(M(a12, a13), a12), a13), g));
     const double s12s23 = M(s12, s23), s13s23 = M(s13, s23);
-    double gT = f64_div(M(d13, a12) + M(d12, s23 - s12s13), den1)
-              + f64_div(M(d12, a13) + M(d13, s23 - s12s13), den2)
-              - f64_div(M(M(d12, a13), s13 - s12s23) + M(M(d13, a12), s12 - s13s23), den3);
+    // the d/dtheta numerators are formed while the square roots of the denominators run: integer pipes
+    double gT = f64_div(E(d13, a12) + E(d12, s23 - s12s13), den1)
+              + f64_div(E(d12, a13) + E(d13, s23 - s12s13), den2)
+              - f64_div(E(E(d12, a13), s13 - s12s23) + E(E(d13, a12), s12 - s13s23), den3);
     gT = M(gT, R);
     double gP = f64_div(M(M(s12s13 - s23, sP12), b.y) - M(M(-1 + s12s12, sP13), c.y), den1)
               - f64_div(M(M(-1 + s13s13, sP12), b.y) + M(M(-s12s13 + s23, sP13), c.y), den2)

@@ -151,10 +151,10 @@ __global__ void k_edges(const double4_32a* __restrict__ pos, const double* __res
         else { j = 2; src = nth_set(b2, k - n0 - n1); }
         const int w = base + src, u = comp(vnbr[w], j);
         const D3 p = ld3(pos, w), U = ld3(pos, u);
-        const D3 C = cross3(p, U);
+        const D3 C = cross3e(p, U);
         const double arc = geodesic_n(U, p, vnorm[u], vnorm[w], R);
         const int e = 3 * w + j;
-        edgeC[e] = make_double4_32a(C.x, C.y, C.z, f64_sqrt(dot3(C, C)));
+        edgeC[e] = make_double4_32a(C.x, C.y, C.z, f64_sqrt(dot3e(C, C)));
         edgeArc[e] = arc;
         // geodesic(u, p) < t is the reference's test (sphericalVertexModel.cpp:475)
         if (t1test && arc < t1Threshold) {
