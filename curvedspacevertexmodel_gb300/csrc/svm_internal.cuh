@@ -103,7 +103,9 @@ __device__ __forceinline__ D3 cross3(D3 p1, D3 p2) {          // inc/functions.h
 // d/dtheta numerators, which are formed while the denominators' square roots run.  Moving the
 // d/dphi numerators too (chains of three products: 0.487 ms), the products at the end of
 // grad_triangle's chains (0.509 ms), all its products, or the pair terms' sums (0.531 ms) was slower.
-// The corner phase (k_edges' cross products and arcs, the included angles' products): 0.159 -> 0.151 ms.
+// The corner phase (k_edges' cross products and arcs, the included angles' products): 0.159 -> 0.151 ms;
+// the norms ahead of the centroids', vertices' and fan triangles' square roots: cells and fallback
+// phases 2-3% shorter.
 __device__ __forceinline__ double early_mul(double x, double y) { return sf::mul(x, y); }
 // dot3 and cross3 with their products on the integer pipes (the same bits)
 __device__ __forceinline__ double dot3e(D3 a, D3 b) {
@@ -122,7 +124,7 @@ __device__ __forceinline__ double det3(D3 a, D3 b, D3 c) {    // a . (b x c), sp
 
 // putInBoxReal (sphericalDomain.h:183-187): p <- R p / |p|
 __device__ __forceinline__ D3 renorm(D3 p, double R) {
-    double inv = f64_div(1.0, f64_sqrt(dot3(p, p)));
+    double inv = f64_div(1.0, f64_sqrt(dot3e(p, p)));
     return scl3(R, scl3(inv, p));
 }
 // move(p, v) (sphericalDomain.h:203-209): project v onto the tangent plane at p, add, renormalise
@@ -138,7 +140,7 @@ __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     return R * svm_acos(f64_div(num, den));
 }
 // |p| as geodesic and sph_coords evaluate it (same operations, so the same value)
-__device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt(p.x * p.x + p.y * p.y + p.z * p.z); }
+__device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt(dot3e(p, p)); }
 // geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
 __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
     return R * svm_acos(f64_div(dot3e(p1, p2), early_mul(n1, n2)));
@@ -244,14 +246,14 @@ __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
 }
 // sphericalTriangleArea (sphericalDomain.h:135-166)
 // q / |q| as sphericalTriangleArea normalises each corner
-__device__ __forceinline__ D3 unit_corner(D3 q) { return scl3(f64_div(1.0, f64_sqrt(dot3(q, q))), q); }
+__device__ __forceinline__ D3 unit_corner(D3 q) { return scl3(f64_div(1.0, f64_sqrt(dot3e(q, q))), q); }
 __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R);
 __device__ __forceinline__ double triangle_area(D3 q1, D3 q2, D3 q3, double R) {
     return triangle_area_unit(unit_corner(q1), unit_corner(q2), unit_corner(q3), R);
 }
 // the same from the normalised corners
 __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double R) {
-    double d12 = dot3(p1, p2), d13 = dot3(p1, p3), d23 = dot3(p2, p3);
+    double d12 = dot3e(p1, p2), d13 = dot3e(p1, p3), d23 = dot3e(p2, p3);
     double area = -kPI;
     area += svm_acos(f64_div(d23 - d12 * d13, f64_sqrt(1 - d12 * d12) * f64_sqrt(1 - d13 * d13)));
     area += svm_acos(f64_div(d12 - d13 * d23, f64_sqrt(1 - d13 * d13) * f64_sqrt(1 - d23 * d23)));
@@ -265,7 +267,7 @@ __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double
 __device__ __forceinline__ double4_32a sph_coords_n(D3 p, double r) {  // r = pos_norm(p)
     double cosT = f64_div(p.z, r);
     double sinT = f64_sqrt(1. - cosT * cosT);
-    double rxy = f64_sqrt(p.x * p.x + p.y * p.y);
+    double rxy = f64_sqrt(early_mul(p.x, p.x) + early_mul(p.y, p.y));
     return make_double4_32a(cosT, sinT, f64_div(p.x, rxy), f64_div(p.y, rxy));
 }
 __device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n(p, pos_norm(p)); }
