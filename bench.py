@@ -167,16 +167,18 @@ def algorithmic_bytes_step(nv: int) -> int:
 
 # From an ncu --set full capture of one k_force_bd launch at N = 100k cells (bench.py --mode profile
 # --cells 100000 --stab 2 --steps 1; profiles/k_force_bd_n100k_full.md): DRAM bytes read + written
-# per vertex by one launch, and the FP64 pipe's busy fraction in that kernel.
-FORCE_BD_DRAM_BYTES_PER_VERTEX = (32.219648e6 + 0.745728e6) / 199_996
-FORCE_BD_FP64_PIPE_PCT = 78.3
+# per vertex by one launch, and the FP64 and integer (ALU) pipes' busy fractions in that kernel.
+FORCE_BD_DRAM_BYTES_PER_VERTEX = (32.27776e6 + 0.608512e6) / 199_996
+FORCE_BD_FP64_PIPE_PCT = 67.7
+FORCE_BD_ALU_PIPE_PCT = 27.7
 # FP64 arithmetic thread operations (DMUL + DFMA + DADD) per vertex in one k_force_bd launch of the
 # build whose divisions and square roots are the hardware sequences (ncu at N = 100k), and the FP64
 # issue rate they are bound by: 16 SM cycles per FP64 warp instruction (ncu:
 # sm__pipe_fp64_cycles_active / sm__inst_executed_pipe_fp64 in every FP64 kernel), i.e. two lanes
 # per clock on each of the 152 SMs at the 2070 MHz maximum SM clock.  The default build computes the
-# divisions and square roots on the integer pipes (same results), so the rate below is
-# FP64-pipe-equivalent work: above 1 it would beat what the FP64 pipe alone can issue.
+# divisions and square roots, and the products that start the gradients' dependency chains, on the
+# integer pipes (same results), so the rate below is FP64-pipe-equivalent work: above 1 it does that
+# work faster than the FP64 pipe alone could issue it.
 FORCE_BD_FP64_OPS_PER_VERTEX = 1420
 FP64_LANES_PER_CLOCK_PER_SM = 2
 GB300_SMS = 152
@@ -375,9 +377,11 @@ def run_ours(args):
                      "traffic": traffic, "kernel": "k_force_bd" if names[dom] == "force" else f"k_{names[dom]}",
                      "peak_source": peak_kind,
                      "fp64_pipe_busy_pct_ncu": FORCE_BD_FP64_PIPE_PCT,
+                     "alu_pipe_busy_pct_ncu": FORCE_BD_ALU_PIPE_PCT,
                      "fp64": fp64_roofline(avg_launch_ms, nv) if names[dom] == "force" else None,
-                     "note": "FP64-issue bound (ncu: FP64 pipe 78% busy, DRAM under 1%; divisions and square roots "
-                             "on the integer pipes); HBM fraction is small by construction",
+                     "note": "FP64-issue and latency bound (ncu: FP64 pipe 68% and integer pipes 28% busy, DRAM "
+                             "under 1%; divisions, square roots and chain-starting products on the integer "
+                             "pipes); HBM fraction is small by construction",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
         "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
         "warm_l2_ms_per_step": warm_ms,
