@@ -146,8 +146,8 @@ __global__ void k32_corners(const float4* __restrict__ pos, const int4* __restri
     for (int j = 0; j < 3; ++j) {
         const float4 q = pos[comp(nb, j)];
         U[j] = D3{sf::widen(q.x), sf::widen(q.y), sf::widen(q.z)};
-        C[j] = cross3(pd, U[j]);
-        nC[j] = f64_sqrt(dot3(C[j], C[j]));
+        C[j] = cross3e(pd, U[j]);
+        nC[j] = f64_sqrt(dot3e(C[j], C[j]));
         arc[j] = arc32(q, p, R);
     }
 #pragma unroll
