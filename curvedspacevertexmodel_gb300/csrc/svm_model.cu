@@ -896,29 +896,51 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
             const D3 p = ld3(A.pos, (int)v);
             A.hostOut[3 * v] = p.x; A.hostOut[3 * v + 1] = p.y; A.hostOut[3 * v + 2] = p.z;
         }
-    const long total = (long)nt * A.Wc;
-    for (long e = g0; e < total; e += gs) {
-        const int cell = t1.touched[e / A.Wc], k = (int)(e % A.Wc);
-        const int n = A.ringCount[cell];
-        if (k >= n) continue;
-        const int* rg = A.ring + (long)cell * A.Wc;
-        const int u = rg[k];
-        const int last = rg[k == 0 ? n - 1 : k - 1], next = rg[k + 1 == n ? 0 : k + 1];
-        for (int s = 0; s < 3; ++s)
-            if (compRef(A.vcell, u, s) == cell) {
-                compRef(A.vrpos, u, s) = k;
-                compRef(A.vlast, u, s) = last;
-                compRef(A.vnext, u, s) = next;
+    // The touched cells go round-robin over the blocks (cell i to block i mod gridDim, 32 of a
+    // block's at a time), and each block packs its cells' ring entries onto consecutive threads: the
+    // few hundred cells of a pass then spread over all SMs, with every lane of a busy warp on a real
+    // entry (a flat index over (cell, slot < capacity) leaves most lanes and most SMs idle).
+    __shared__ int patchCell[32], patchOff[33];
+    for (int base = blockIdx.x; base < nt; base += 32 * gridDim.x) {
+        if (threadIdx.x < 32) {
+            const int i = base + (int)gridDim.x * (int)threadIdx.x;
+            const int cell = i < nt ? t1.touched[i] : -1;
+            const int cnt = cell >= 0 ? A.ringCount[cell] : 0;
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)threadIdx.x >= o) incl += y;
             }
-        const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
-        if (A.hostOut && !hostAll) { A.hostOut[3L * u] = p.x; A.hostOut[3L * u + 1] = p.y; A.hostOut[3L * u + 2] = p.z; }
-        if (A.pos32) {
-            A.corner[(long)cell * A.Wc + k] =
-                make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped(pl, p, px));
-        } else {
-            A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
-            A.vsph[u] = sph_coords(p);
+            patchCell[threadIdx.x] = cell;
+            patchOff[threadIdx.x] = incl - cnt;
+            if (threadIdx.x == 31) patchOff[32] = incl;
         }
+        __syncthreads();
+        for (int e = threadIdx.x; e < patchOff[32]; e += blockDim.x) {
+            int j = 0;
+            while (patchOff[j + 1] <= e) ++j;
+            const int cell = patchCell[j], k = e - patchOff[j];
+            const int n = A.ringCount[cell];
+            const int* rg = A.ring + (long)cell * A.Wc;
+            const int u = rg[k];
+            const int last = rg[k == 0 ? n - 1 : k - 1], next = rg[k + 1 == n ? 0 : k + 1];
+            for (int s = 0; s < 3; ++s)
+                if (compRef(A.vcell, u, s) == cell) {
+                    compRef(A.vrpos, u, s) = k;
+                    compRef(A.vlast, u, s) = last;
+                    compRef(A.vnext, u, s) = next;
+                }
+            const D3 pl = apos(A, last), p = apos(A, u), px = apos(A, next);
+            if (A.hostOut && !hostAll) { A.hostOut[3L * u] = p.x; A.hostOut[3L * u + 1] = p.y; A.hostOut[3L * u + 2] = p.z; }
+            if (A.pos32) {
+                A.corner[(long)cell * A.Wc + k] =
+                    make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped(pl, p, px));
+            } else {
+                A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
+                A.vsph[u] = sph_coords(p);
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1981,7 +2003,7 @@ int launch_t1_apply(svm_model* m, int bump) {
             m->t1.undoCap / nSeg);
     }
     k_t1_apply<<<1, kApplyThreads, 0, m->stream>>>(apply_args(m, bump), m->t1);
-    k_t1_patch<<<2 * 152, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
+    k_t1_patch<<<2 * m->sms, 256, 0, m->stream>>>(apply_args(m, bump), m->t1);
     if (int rc = check_launch()) return rc;
     return mark_pass(m);
 }
