@@ -282,3 +282,36 @@ def test_fire_fp64_vector_reaches_tight_tolerance(svm):
     assert st["max_force"] < 1e-9
     m.computeForces()
     assert np.max(np.linalg.norm(m.returnForces(), axis=1)) < 1e-9
+
+
+@pytest.mark.parametrize("form", ["mixed", "fp64_vector"])
+def test_host_buffer_steps_follow_the_step_loop(svm, form):
+    """Chained svm_brownian_step_io calls with page-locked buffers (each step's positions fed back
+    in) follow the device-resident step loop bit for bit in the mixed form (positions converted to
+    FP32 on the way in and widened on the way out, exactly) and in the FP64 vector form (positions
+    written into the mapped output by the step's kernels): positions, connectivity, flip count and
+    the energies each step reports."""
+    import ctypes as C
+    import torch
+    from curvedspacevertexmodel_gb300 import _lib
+    a, _ = stabilised(svm, 3000, seed=13, stab=40, steps=40)
+    b, _ = stabilised(svm, 3000, seed=13, stab=40, steps=40)
+    for m in (a, b):
+        m.precision = form
+        m.setT1Threshold(0.08)   # flips every step
+    a.t1Stats(), b.t1Stats()
+    n = 3 * a.nVertices
+    pos = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    out = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    pos[:] = a.returnPositions().reshape(-1)
+    e_io = C.c_double()
+    for k in range(20):
+        _lib.call("svm_brownian_step_io", a.handle, 0.05, 0.01, 1.0, 77, pos, out, C.byref(e_io))
+        _lib.call("svm_brownian_step", b.handle, 0.05, 0.01, 1.0, _lib.SVM_NOISE_PHILOX, None, 77)
+        assert e_io.value == b.computeEnergy(), k
+        pos, out = out, pos
+    assert np.array_equal(pos.reshape(-1, 3), b.returnPositions())
+    assert np.array_equal(a.vertexNeighbors(), b.vertexNeighbors())
+    fa, fb = a.t1Stats()["flips"], b.t1Stats()["flips"]
+    assert fa == fb and fa > 20
+    assert a.deviceStatus() == 0 and b.deviceStatus() == 0
