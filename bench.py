@@ -274,7 +274,7 @@ def run_ours(args):
     # ---- timed region: K steps, each after an L2 flush, events on the model's stream ----
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    _lib.call("svm_model_profile", model.handle, 1)
+    _lib.call("svm_model_profile", model.handle, force_only_mask())  # the force kernel's events only
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
@@ -297,6 +297,7 @@ def run_ours(args):
     t1stats = model.t1Stats()
     fallbacks_timed = model.fallbackCount()
     _lib.call("svm_model_profile", model.handle, 0)
+    phases = phase_breakdown(model, bd, stream, flush, args.steps)
     total_s, value = job_throughput(pg, float(sum(step_ms)) / 1e3, nv, args.steps, world)
     total_ms = 1e3 * total_s
     ms_per_step = total_ms / args.steps
@@ -383,7 +384,8 @@ def run_ours(args):
                              "under 1%; divisions, square roots and chain-starting products on the integer "
                              "pipes); HBM fraction is small by construction",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_launch_ms},
-        "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(names, ms)},
+        "phases_ms_per_step": phases,
+        "phases_note": "every phase bracketed by events, over as many further steps after the timed region",
         "warm_l2_ms_per_step": warm_ms,
         "t1_per_step": {k: v / args.steps for k, v in t1stats.items()},
         "wall_s": wall,
@@ -396,6 +398,31 @@ def run_ours(args):
         "fire_warm_start": fire,
     }
     print(json.dumps(out), flush=True)
+
+
+def force_only_mask():
+    from curvedspacevertexmodel_gb300 import _lib
+    return _lib.SVM_PROFILE_ONLY | (1 << _lib.PHASES.index("force"))
+
+
+def phase_breakdown(model, bd, stream, flush, steps):
+    """Milliseconds per step of every phase, from `steps` further steps (each after the L2 flush)
+    with every phase bracketed by events -- outside the timed region, whose steps carry only the
+    force kernel's pair of events (a pair per phase adds ~20 us to a step)."""
+    import numpy as np
+    import torch
+    from curvedspacevertexmodel_gb300 import _lib
+    ms = np.zeros(len(_lib.PHASES), dtype=np.float64)
+    launches = np.zeros(len(_lib.PHASES), dtype=np.int32)
+    _lib.call("svm_model_profile", model.handle, 1)
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        bd.integrateEquationOfMotion()
+    torch.cuda.synchronize()
+    _lib.call("svm_model_profile_read", model.handle, ms, launches)
+    _lib.call("svm_model_profile", model.handle, 0)
+    return {nm: float(t / steps) for nm, t in zip(_lib.PHASES, ms)}
 
 
 def time_fire(args, rank):
@@ -499,7 +526,7 @@ def time_mixed_form(args, model, bd, stream, flush, nv, nc):
     model.t1Stats()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    _lib.call("svm_model_profile", model.handle, 1)
+    _lib.call("svm_model_profile", model.handle, force_only_mask())
     torch.cuda.synchronize()
     for i in range(args.steps):
         with torch.cuda.stream(stream):
@@ -514,6 +541,7 @@ def time_mixed_form(args, model, bd, stream, flush, nv, nc):
     _lib.call("svm_model_profile", model.handle, 0)
     t1 = model.t1Stats()
     total_ms = float(sum(s.elapsed_time(e) for s, e in zip(starts, ends)))
+    phases = phase_breakdown(model, bd, stream, flush, args.steps)
     status = model.deviceStatus()
     model.computeGeometry()
     e = model.computeEnergy() / nc
@@ -524,7 +552,7 @@ def time_mixed_form(args, model, bd, stream, flush, nv, nc):
     alg = algorithmic_bytes_force_mixed(nv, nc)
     peak, peak_kind = peaks()
     return {"ms_per_step": total_ms / args.steps, "value": nv * args.steps / (total_ms / 1e3), "unit": UNIT,
-            "phases_ms_per_step": {nm: float(t / args.steps) for nm, t in zip(_lib.PHASES, ms)},
+            "phases_ms_per_step": phases,
             "force_kernel": {"kernel": "k32_force_bd", "avg_launch_ms": force_ms, "algorithmic_bytes_per_launch": alg,
                              "achieved_gbs": alg / (force_ms / 1e3) / 1e9,
                              "frac_of_" + peak_kind + "_hbm": alg / (force_ms / 1e3) / 1e9 / peak},

@@ -28,6 +28,7 @@ SVM_DEV_T1_TIMEOUT = 0x10
 SVM_NOISE_PHILOX = 0
 SVM_NOISE_BUFFER = 1
 PHASES = ("corners", "cells", "fallback", "force", "t1_apply", "move")
+SVM_PROFILE_ONLY = 0x100
 SVM_NOALLOC_MAX_CELLS = 2097152
 SVM_FIRE_RMS_OVER_N = 0
 SVM_FIRE_MAX_FORCE = 1

@@ -473,6 +473,7 @@ struct svm_model {
     int bdGraphCur = -1;
     // per-phase event timing (svm_model_profile)
     bool prof = false;
+    int profMask = 0xff;               // phases bracketed by events while profiling (bit per phase)
     std::vector<cudaEvent_t> profEvents[SVM_PHASE_COUNT];   // start/stop pairs, in launch order
     int profUsed[SVM_PHASE_COUNT] = {0};
     double profMs[SVM_PHASE_COUNT] = {0};
@@ -499,7 +500,8 @@ namespace svm {
 struct PhaseTimer {
     svm_model* m;
     int phase;
-    bool on;
+    bool on;       // profiling on: the phase's launches are counted
+    bool timed;    // and bracketed by events (the phase is in the profile mask)
     PhaseTimer(svm_model* m_, int phase_, int kernels = 1);
     ~PhaseTimer();
 };

@@ -52,8 +52,14 @@ static void profile_drain(svm_model* m) {
     }
 }
 
-PhaseTimer::PhaseTimer(svm_model* m_, int phase_, int kernels) : m(m_), phase(phase_), on(m_->prof && !capturing(m_->stream)) {
+PhaseTimer::PhaseTimer(svm_model* m_, int phase_, int kernels)
+    : m(m_), phase(phase_), on(m_->prof && !capturing(m_->stream)), timed(false) {
     if (!on) return;
+    timed = ((m->profMask >> phase) & 1) != 0;
+    if (!timed) {  // counted, not timed
+        m->profLaunches[phase] += kernels;
+        return;
+    }
     auto& ev = m->profEvents[phase];
     if (m->profUsed[phase] + 2 > 512) profile_drain(m);
     m->profKernels[phase].push_back(kernels);
@@ -65,7 +71,7 @@ PhaseTimer::PhaseTimer(svm_model* m_, int phase_, int kernels) : m(m_), phase(ph
     cudaEventRecord(ev[m->profUsed[phase]], m->stream);
 }
 PhaseTimer::~PhaseTimer() {
-    if (!on) return;
+    if (!on || !timed) return;
     cudaEventRecord(m->profEvents[phase][m->profUsed[phase] + 1], m->stream);
     m->profUsed[phase] += 2;
 }
@@ -2600,6 +2606,7 @@ int svm_model_profile(svm_model* m, int enable) {
     if (!m) return SVM_ERR_ARG;
     if (m->prof) svm::profile_drain(m);
     m->prof = enable != 0;
+    m->profMask = (enable & SVM_PROFILE_ONLY) ? (enable & ((1 << SVM_PHASE_COUNT) - 1)) : 0xff;
     for (int ph = 0; ph < SVM_PHASE_COUNT; ++ph) { m->profMs[ph] = 0; m->profLaunches[ph] = 0; }
     return SVM_OK;
 }

@@ -247,6 +247,9 @@ int svm_model_stream(svm_model* m, void** stream);
 #define SVM_PHASE_T1APPLY 4    /* ordered T1 flips (parallel pass, sequential replay, patch: 3 kernels) */
 #define SVM_PHASE_MOVE 5       /* standalone moves and velocity-Verlet drift */
 #define SVM_PHASE_COUNT 6
+/* enable: 0 off, 1 every phase; SVM_PROFILE_ONLY | (1 << phase) | ... brackets only the phases named
+ * (each pair of events adds a little time to the step) and counts the launches of all of them. */
+#define SVM_PROFILE_ONLY 0x100
 int svm_model_profile(svm_model* m, int enable);
 int svm_model_profile_read(svm_model* m, double* msPerPhase, int* launchesPerPhase);
 
