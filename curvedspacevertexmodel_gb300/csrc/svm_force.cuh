@@ -23,7 +23,7 @@ struct ForceArgs {
     const double2* ap;
     const double2* pref;
     double Kr, R;
-    int vec;   // SVM_PRECISION_FP64_VECTOR: the exact gradient as vectors (vertex_force_vec)
+    int vec;   // SVM_PRECISION_FP64_VECTOR: the exact gradient as vectors (grad_geo_vec, grad_tri_vec)
 };
 
 __device__ __forceinline__ int comp(const int4& a, int s) { return s == 0 ? a.x : (s == 1 ? a.y : a.z); }
@@ -47,80 +47,21 @@ __device__ __forceinline__ D3 grad_tri_vec(D3 a, D3 beta, D3 gamma, double R) {
     return scl3(R, sub3(g, scl3(dot3(g, a), a)));
 }
 
-// The same force as vertex_force (the negative energy gradient) with well-conditioned vector
-// formulas; the reference's formulas below lose digits for short edges and thin fan triangles.
-__device__ __forceinline__ D3 vertex_force_vec(const ForceArgs& A, int v) {
-    const D3 P = ld3(A.pos, v);
-    const double inv = f64_div(1.0, f64_sqrt(dot3(P, P)));
-    const D3 a = scl3(inv, P);
-    const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
-    D3 f{0.0, 0.0, 0.0};
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-        const int c = comp(cells, s);
-        const D3 dc = sub3(ld3(A.cellPos, c), P);
-        const D3 dl = sub3(ld3(A.pos, comp(lasts, s)), P), dx = sub3(ld3(A.pos, comp(nexts, s)), P);
-        const double2 apc = A.ap[c], pr = A.pref[c];
-        const double pp = 2.0 * (apc.y - pr.y), aa = 2.0 * A.Kr * (apc.x - pr.x);
-        const D3 bl = scl3(inv, dl), bc = scl3(inv, dc), bx = scl3(inv, dx);
-        const D3 fs = add3(scl3(-pp, add3(grad_geo_vec(a, dl), grad_geo_vec(a, dx))),
-                           scl3(-aa, add3(grad_tri_vec(a, bl, bc, A.R), grad_tri_vec(a, bc, bx, A.R))));
-        if (!isnan(fs.x)) f = add3(f, fs);
-    }
-    return f;
-}
-
-__device__ __forceinline__ D3 vertex_force(const ForceArgs& A, int v) {
-    if (A.vec) return vertex_force_vec(A, v);
-    const D3 p = ld3(A.pos, v);
-    const double4_32a sv = A.vsph[v];
-    const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
-    // The ring predecessors (and successors) of v in its three cells are its three neighbours, so
-    // each neighbour's geodesic gradient serves two cells: evaluated once per neighbour, keyed by
-    // the neighbours' order in `lasts` (a successor is found among them).
-    D3 gG[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) gG[j] = from_basis(sv, grad_geodesic(sv, A.vsph[comp(lasts, j)]));
-    D3 f{0.0, 0.0, 0.0};
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-        const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
-        const D3 cp = ld3(A.cellPos, c);
-        const double4_32a sc = A.cellSph[c];
-        const double2 apc = A.ap[c], pr = A.pref[c];
-        const double dA = apc.x - pr.x, dP = apc.y - pr.y;
-        const D3 pl = ld3(A.pos, L), px = ld3(A.pos, X);
-        const double4_32a sl = A.vsph[L], sx = A.vsph[X];
-        const double pp = 2.0 * dP;
-        const double aa = 2.0 * A.Kr * dA;
-        const int jx = X == lasts.x ? 0 : (X == lasts.y ? 1 : (X == lasts.z ? 2 : -1));
-        D3 fs{0.0, 0.0, 0.0}, t;
-        t = gG[s];
-        fs = sub3(fs, scl3(pp, t));
-        t = jx >= 0 ? pick3(gG, jx) : from_basis(sv, grad_geodesic(sv, sx));
-        fs = sub3(fs, scl3(pp, t));
-        t = from_basis(sv, grad_triangle(sv, sl, sc, p, pl, cp, A.R));
-        fs = sub3(fs, scl3(aa, t));
-        t = from_basis(sv, grad_triangle(sv, sc, sx, p, cp, px, A.R));
-        fs = sub3(fs, scl3(aa, t));
-        if (!isnan(fs.x)) f = add3(f, fs);
-    }
-    return f;
-}
-
 // The geodesic-length gradient at v towards its ring predecessor in cell slot s, in Cartesian
-// form: vertex_force's gG[s].  Each neighbour of v is the predecessor in one of its cells and the
-// successor in another, so the three of them cover both terms of every slot.
+// form.  Each neighbour of v is the predecessor in one of its cells and the successor in another,
+// so the three of them cover both geodesic terms of every slot, each evaluated once.
 __device__ __forceinline__ D3 slot_geodesic(const ForceArgs& A, int v, int s) {
     const double4_32a sv = A.vsph[v];
     return from_basis(sv, grad_geodesic(sv, A.vsph[comp(A.vlast[v], s)]));
 }
 
-// The contribution of cell slot s to the force on vertex v: one term of vertex_force's (or
-// vertex_force_vec's) sum, with the same operations, so that summing the three terms in slot order
-// and skipping a NaN term, as those functions do, gives the same force bit for bit.  Lets three
-// threads share a vertex (more warps in flight when the vertex count is small).  gG: the vertex's
-// three slot_geodesic values (reference form only).
+// The contribution of cell slot s to the force on vertex v: the fSet term of the header's sum for
+// the vertex's cell s, which block_slot_force adds in slot order, skipping a NaN term, as the
+// reference's loop over the three cells does.  Three threads share a vertex (more warps in flight
+// when the vertex count is small).  gG: the vertex's three slot_geodesic values (reference form
+// only).  The vector form (A.vec: the exact gradient as vectors, well conditioned where the
+// reference's closed forms lose digits -- short edges, thin fan triangles) uses grad_geo_vec and
+// grad_tri_vec on the position differences instead.
 __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s, const D3* gG) {
     const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
     const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
