@@ -488,6 +488,7 @@ struct svm_model {
         double T = 0, dt = 0, mu = 0;
         uint64_t seed = 0;
         const void *in = nullptr, *out = nullptr;
+        const void* outDev = nullptr;   // the output's mapped device address the kernels write, or null
         unsigned version = ~0u;
         int precision = -1;
     } ioGraph[2];

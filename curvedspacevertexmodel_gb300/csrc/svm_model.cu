@@ -2726,7 +2726,8 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
         double* hostOut = io_mapped_out(m, posOut);
         auto& g = m->ioGraph[m->cur];
         const bool reuse = g.exec && g.T == T && g.dt == dt && g.mu == mu && g.seed == seed && g.in == posIn &&
-                           g.out == posOut && g.version == m->paramsVersion && g.precision == m->precision;
+                           g.out == posOut && g.outDev == hostOut && g.version == m->paramsVersion &&
+                           g.precision == m->precision;
         const int cur0 = m->cur;
         if (!reuse) {
             if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
@@ -2739,7 +2740,7 @@ int svm_brownian_step_io(svm_model* m, double T, double dt, double mu, uint64_t 
             ce = cudaGraphInstantiate(&g.exec, graph, 0);
             cudaGraphDestroy(graph);
             if (ce != cudaSuccess) { g.exec = nullptr; return SVM_ERR_CUDA; }
-            g.T = T; g.dt = dt; g.mu = mu; g.seed = seed; g.in = posIn; g.out = posOut;
+            g.T = T; g.dt = dt; g.mu = mu; g.seed = seed; g.in = posIn; g.out = posOut; g.outDev = hostOut;
             g.version = m->paramsVersion; g.precision = m->precision;
         }
         SVM_CUDA(cudaGraphLaunch(g.exec, m->stream));
