@@ -35,20 +35,26 @@ struct D3 { double x, y, z; };
 // Division and square root of the FP64 kernels.  Both are the IEEE correctly rounded operations
 // either way; by default they run on the integer and FP32 pipes (svm_softf64.cuh), which leaves
 // GB300's FP64 pipe -- 2 lanes per clock per SM, the bound of these kernels -- to the products and
-// sums, where a hardware division or square root would take about eight FP64 instructions.  A build
-// with -DSVM_NATIVE_FP64_DIV uses the hardware sequences (same results).
+// sums, where a hardware division or square root would take about eight FP64 instructions.  kHw
+// (the T1 pass's kernels, where one warp's chain of dependent operations, not the FP64 pipe's
+// issue rate, sets the time) takes the hardware sequences, whose latency is shorter; so does a
+// build with -DSVM_NATIVE_FP64_DIV.  The results are the same bits.
+template <bool kHw = false>
 __device__ __forceinline__ double f64_div(double a, double b) {
 #ifdef SVM_NATIVE_FP64_DIV
     return __ddiv_rn(a, b);
 #else
-    return sf::div(a, b);
+    if constexpr (kHw) return __ddiv_rn(a, b);
+    else return sf::div(a, b);
 #endif
 }
+template <bool kHw = false>
 __device__ __forceinline__ double f64_sqrt(double a) {
 #ifdef SVM_NATIVE_FP64_DIV
     return __dsqrt_rn(a);
 #else
-    return sf::sqrt(a);
+    if constexpr (kHw) return __dsqrt_rn(a);
+    else return sf::sqrt(a);
 #endif
 }
 
@@ -106,17 +112,25 @@ __device__ __forceinline__ D3 cross3(D3 p1, D3 p2) {          // inc/functions.h
 // The corner phase (k_edges' cross products and arcs, the included angles' products): 0.159 -> 0.151 ms;
 // the norms ahead of the centroids', vertices' and fan triangles' square roots: cells and fallback
 // phases 2-3% shorter.
-__device__ __forceinline__ double early_mul(double x, double y) { return sf::mul(x, y); }
+// (kHw: the hardware multiply, for the T1 pass's latency-bound chains.)
+template <bool kHw = false>
+__device__ __forceinline__ double early_mul(double x, double y) {
+    if constexpr (kHw) return __dmul_rn(x, y);
+    else return sf::mul(x, y);
+}
 // dot3 and cross3 with their products on the integer pipes (the same bits)
+template <bool kHw = false>
 __device__ __forceinline__ double dot3e(D3 a, D3 b) {
-    double s = early_mul(a.x, b.x);
-    s += early_mul(a.y, b.y);
-    s += early_mul(a.z, b.z);
+    double s = early_mul<kHw>(a.x, b.x);
+    s += early_mul<kHw>(a.y, b.y);
+    s += early_mul<kHw>(a.z, b.z);
     return s;
 }
+template <bool kHw = false>
 __device__ __forceinline__ D3 cross3e(D3 p1, D3 p2) {
-    return D3{early_mul(p1.y, p2.z) - early_mul(p1.z, p2.y), early_mul(p1.z, p2.x) - early_mul(p1.x, p2.z),
-              early_mul(p1.x, p2.y) - early_mul(p1.y, p2.x)};
+    return D3{early_mul<kHw>(p1.y, p2.z) - early_mul<kHw>(p1.z, p2.y),
+              early_mul<kHw>(p1.z, p2.x) - early_mul<kHw>(p1.x, p2.z),
+              early_mul<kHw>(p1.x, p2.y) - early_mul<kHw>(p1.y, p2.x)};
 }
 __device__ __forceinline__ double det3(D3 a, D3 b, D3 c) {    // a . (b x c), sphericalDomain.h:123-125
     return a.x * (b.y * c.z - b.z * c.y) + a.y * (b.z * c.x - b.x * c.z) + a.z * (b.x * c.y - b.y * c.x);
@@ -134,13 +148,16 @@ __device__ __forceinline__ D3 sphere_move(D3 p, D3 v, double R) {
     return renorm(add3(p, d), R);
 }
 // geodesicDistance (sphericalDomain.h:94-112)
+template <bool kHw = false>
 __device__ __forceinline__ double geodesic(D3 p1, D3 p2, double R) {
     double num = p1.x * p2.x + p1.y * p2.y + p1.z * p2.z;
-    double den = f64_sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * f64_sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
-    return R * svm_acos(f64_div(num, den));
+    double den = f64_sqrt<kHw>(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) *
+                 f64_sqrt<kHw>(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    return R * svm_acos(f64_div<kHw>(num, den));
 }
 // |p| as geodesic and sph_coords evaluate it (same operations, so the same value)
-__device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt(dot3e(p, p)); }
+template <bool kHw = false>
+__device__ __forceinline__ double pos_norm(D3 p) { return f64_sqrt<kHw>(dot3e<kHw>(p, p)); }
 // geodesic with the two norms given (n1 = pos_norm(p1), n2 = pos_norm(p2)): the same value
 __device__ __forceinline__ double geodesic_n(D3 p1, D3 p2, double n1, double n2, double R) {
     return R * svm_acos(f64_div(dot3e(p1, p2), early_mul(n1, n2)));
@@ -179,6 +196,7 @@ __host__ inline void t1_sin2_bracket(double t, double R, double* lo, double* hi)
     *lo = s * s * (1.0 - eps);
     *hi = s * s * (1.0 + eps);
 }
+template <bool kHw = false>
 __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, double cosLo, double cosHi,
                                              double s2Lo, double s2Hi) {
     if (svm_edge::clearly_longer(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, R, t)) return false;
@@ -189,8 +207,9 @@ __device__ __forceinline__ bool shorter_than(D3 p1, D3 p2, double R, double t, d
         if (xx < s2Lo * d && xx > 1e-13 * d) return true;
         if (xx > s2Hi * d) return false;
     }
-    const double den = f64_sqrt(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) * f64_sqrt(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
-    const double c = f64_div(num, den);
+    const double den = f64_sqrt<kHw>(p1.x * p1.x + p1.y * p1.y + p1.z * p1.z) *
+                       f64_sqrt<kHw>(p2.x * p2.x + p2.y * p2.y + p2.z * p2.z);
+    const double c = f64_div<kHw>(num, den);
     if (c > cosHi && c <= 1.0) return true;   // c > 1 (rounding) makes acos NaN: not shorter
     if (c < cosLo) return false;
     return R * svm_acos(c) < t;
@@ -203,10 +222,11 @@ __device__ __forceinline__ float arc32(float4 p, float4 q, float R) {
     return 2.0f * R * asinf(sqrtf(dx * dx + dy * dy + dz * dz) / (2.0f * R));
 }
 // includedAngle (sphericalDomain.h:114-133)
+template <bool kHw = false>
 __device__ __forceinline__ double included_angle(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
-    double a = svm_acos(f64_div(-dot3(ci, cim1), f64_sqrt(dot3(ci, ci)) * f64_sqrt(dot3(cim1, cim1))));
+    double a = svm_acos(f64_div<kHw>(-dot3(ci, cim1), f64_sqrt<kHw>(dot3(ci, ci)) * f64_sqrt<kHw>(dot3(cim1, cim1))));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
     return a;
@@ -235,10 +255,11 @@ __device__ __forceinline__ T pick3(const T* a, int j) { return j == 0 ? a[0] : (
 // slot of vertex u among the three neighbour slots nb (-1 if absent)
 __device__ __forceinline__ int nbr_slot(int4 nb, int u) { return u == nb.x ? 0 : (u == nb.y ? 1 : (u == nb.z ? 2 : -1)); }
 // included_angle with the cosine clamped to [-1, 1] (the mixed form)
+template <bool kHw = false>
 __device__ __forceinline__ double included_angle_clamped(D3 p1, D3 p2, D3 p3) {
     D3 ci = cross3(p2, p3), cim1 = cross3(p1, p2);
     double det = det3(p1, p2, p3);
-    double c = f64_div(-dot3(ci, cim1), f64_sqrt(dot3(ci, ci)) * f64_sqrt(dot3(cim1, cim1)));
+    double c = f64_div<kHw>(-dot3(ci, cim1), f64_sqrt<kHw>(dot3(ci, ci)) * f64_sqrt<kHw>(dot3(cim1, cim1)));
     double a = svm_acos(fmin(1.0, fmax(-1.0, c)));
     if (det > 0) a = -a;
     if (a < 0) a += 2. * kPI;
@@ -264,13 +285,15 @@ __device__ __forceinline__ double triangle_area_unit(D3 p1, D3 p2, D3 p3, double
 // Spherical coordinates of a point as the reference's gradients compute them
 // (sphericalDomain.h:218-232, 251-261): cos t = z/|p|, sin t = sqrt(1 - cos^2 t),
 // cos p = x / sqrt(x^2+y^2), sin p = y / sqrt(x^2+y^2).
+template <bool kHw = false>
 __device__ __forceinline__ double4_32a sph_coords_n(D3 p, double r) {  // r = pos_norm(p)
-    double cosT = f64_div(p.z, r);
-    double sinT = f64_sqrt(1. - cosT * cosT);
-    double rxy = f64_sqrt(early_mul(p.x, p.x) + early_mul(p.y, p.y));
-    return make_double4_32a(cosT, sinT, f64_div(p.x, rxy), f64_div(p.y, rxy));
+    double cosT = f64_div<kHw>(p.z, r);
+    double sinT = f64_sqrt<kHw>(1. - cosT * cosT);
+    double rxy = f64_sqrt<kHw>(early_mul<kHw>(p.x, p.x) + early_mul<kHw>(p.y, p.y));
+    return make_double4_32a(cosT, sinT, f64_div<kHw>(p.x, rxy), f64_div<kHw>(p.y, rxy));
 }
-__device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n(p, pos_norm(p)); }
+template <bool kHw = false>
+__device__ __forceinline__ double4_32a sph_coords(D3 p) { return sph_coords_n<kHw>(p, pos_norm<kHw>(p)); }
 
 // gradientGeodesicDistance (sphericalDomain.h:248-273) in the (theta, phi) basis of v1:
 // returns (d/dtheta, d/dphi) components.

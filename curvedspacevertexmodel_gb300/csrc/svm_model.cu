@@ -473,7 +473,7 @@ __global__ void k_t1_test(const double4_32a* __restrict__ pos, const float4* __r
         const int u = comp(nb, s);
         if (!(v < u)) continue;
         const bool shortEdge = pos32 ? arc32(pos32[v], pos32[u], (float)repR[rep_of(pos32[v])]) < (float)t1Threshold
-                                     : shorter_than(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi, s2Lo, s2Hi);
+                                     : shorter_than<true>(ld3(pos, v), ld3(pos, u), R, t1Threshold, cosLo, cosHi, s2Lo, s2Hi);
         if (shortEdge) {
             const int q = 3 * v + s;
             atomicOr(&t1.bits[q >> 5], 1u << (q & 31));
@@ -572,9 +572,9 @@ __device__ __forceinline__ D3 rodrigues(D3 v, D3 k, double c, double s) {
               __dadd_rn(__dadd_rn(__dmul_rn(c, v.y), __dmul_rn(s, cp.y)), __dmul_rn(w, k.y)),
               __dadd_rn(__dadd_rn(__dmul_rn(c, v.z), __dmul_rn(s, cp.z)), __dmul_rn(w, k.z))};
 }
-__device__ __forceinline__ D3 renorm_exact(D3 p, double R) {
+__device__ __forceinline__ D3 renorm_exact(D3 p, double R) {  // the T1 moves: hardware sequences
     const double pp = __dadd_rn(__dadd_rn(__dmul_rn(p.x, p.x), __dmul_rn(p.y, p.y)), __dmul_rn(p.z, p.z));
-    const double inv = f64_div(1.0, f64_sqrt(pp));
+    const double inv = f64_div<true>(1.0, f64_sqrt<true>(pp));
     return D3{__dmul_rn(R, __dmul_rn(inv, p.x)), __dmul_rn(R, __dmul_rn(inv, p.y)), __dmul_rn(R, __dmul_rn(inv, p.z))};
 }
 
@@ -940,10 +940,10 @@ __global__ void k_t1_patch(ApplyArgs A, T1Scratch t1) {
             if (A.hostOut && !hostAll) { A.hostOut[3L * u] = p.x; A.hostOut[3L * u + 1] = p.y; A.hostOut[3L * u + 2] = p.z; }
             if (A.pos32) {
                 A.corner[(long)cell * A.Wc + k] =
-                    make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped(pl, p, px));
+                    make_double2((double)arc32(A.pos32[last], A.pos32[u], (float)aR(A, u)), included_angle_clamped<true>(pl, p, px));
             } else {
-                A.corner[(long)cell * A.Wc + k] = make_double2(geodesic(pl, p, A.R), included_angle(pl, p, px));
-                A.vsph[u] = sph_coords(p);
+                A.corner[(long)cell * A.Wc + k] = make_double2(geodesic<true>(pl, p, A.R), included_angle<true>(pl, p, px));
+                A.vsph[u] = sph_coords<true>(p);
             }
         }
         __syncthreads();
@@ -979,7 +979,7 @@ __device__ __forceinline__ bool t1_short(const ApplyArgs& A, const TPos& a, cons
     if (A.pos32)
         return arc32(make_float4((float)a.x, (float)a.y, (float)a.z, 0.f), make_float4((float)b.x, (float)b.y, (float)b.z, 0.f),
                      (float)A.repR[a.rep]) < (float)A.t1Threshold;
-    return shorter_than(D3{a.x, a.y, a.z}, D3{b.x, b.y, b.z}, A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
+    return shorter_than<true>(D3{a.x, a.y, a.z}, D3{b.x, b.y, b.z}, A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
 }
 
 __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
@@ -987,7 +987,7 @@ __device__ __forceinline__ bool t1_candidate(const ApplyArgs& A, int q) {
     const int u = compRef(A.vnbr, v, s);
     if (!(v < u)) return false;
     if (A.pos32) return arc32(A.pos32[v], A.pos32[u], (float)aR(A, v)) < (float)A.t1Threshold;
-    return shorter_than(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
+    return shorter_than<true>(ld3(A.pos, v), ld3(A.pos, u), A.R, A.t1Threshold, A.cosLo, A.cosHi, A.s2Lo, A.s2Hi);
 }
 
 // Applies the flagged T1 flips in the order of the CPU loop (ascending vertex1, then slot),
