@@ -62,10 +62,14 @@ __device__ __forceinline__ D3 slot_geodesic(const ForceArgs& A, int v, int s) {
 // only).  The vector form (A.vec: the exact gradient as vectors, well conditioned where the
 // reference's closed forms lose digits -- short edges, thin fan triangles) uses grad_geo_vec and
 // grad_tri_vec on the position differences instead.
+// The force form of a kernel: chosen per launch from A.vec (kFormAny), or fixed at compile time, which
+// lets a kernel that runs one form drop the other's registers.
+constexpr int kFormAny = 0, kFormVector = 1, kFormReference = 2;
+template <int kForm = kFormAny>
 __device__ __forceinline__ D3 slot_force(const ForceArgs& A, int v, int s, const D3* gG) {
     const int4 cells = A.vcell[v], lasts = A.vlast[v], nexts = A.vnext[v];
     const int c = comp(cells, s), L = comp(lasts, s), X = comp(nexts, s);
-    if (A.vec) {
+    if (kForm == kFormVector || (kForm == kFormAny && A.vec)) {
         const D3 P = ld3(A.pos, v);
         const double inv = f64_div(1.0, f64_sqrt(dot3(P, P)));
         const D3 a = scl3(inv, P);
@@ -112,11 +116,13 @@ constexpr int kSlotVerts = 64;
 // likewise).  Blocks of 32 vertices (six per SM) measured no faster at 20k or 100k cells.
 constexpr int kSlotMinBlocks = 3;
 struct SlotShared { double x[3 * kSlotVerts], y[3 * kSlotVerts], z[3 * kSlotVerts]; };
+template <int kForm = kFormAny>
 __device__ __forceinline__ D3 block_slot_force(const ForceArgs& A, int nV, SlotShared& sh) {
+    const bool vec = kForm == kFormVector || (kForm == kFormAny && A.vec);
     const int t = threadIdx.x, base = blockIdx.x * kSlotVerts;
     const int vi = t / 3, s = t - 3 * (t / 3);
     const int v = base + vi;
-    if (!A.vec) {
+    if (!vec) {
         if (v < nV) {
             const D3 g = slot_geodesic(A, v, s);
             sh.x[t] = g.x; sh.y[t] = g.y; sh.z[t] = g.z;
@@ -126,10 +132,10 @@ __device__ __forceinline__ D3 block_slot_force(const ForceArgs& A, int nV, SlotS
     D3 fs{0.0, 0.0, 0.0};
     if (v < nV) {
         D3 gG[3];
-        if (!A.vec)
+        if (!vec)
 #pragma unroll
             for (int j = 0; j < 3; ++j) gG[j] = D3{sh.x[3 * vi + j], sh.y[3 * vi + j], sh.z[3 * vi + j]};
-        fs = slot_force(A, v, s, gG);
+        fs = slot_force<kForm>(A, v, s, gG);
     }
     __syncthreads();
     if (v < nV) { sh.x[t] = fs.x; sh.y[t] = fs.y; sh.z[t] = fs.z; }
