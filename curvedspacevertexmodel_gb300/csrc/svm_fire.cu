@@ -4,7 +4,8 @@
 // 122-200) and velocityVerlet::integrateEOMCPU (src/updaters/velocityVerlet.cpp:6-38).  One
 // iteration is
 //   k_fire_vv1     per vertex: the previous iteration's FIRE velocity update, then
-//                  disp = dt v + dt^2/2 F, v += dt/2 F / m, move onto the sphere (in place)
+//                  disp = dt v + dt^2/2 F, v += dt/2 F / m, move onto the sphere (in place), and
+//                  the moved vertex's norm for the corner pass
 //   [T1]           unless motion is restricted
 //   geometry       k_corners, k_cells, k_fallback
 //   k_fire_force   per vertex: F, v += dt/2 F / m, block partials of F.v, F.F, v.v, max |F|^2;
@@ -91,14 +92,16 @@ __device__ __forceinline__ D3 fire_velocity(const FireState& S, D3 v, D3 f) {
 // velocityVerlet::integrateEOMCPU's first loop for one vertex (velocityVerlet.cpp:14-20: unit
 // masses, the model's masses being 1): disp = dt v + (dt^2 / 2) F, v += (dt / 2) F, then the move
 // onto the sphere (moveParticles).  Products rounded before the sums, as on the CPU.
-__device__ __forceinline__ void vv_drift(double4_32a* __restrict__ pos, double4_32a* __restrict__ vel, int i, D3 v,
-                                         D3 f, double dt, double R) {
+__device__ __forceinline__ void vv_drift(double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                                         double* __restrict__ vnorm, int i, D3 v, D3 f, double dt, double R) {
     const double hv = (0.5 / 1.0) * dt, h2 = 0.5 * dt * dt;
     const D3 d{__dadd_rn(__dmul_rn(dt, v.x), __dmul_rn(h2, f.x)), __dadd_rn(__dmul_rn(dt, v.y), __dmul_rn(h2, f.y)),
                __dadd_rn(__dmul_rn(dt, v.z), __dmul_rn(h2, f.z))};
     v = D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
     st3(vel, i, v);
-    st3(pos, i, move_exact_f(ld3(pos, i), d, R));
+    const D3 q = move_exact_f(ld3(pos, i), d, R);
+    st3(pos, i, q);
+    vnorm[i] = pos_norm(q);  // k_vnorm's value, for the corner pass that follows
 }
 // gpu_update_velocity (velocityVerlet.cu): v += (dt / 2) F / m with unit masses.
 __device__ __forceinline__ D3 vv_kick(D3 v, D3 f, double dt) {
@@ -106,24 +109,33 @@ __device__ __forceinline__ D3 vv_kick(D3 v, D3 f, double dt) {
     return D3{__dadd_rn(v.x, __dmul_rn(hv, f.x)), __dadd_rn(v.y, __dmul_rn(hv, f.y)), __dadd_rn(v.z, __dmul_rn(hv, f.z))};
 }
 
+// The iteration's first kernel.  It leaves the pending flag as it is: the control of every iteration
+// (k_fire_force's last block) sets it again before this kernel next reads it, and after the last
+// iteration k_fire_finish applies the update it stands for.  Once FIRE has stopped, the positions
+// stay and only their norms are written (the corner pass of a batch's remaining iterations reads them).
 __global__ void k_fire_vv1(const FireState* __restrict__ Sp, double4_32a* __restrict__ pos,
-                           double4_32a* __restrict__ vel, const double4_32a* __restrict__ force, int nV, double R) {
+                           double4_32a* __restrict__ vel, const double4_32a* __restrict__ force,
+                           double* __restrict__ vnorm, int nV, double R) {
     const FireState S = *Sp;
-    if (S.done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nV) return;
+    if (S.done) {
+        vnorm[i] = pos_norm(ld3(pos, i));
+        return;
+    }
     const D3 f = ld3(force, i);
     D3 v = ld3(vel, i);
     if (S.pending) v = fire_velocity(S, v, f);
-    vv_drift(pos, vel, i, v, f, S.dt, R);
+    vv_drift(pos, vel, vnorm, i, v, f, S.dt, R);
 }
 
 // The standalone velocity-Verlet drift: vv_drift with the caller's dt.
 __global__ void k_vv_drift(double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
-                           const double4_32a* __restrict__ force, int nV, double dt, double R) {
+                           const double4_32a* __restrict__ force, double* __restrict__ vnorm, int nV, double dt,
+                           double R) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nV) return;
-    vv_drift(pos, vel, i, ld3(vel, i), ld3(force, i), dt, R);
+    vv_drift(pos, vel, vnorm, i, ld3(vel, i), ld3(force, i), dt, R);
 }
 __global__ void k_vv_half(double4_32a* __restrict__ vel, const double4_32a* __restrict__ force, int nV, double dt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -198,11 +210,6 @@ __device__ void fire_reduce_tail(FireState* __restrict__ Sp, double P, double FF
     *Sp = S;
 }
 
-// Clears the pending flag after the first vertex kernel of an iteration has consumed it.
-__global__ void k_fire_consume(FireState* S) {
-    if (!S->done) S->pending = 0;
-}
-
 // Blocks of 3 kSlotVerts threads: three per vertex for the force (one per cell slot), then the
 // first kSlotVerts threads finish their vertex.  One instantiation per force form: the vector form
 // alone fits 78 registers without spill, so four blocks per SM (a 40k-vertex sphere's 625 blocks in
@@ -266,13 +273,12 @@ int fire_iteration(svm_fire* F) {
     const int bs = spread_block(m, m->nVertices), nb = (m->nVertices + bs - 1) / bs;
     {
         PhaseTimer pt(m, SVM_PHASE_MOVE);
-        k_fire_vv1<<<nb, bs, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->nVertices, m->R);
-        k_fire_consume<<<1, 1, 0, m->stream>>>(F->d);
+        k_fire_vv1<<<nb, bs, 0, m->stream>>>(F->d, m->pos[m->cur], m->vel, m->force, m->vnorm, m->nVertices, m->R);
     }
     m->cornersValid = false;
     int rc;
     if (!m->restricted) {
-        rc = launch_corners(m, true);
+        rc = launch_corners(m, true, /*vnormReady=*/true);
         if (rc) return rc;
         rc = launch_t1_apply(m, 0);
         if (rc) return rc;
@@ -422,12 +428,12 @@ int svm_velocity_verlet_step(svm_model* m, double dt, int nSteps) {
     for (int k = 0; k < nSteps; ++k) {
         {
             PhaseTimer pt(m, SVM_PHASE_MOVE);
-            k_vv_drift<<<nb, bs, 0, m->stream>>>(m->pos[m->cur], m->vel, m->force, m->nVertices, dt, m->R);
+            k_vv_drift<<<nb, bs, 0, m->stream>>>(m->pos[m->cur], m->vel, m->force, m->vnorm, m->nVertices, dt, m->R);
         }
         m->cornersValid = false;
         int rc;
         if (!m->restricted) {  // moveParticles -> enforceTopology (sphericalVertexModel.cpp:111-148)
-            rc = launch_corners(m, true);
+            rc = launch_corners(m, true, /*vnormReady=*/true);
             if (rc) return rc;
             rc = launch_t1_apply(m, 0);
             if (rc) return rc;

@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force(ForceA
 }
 
 // Fused Brownian step for one vertex: force, displacement, move; reads `A.pos`, writes posNext (and
-// hostOut, when non-null).
+// hostOut, when non-null).  (Writing the moved vertex's norm here as well, which would spare the
+// corner pass its k_vnorm, made this FP64-bound kernel as much slower as the corner pass got faster.)
 template <int kNoise>
 __global__ void __launch_bounds__(3 * kSlotVerts, kSlotMinBlocks) k_force_bd(
                                                              ForceArgs A, int nV, double4_32a* __restrict__ force,

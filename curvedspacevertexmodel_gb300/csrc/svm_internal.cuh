@@ -531,7 +531,9 @@ struct PhaseTimer {
 };
 // launch helpers shared across translation units (svm_model.cu)
 int launch_geometry(svm_model* m);
-int launch_corners(svm_model* m, bool t1test);
+// vnormReady: the kernel that last moved every vertex also wrote its norm (pos_norm) to m->vnorm, so
+// the corner pass skips k_vnorm.
+int launch_corners(svm_model* m, bool t1test, bool vnormReady = false);
 int launch_t1_apply(svm_model* m, int bump);
 int grow_rings(svm_model* m, int newCapacity);
 // Threads per block for a one-thread-per-item FP64 kernel over n items: the largest of 256, 128, 64

@@ -1802,15 +1802,16 @@ static ApplyArgs apply_args(svm_model* m, int bump) {
     return A;
 }
 
-int launch_corners(svm_model* m, bool t1test) {
-    PhaseTimer pt(m, SVM_PHASE_CORNERS, m->precision == SVM_PRECISION_MIXED ? 1 : 3);  // FP64: k_vnorm, k_edges, k_corner
+int launch_corners(svm_model* m, bool t1test, bool vnormReady) {
+    // FP64: k_vnorm (unless the moving kernel wrote the norms), k_edges, k_corner
+    PhaseTimer pt(m, SVM_PHASE_CORNERS, m->precision == SVM_PRECISION_MIXED ? 1 : (vnormReady ? 2 : 3));
     if (m->precision == SVM_PRECISION_MIXED) {
         m->cornersValid = true;
         return m->nRep > 1 ? batch_tuned_corners(m, t1test) : mixed_launch_corners(m, t1test);
     }
     if (!m->edgeC) return SVM_ERR_ARG;  // FP64 corners exist for single spheres only
     const int bv = spread_block(m, m->nVertices);
-    k_vnorm<<<blocksFor(m->nVertices, bv), bv, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
+    if (!vnormReady) k_vnorm<<<blocksFor(m->nVertices, bv), bv, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->nVertices);
     k_edges<<<blocksFor(m->nVertices, bv), bv, 0, m->stream>>>(m->pos[m->cur], m->vnorm, m->vsph, m->vnbr, m->edgeC,
                                                               m->edgeArc, m->nVertices, m->R, t1test ? 1 : 0,
                                                               m->t1Threshold, m->t1);
