@@ -226,10 +226,17 @@ def cpu_baseline_sample(state, steps: int):
 
 
 # --------------------------------------------------------------------------------------------
+def rank_visible_devices(local: int, visible):
+    """CUDA_VISIBLE_DEVICES for local rank `local`: its own entry of an inherited device list (a
+    launcher may export every GPU of the node), else the device with the rank's number."""
+    devs = [d.strip() for d in visible.split(",") if d.strip()] if visible else []
+    return devs[local % len(devs)] if devs else str(local)
+
+
 def run_ours(args):
     rank, world, local = dist_env()
-    if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    if world > 1:  # one GPU per rank, seen by the rank as device 0
+        os.environ["CUDA_VISIBLE_DEVICES"] = rank_visible_devices(local, os.environ.get("CUDA_VISIBLE_DEVICES"))
     import numpy as np
     import torch
     import curvedspacevertexmodel_gb300 as svm

@@ -75,3 +75,16 @@ def test_fp64_roofline_arithmetic():
     assert abs(r["peak"] - 629.28) < 1e-9
     assert abs(r["achieved"] - 1420 * 199996 / 0.6e-3 / 1e9) < 1e-9
     assert 0.7 < r["frac"] < 0.8
+
+
+def test_each_rank_gets_its_own_gpu():
+    """Under torchrun every rank sees one GPU as device 0: its own entry of an inherited device list
+    (a launcher may export all of the node's GPUs), or the GPU with its local rank's number."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.rank_visible_devices(3, None) == "3"
+    assert bench.rank_visible_devices(3, "") == "3"
+    assert bench.rank_visible_devices(3, "0,1,2,3,4,5,6,7") == "3"
+    assert bench.rank_visible_devices(1, "4,5") == "5"
+    assert bench.rank_visible_devices(0, "6") == "6"
+    assert bench.rank_visible_devices(2, " 2, 3, 4 ") == "4"
