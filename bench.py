@@ -822,6 +822,31 @@ def mode_large(args):
                        "area_fallback_taken_last_step": bool(m.areaCheck()[2])}
     m.computeGeometry()
     out["brownian"]["energy_per_cell"] = m.computeEnergy() / m.nCells
+    # ensemble error bars: from the same state, 10 blocks of 200 steps in each form (the FP64 form with
+    # its own noise stream), the energy per cell after every block; mean and standard error of each,
+    # and their difference in combined standard errors
+    if args.ensemble_blocks > 0:
+        state = m.saveState()
+        ens = {}
+        for form in ("mixed", "fp64"):
+            m.precision = "fp64"   # the state goes in through the FP64 form, then the form is chosen
+            m.loadState(state)
+            m.precision = form
+            series = []
+            for _ in range(args.ensemble_blocks):
+                bd.run(200)
+                m.computeGeometry()
+                series.append(m.computeEnergy() / m.nCells)
+            ens[form] = _mean_se(series)
+        (mm, sm), (mf, sf) = ens["mixed"], ens["fp64"]
+        out["ensemble_energy_per_cell"] = {
+            "mixed": [mm, sm], "fp64": [mf, sf], "relative_difference": (mm - mf) / mf,
+            "difference_over_combined_se": (mm - mf) / max(1e-300, (sm * sm + sf * sf) ** 0.5),
+            "blocks": f"{args.ensemble_blocks} blocks of 200 steps from the same state after the timed run, "
+                      "energy per cell after each block"}
+        m.precision = "fp64"
+        m.loadState(state)
+        m.precision = "mixed"
     if args.fire_cap > 0:
         m.precision = "fp64_vector"
         start = m.saveState()
@@ -1207,6 +1232,8 @@ def main():
     ap.add_argument("--every", type=int, default=1000, help="forms: checkpoint interval")
     ap.add_argument("--compare-steps", type=int, default=2000, help="batch: steps of the FP64 trajectory comparison")
     ap.add_argument("--fire-cap", type=int, default=12000, help="large: FIRE iteration cap (0: no FIRE)")
+    ap.add_argument("--ensemble-blocks", type=int, default=10,
+                    help="large: blocks of 200 steps per form for the energy error bars (0: none)")
     ap.add_argument("--mixed", action="store_true", help="profile: the steps in the mixed form")
     ap.add_argument("--fire", type=int, default=0, help="profile: FIRE iterations after the steps")
     ap.add_argument("--fire-form", default="fp64_vector", choices=("fp64", "fp64_vector"),
