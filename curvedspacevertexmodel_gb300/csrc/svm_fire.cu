@@ -6,8 +6,9 @@
 //   k_fire_vv1     per vertex: the previous iteration's FIRE velocity update, then
 //                  disp = dt v + dt^2/2 F, v += dt/2 F / m, move onto the sphere (in place), and
 //                  the moved vertex's norm for the corner pass
-//   [T1]           unless motion is restricted
-//   geometry       k_corners, k_cells, k_fallback
+//   corners + T1   unless motion is restricted: k_edges (edge terms and the T1 length test),
+//                  k_corner or k_corner_s, then the T1 pass (k_t1_parallel, k_t1_apply, k_t1_patch)
+//   geometry       k_cells, k_fallback_fan (the corners too when motion is restricted)
 //   k_fire_force   per vertex: F, v += dt/2 F / m, block partials of F.v, F.F, v.v, max |F|^2;
 //                  the last block reduces them in a fixed order and runs the FIRE control
 //                  (power test, dt / alpha adaptation, stopping test)
