@@ -1202,7 +1202,7 @@ def mode_fire_ablation(args):
 
 
 MODE_DEFAULTS = {  # cells, steps, stab, equil, replicas
-    "headline": (N_CELLS, 200, 100, 200, 512),   # 200 steps: the area fallback (~1 step in 5) averages out
+    "headline": (N_CELLS, 200, 100, 200, 512),   # 200 steps: the area fallback (~1 step in 8 to 20) averages out
     "forms": (N_CELLS, 10000, 100, 200, 0),
     "large": (1_000_000, 5000, 100, 0, 0),
     "batch": (0, 10000, 100, 0, 512),
